@@ -1,0 +1,405 @@
+#!/usr/bin/env python3
+"""STRIDE decode benchmark: one JSON line per run.
+
+Workloads (``--workload``):
+  heightfield   (default) one 2049 x 2049 heightfield mesh, 8,388,608
+                triangles, 12-bit bbox quantisation (``--bits``), seeded
+                value-noise heights, encoded by the project encoder.  One step
+                = one decode of the whole stream (parse kernel + decode
+                kernel) into resident device buffers.
+  icosphere     the level-8 displaced icosphere (1,310,720 triangles).
+  batch         many meshes with log-uniform sizes decoded in one persistent
+                launch (CUDA graph), next to per-mesh launches.
+  serve         Poisson arrivals into the continuous-batching server.
+
+Metric: decoded triangles per second (M tris/s).  ``value`` is device time
+of the decode with the stream already in HBM and L2 flushed before every step
+(a 256 MiB write, not timed); ``e2e`` goes through the public
+ParaDeltaV5GpuDecoder API with pinned host buffers (upload, decode, download,
+synchronise each step).  ``roofline`` relates the decode kernel's duration to
+the measured HBM copy bandwidth; ``cpu_baseline`` times the CPU oracle (a C
+restatement of the reference decoder) on all host cores.
+
+``--impl reference`` times the CPU decoder (oracle) alone on the same
+workload and prints the reference line.  Multi-GPU (torchrun): every rank
+decodes its own replica; the step time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+from meshpress_gb300 import encoder, synth  # noqa: E402
+
+WORKLOADS = ("heightfield", "icosphere", "batch", "serve")
+
+
+def parse_args(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--workload", default="heightfield", choices=WORKLOADS)
+    ap.add_argument("--bits", type=int, default=12)
+    ap.add_argument("--grid", type=int, default=2049)
+    ap.add_argument("--tune", type=int, default=1, help="autotune the launch shape before timing")
+    ap.add_argument("--batch-meshes", type=int, default=4096)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args(argv)
+
+
+# ---------------------------------------------------------------------------
+# distributed helpers (replicas only: no data-path collective)
+# ---------------------------------------------------------------------------
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+def dist_init(backend: str):
+    import torch.distributed as dist
+    rank, local, world = dist_env()
+    if world > 1 and not dist.is_initialized():
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group(backend=backend, rank=rank, world_size=world)
+    return rank, local, world
+
+
+def reduce_max(x: float, device=None) -> float:
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()):
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(device=None):
+    import torch.distributed as dist
+    if dist.is_available() and dist.is_initialized():
+        if device is not None:
+            dist.barrier(device_ids=[device.index])
+        else:
+            dist.barrier()
+
+
+def replica_value(units_per_rank: int, world: int, max_seconds: float) -> float:
+    """Whole-job throughput of ``world`` replicas: all units / slowest rank."""
+    return units_per_rank * world / max_seconds
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+def heightfield_stream(n: int, bits: int):
+    V, T = synth.noise_heightfield(n, seed=3)
+    e = encoder.encode(V, T, precision_error=synth.bbox_bits_error(bits), precision_mode="bbox_frac")
+    return e.data, {"workload": f"heightfield_{n}x{n}_{bits}bit", "grid": n, "bits": bits,
+                    "triangles": int(len(T)), "source_vertices": int(len(V)),
+                    "vertices_dup": int(e.n_v_dup), "meshlets": int(e.n_meshlets),
+                    "stream_bytes": len(e.data),
+                    "heights": "seeded 6-octave value noise (seed 3)",
+                    "encoder": "project encoder, fitted IRLP, max_verts=max_tris=256"}
+
+
+def icosphere_stream(bits: int):
+    V, T = synth.icosphere(8, seed=2)
+    e = encoder.encode(V, T, precision_error=synth.bbox_bits_error(bits), precision_mode="bbox_frac")
+    return e.data, {"workload": f"icosphere_L8_{bits}bit", "bits": bits, "triangles": int(len(T)),
+                    "source_vertices": int(len(V)), "vertices_dup": int(e.n_v_dup),
+                    "meshlets": int(e.n_meshlets), "stream_bytes": len(e.data),
+                    "displacement": "5-octave value noise, 5% of radius, seeded vertex shuffle",
+                    "encoder": "project encoder, fitted IRLP, max_verts=max_tris=256"}
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        import tempfile
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        sm = [r[0] for r in rows]
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, burst copy)"
+    return 6800.0, "fallback 6.8 TB/s"
+
+
+def ncu_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch from the committed ncu summary, if any."""
+    path = os.path.join(REPO, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        t = json.load(f)
+    v = t.get(kernel, {}).get(workload)
+    return None if v is None else float(v)
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle (baseline leg only)
+# ---------------------------------------------------------------------------
+def cpu_oracle_rate(data: bytes, n_t: int, min_wall: float = 1.5, max_reps: int = 40):
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    h = oracle.parse_header(data)
+    out = (np.empty((h.n_v_total, 3), np.float32), np.empty((h.n_t, 3), np.int64))
+    oracle.decode_mt(data, cores, out=out)  # warm caches
+    reps = 0
+    t0 = time.perf_counter()
+    while reps < 3 or (time.perf_counter() - t0 < min_wall and reps < max_reps):
+        oracle.decode_mt(data, cores, out=out)
+        reps += 1
+    wall = time.perf_counter() - t0
+    return n_t * reps / wall / 1e6, cores, reps, wall
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the CPU decoder on all host cores
+# ---------------------------------------------------------------------------
+def run_reference(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return 0
+    data, cfg = make_stream(args)
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    h = oracle.parse_header(data)
+    out = (np.empty((h.n_v_total, 3), np.float32), np.empty((h.n_t, 3), np.int64))
+    for _ in range(max(1, args.warmup)):
+        oracle.decode_mt(data, cores, out=out)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        oracle.decode_mt(data, cores, out=out)
+    wall = time.perf_counter() - t0
+    value = h.n_t * args.steps / wall / 1e6
+    line = {
+        "impl": "reference", "metric": "decoded triangles per second", "value": round(value, 3),
+        "unit": "M tris/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(wall / args.steps * 1e3, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32+f64->f32", "data": "synthetic",
+        "config": cfg,
+        "cpu_baseline": {"value": round(value, 3), "unit": "M tris/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full decodes of the stream (C restatement of decode_dup, "
+                                   f"meshlet-parallel over {cores} threads)"},
+        "e2e": {"value": round(value, 3), "unit": "M tris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def make_stream(args):
+    if args.workload == "heightfield":
+        return heightfield_stream(args.grid, args.bits)
+    if args.workload == "icosphere":
+        return icosphere_stream(args.bits)
+    raise ValueError(args.workload)
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def run_single(args):
+    import torch
+    from meshpress_gb300 import ParaDeltaV5GpuDecoder, _lib
+    rank, local, world = dist_init("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    data, cfg = make_stream(args)
+    lib = _lib.load()
+    dec = ParaDeltaV5GpuDecoder(data)
+    n_t, n_v = dec.n_t_total, dec.n_v_total
+    idx = torch.empty((n_t, 3), dtype=torch.int32, device=dev)
+    pos = torch.empty((n_v, 3), dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    sh = ctypes.c_void_p(int(stream.cuda_stream))
+
+    # launch shape: autotune over a one-mesh batch, apply to the handle
+    launch = None
+    if args.tune:
+        from meshpress_gb300.batch import BatchDecoder
+        b = BatchDecoder([data])
+        best, best_ms = b.autotune(iters=3)
+        b.close()
+        dec.set_launch_config(best)
+        launch = dict(best.as_dict(), tuned_ms=round(best_ms, 4))
+
+    # parity before timing: bit-exact against the CPU oracle
+    dec.decode_into(idx, pos)
+    exact = None
+    if rank == 0:
+        import oracle
+        opos, oidx = oracle.decode_mt(data, 0)
+        exact = bool(np.array_equal(pos.cpu().numpy().view(np.uint32), opos.view(np.uint32)) and
+                     np.array_equal(idx.cpu().numpy().view(np.uint32).astype(np.int64), oidx))
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    pms = ctypes.c_float()
+    dms = ctypes.c_float()
+    for _ in range(max(args.warmup, 3)):
+        flush.fill_(1)
+        _lib.check(lib.stride_decode_timed(dec._h, sh, ctypes.c_void_p(idx.data_ptr()),
+                                           ctypes.c_void_p(pos.data_ptr()), ctypes.byref(pms),
+                                           ctypes.byref(dms)), "decode")
+    dec.check()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    parse_ms, decode_ms = [], []
+    clocks = ClockSampler(local)
+    barrier(dev)
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    t_wall = time.perf_counter()
+    for k in range(args.steps):
+        flush.fill_(k & 0xFF)
+        ev[k][0].record(stream)
+        _lib.check(lib.stride_decode_timed(dec._h, sh, ctypes.c_void_p(idx.data_ptr()),
+                                           ctypes.c_void_p(pos.data_ptr()), ctypes.byref(pms),
+                                           ctypes.byref(dms)), "decode")
+        ev[k][1].record(stream)
+        parse_ms.append(pms.value)
+        decode_ms.append(dms.value)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_wall
+    barrier(dev)
+    clk = clocks.stop()
+    dec.check()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    mean_step = reduce_max(sum(step_ms) / len(step_ms), dev)
+    value = replica_value(n_t, world, mean_step / 1e3) / 1e6
+
+    alg_bytes = len(data) + 12 * (n_v + n_t)
+    peak, peak_src = measured_peak()
+    dec_ms = sum(decode_ms) / len(decode_ms)
+    achieved = alg_bytes / (dec_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": ncu_traffic("decode_kernel", cfg["workload"]),
+                "kernel": "decode_kernel", "kernel_ms": round(dec_ms, 4),
+                "parse_kernel_ms": round(sum(parse_ms) / len(parse_ms), 4),
+                "alg_bytes_per_launch": alg_bytes, "peak_source": peak_src,
+                "step_frac": round(alg_bytes / (mean_step / 1e3) / 1e9 / peak, 4)}
+
+    # end to end through the public API with pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        h_blob = torch.empty(len(data), dtype=torch.uint8, pin_memory=True)
+        h_blob.numpy()[:] = np.frombuffer(data, np.uint8)
+        h_pos = torch.empty((n_v, 3), dtype=torch.float32, pin_memory=True)
+        h_idx = torch.empty((n_t, 3), dtype=torch.int32, pin_memory=True)
+        blob_ptr = ctypes.c_void_p(h_blob.data_ptr())
+        for _ in range(2):
+            _lib.check(lib.stride_reload(dec._h, blob_ptr, len(data), sh), "reload")
+            _lib.check(lib.stride_decode_host(dec._h, sh, ctypes.c_void_p(h_idx.data_ptr()),
+                                              ctypes.c_void_p(h_pos.data_ptr())), "decode_host")
+        ts = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            _lib.check(lib.stride_reload(dec._h, blob_ptr, len(data), sh), "reload")
+            _lib.check(lib.stride_decode_host(dec._h, sh, ctypes.c_void_p(h_idx.data_ptr()),
+                                              ctypes.c_void_p(h_pos.data_ptr())), "decode_host")
+            ts.append(time.perf_counter() - t0)
+        e2e_s = reduce_max(sum(ts) / len(ts), dev)
+        e2e = {"value": round(replica_value(n_t, world, e2e_s) / 1e6, 3), "unit": "M tris/s",
+               "h2d_bytes_per_step": len(data), "d2h_bytes_per_step": 12 * (n_v + n_t),
+               "ms_per_step": round(e2e_s * 1e3, 4), "path": "ParaDeltaV5GpuDecoder C ABI: stride_reload + "
+                                                              "stride_decode_host, pinned host buffers"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, cores, reps, w = cpu_oracle_rate(data, n_t)
+        cpu = {"value": round(v, 3), "unit": "M tris/s", "cores": cores, "kind": "port",
+               "sample": f"{reps} full decodes of the same stream in {w:.2f} s wall "
+                         f"(C restatement of decode_dup, meshlet-parallel)"}
+
+    if rank == 0:
+        cfg = dict(cfg)
+        cfg["l2"] = "flushed before every step (256 MiB write, untimed)"
+        cfg["launch"] = launch
+        cfg["parallelism"] = f"replicas x{world}"
+        cfg["parity"] = "bit-exact vs CPU oracle (positions, indices)" if exact else f"MISMATCH ({exact})"
+        line = {
+            "metric": "decoded triangles per second", "value": round(value, 3), "unit": "M tris/s",
+            "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": round(mean_step, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32+f32 (exact f64 expression)",
+            "data": "synthetic (seeded heightfield; reference meshes not available)",
+            "config": cfg, "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e,
+            "gpu_launches": 2 * args.steps, "clocks": clk, "wall_s": round(wall, 3),
+        }
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main(argv=None):
+    args = parse_args(argv)
+    if args.workload in ("batch", "serve"):
+        raise SystemExit(f"workload {args.workload!r} is not wired into bench.py yet")
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_single(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

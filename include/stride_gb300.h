@@ -1,0 +1,210 @@
+/*
+ * stride_gb300.h -- C ABI of the GB300 (sm_103a) STRIDE "DPR4" v3 decoder.
+ *
+ * Plain pointers and sizes only (no torch or CUDA C++ types): `stream`
+ * arguments are `cudaStream_t` values passed as `void*` (0 = legacy default
+ * stream), device pointers are plain addresses in the current CUDA device.
+ *
+ * Every function returns 0 on success or a negative STRIDE_ERR_* code;
+ * stride_last_error_message() gives a human-readable reason for the calling
+ * thread's last failure.
+ *
+ * The reference decodes this format with the CPU function decode_dup
+ * (encoder/paradelta_v5_dup.py:471-618) and exposes GPU decoding through
+ * ParaDeltaV5GpuDecoder (utils/paradelta_v5_cuda.py:580-718), whose
+ * constructor uploads the bytes and sizes the outputs (:597-684), whose
+ * decode() enqueues the persistent decode kernel (:686-712) and whose
+ * decode_to_host() copies the results back (:714-718).  The entry points
+ * below replace that class's internals; the Python class
+ * meshpress_gb300.ParaDeltaV5GpuDecoder binds them with ctypes.
+ */
+#ifndef STRIDE_GB300_H
+#define STRIDE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define STRIDE_OK 0
+#define STRIDE_ERR_ARG (-1)         /* bad argument (null pointer, size)            */
+#define STRIDE_ERR_MAGIC (-2)       /* not a DPR4 stream (paradelta_v5_dup.py:520)  */
+#define STRIDE_ERR_VERSION (-3)     /* DPR4 version != 3 (paradelta_v5_dup.py:523)  */
+#define STRIDE_ERR_TRUNCATED (-4)   /* header / offset table past the end           */
+#define STRIDE_ERR_OFFSET (-5)      /* offset table not increasing or out of range  */
+#define STRIDE_ERR_CORRUPT (-6)     /* meshlet payload inconsistent (FIFO index,
+                                       vertex id, triangle count, code range,
+                                       payload end != next offset)                 */
+#define STRIDE_ERR_UNSUPPORTED (-7) /* valid but outside this decoder's limits:
+                                       > 256 local vertices or triangles per
+                                       meshlet, g_bits > 24, K > 30, residual
+                                       k > 24, IRLP sums beyond int32               */
+#define STRIDE_ERR_CUDA (-8)        /* CUDA runtime error                           */
+#define STRIDE_ERR_TIMEOUT (-9)     /* a bounded device/host wait gave up           */
+#define STRIDE_ERR_NOMEM (-10)      /* allocation failed / admission budget          */
+#define STRIDE_ERR_BUSY (-11)       /* server queue full                            */
+
+typedef struct stride_handle stride_handle;
+
+typedef struct {
+    uint32_t n_meshlets;
+    uint32_t g_bits[3];
+    uint64_t n_v;        /* decoded (duplicated) vertices = sum of n_local      */
+    uint64_t n_t;        /* triangles                                           */
+    uint64_t nbytes;     /* length of the encoded stream                        */
+    float center[3];
+    float scale;
+    int32_t pred_n[9];
+    int32_t pred_k[3];
+} stride_info_t;
+
+/* Launch shape of the decode kernel (the autotuner's search space). */
+typedef struct {
+    int32_t warps_per_cta;   /* warps (32 meshlets each) per CTA: 1, 2 or 4   */
+    int32_t persistent;      /* 1 = persistent work-stealing grid            */
+    int32_t ctas_per_sm;     /* persistent grid = ctas_per_sm * SMs (0 = 4)   */
+    uint32_t stage_bytes;    /* per-warp shared-memory payload staging       */
+    uint32_t code_bytes;     /* per-warp shared-memory integer-code storage  */
+} stride_launch_cfg;
+
+/* Thread-local description of the last error in this thread. */
+const char* stride_last_error_message(void);
+const char* stride_error_string(int code);
+
+/* Library/device facts: number of SMs of the current device and the build's
+ * target architecture (e.g. 103 for sm_103a). */
+int stride_device_info(int* sm_count, int* arch);
+
+/* Host-only: parse and validate the 86-byte global header and the size of the
+ * offset table without touching the GPU.  Replaces the header part of
+ * parse_globals_v5 (utils/paradelta_v5_cuda.py:515-577) for the DPR4 format
+ * (header layout encoder/paradelta_v5_dup.py:412-447). */
+int stride_inspect(const uint8_t* data, size_t len, stride_info_t* info);
+
+/* ---- single mesh ---------------------------------------------------------
+ * stride_open: parse + validate the global header on the host, allocate the
+ * device copy of the bytes and the decoder's scratch, upload (synchronous).
+ * Replaces ParaDeltaV5GpuDecoder.__init__ (utils/paradelta_v5_cuda.py:597-684)
+ * and its CPU header parse parse_globals_v5 (:515-577).  The caller keeps
+ * ownership of `data`. */
+int stride_open(const uint8_t* data, size_t len, stride_handle** out);
+
+/* Replace the handle's stream with new bytes (re-validates the header,
+ * grows device buffers if needed, uploads asynchronously on `stream`).
+ * `data` must stay valid until the upload completes; pinned host memory makes
+ * the upload asynchronous. */
+int stride_reload(stride_handle* h, const uint8_t* data, size_t len, void* stream);
+
+int stride_info(const stride_handle* h, stride_info_t* info);
+
+/* Enqueue one decode on `stream`: the header/meshlet-table parse kernel with
+ * its device-wide scan, then the meshlet decode kernel.  Writes n_t x 3
+ * uint32 triangle indices to d_idx and n_v x 3 float32 world-space positions
+ * to d_pos (both device pointers, C-contiguous).  If d_codes is not NULL the
+ * integer quantisation codes (n_v x 3 int32) are written too.  Asynchronous:
+ * call stride_status() to learn whether the stream was valid.
+ * Replaces ParaDeltaV5GpuDecoder.decode (utils/paradelta_v5_cuda.py:686-712)
+ * plus the world-space transform of decode_to_host (:714-717). */
+int stride_decode(stride_handle* h, void* stream, uint32_t* d_idx, float* d_pos,
+                  int32_t* d_codes);
+
+/* Decode with host buffers: enqueue decode into handle-owned device outputs,
+ * copy them to h_idx / h_pos (host, n_t*3 uint32 and n_v*3 float32) and
+ * synchronise.  Returns the decode status.  Replaces decode_to_host
+ * (utils/paradelta_v5_cuda.py:714-718). */
+int stride_decode_host(stride_handle* h, void* stream, uint32_t* h_idx, float* h_pos);
+
+/* Status of the last decode enqueued on this handle.  wait != 0 blocks until
+ * it finished.  Returns STRIDE_OK, a STRIDE_ERR_* code for an invalid stream,
+ * or STRIDE_ERR_BUSY when wait == 0 and the decode is still running.
+ * *bad_meshlet (optional) receives the first failing meshlet. */
+int stride_status(stride_handle* h, int wait, uint32_t* bad_meshlet);
+
+/* Measurement entry point (no reference counterpart): one decode like
+ * stride_decode, with CUDA events recorded on `stream` around the parse
+ * kernel and around the decode kernel; waits and returns both durations in
+ * milliseconds. */
+int stride_decode_timed(stride_handle* h, void* stream, uint32_t* d_idx, float* d_pos,
+                        float* parse_ms, float* decode_ms);
+
+/* Launch shape for this handle's decodes (defaults are used until set). */
+int stride_set_config(stride_handle* h, const stride_launch_cfg* cfg);
+
+void stride_close(stride_handle* h);
+
+/* ---- many meshes, one launch ---------------------------------------------
+ * A batch holds the device copies of many streams and one device meshlet
+ * queue over all of them.  Outputs are concatenated: mesh i writes its
+ * triangles at d_idx + 3*t_offset[i] (indices local to mesh i) and its
+ * positions at d_pos + 3*v_offset[i].  No reference counterpart: the
+ * reference decodes one mesh per ParaDeltaV5GpuDecoder. */
+typedef struct stride_batch stride_batch;
+
+
+int stride_batch_create(const uint8_t* const* blobs, const size_t* lens, uint32_t n_meshes,
+                        stride_batch** out);
+int stride_batch_info(const stride_batch* b, uint64_t* n_meshlets, uint64_t* n_v, uint64_t* n_t);
+/* Per-mesh output offsets (in vertices / triangles), n_meshes entries each. */
+int stride_batch_offsets(const stride_batch* b, uint64_t* v_offset, uint64_t* t_offset);
+int stride_batch_set_config(stride_batch* b, const stride_launch_cfg* cfg);
+int stride_batch_get_config(const stride_batch* b, stride_launch_cfg* cfg);
+int stride_batch_decode(stride_batch* b, void* stream, uint32_t* d_idx, float* d_pos);
+/* Capture the decode sequence for these output pointers into a CUDA graph
+ * (replaces any earlier graph) and replay it with stride_batch_launch_graph. */
+int stride_batch_capture_graph(stride_batch* b, void* stream, uint32_t* d_idx, float* d_pos);
+int stride_batch_launch_graph(stride_batch* b, void* stream);
+/* Time every launch configuration on this batch (CUDA events, `iters` runs
+ * each), keep the fastest, and report it. */
+int stride_batch_autotune(stride_batch* b, void* stream, uint32_t* d_idx, float* d_pos,
+                          int iters, stride_launch_cfg* best, float* best_ms);
+int stride_batch_status(stride_batch* b, int wait, uint32_t* bad_mesh, uint32_t* bad_meshlet);
+void stride_batch_destroy(stride_batch* b);
+
+/* ---- serving: continuous batching over a device-resident arena ----------
+ * Requests (encoded blobs) are submitted from any host thread.  A scheduler
+ * thread admits queued requests while the arena (payload + output bytes)
+ * stays under `hbm_budget_bytes`, packs whatever was admitted into one
+ * persistent-kernel launch on one of `n_streams` streams, and keeps up to
+ * n_streams launches in flight, so requests arriving while others decode are
+ * admitted as soon as arena space frees.  Results stay in device memory until
+ * the caller releases them.  No reference counterpart. */
+typedef struct stride_server stride_server;
+
+typedef struct {
+    uint64_t hbm_budget_bytes;   /* arena limit for payloads + outputs        */
+    uint32_t max_batch;          /* requests per launch (0 = 256)             */
+    uint32_t n_streams;          /* launches in flight (0 = 2)                */
+    uint32_t max_queue;          /* queued requests before submit is refused  */
+    uint32_t copy_to_host;       /* 1 = also copy results to host buffers     */
+} stride_server_opts;
+
+typedef struct {
+    int32_t status;              /* STRIDE_OK or STRIDE_ERR_*                   */
+    uint32_t pad;
+    uint64_t n_v, n_t;
+    const uint32_t* d_idx;       /* device results (valid until released)     */
+    const float* d_pos;
+    const uint32_t* h_idx;       /* host copies when copy_to_host             */
+    const float* h_pos;
+    double t_submit_us, t_admit_us, t_done_us; /* host steady clock, microseconds */
+} stride_result;
+
+int stride_server_create(const stride_server_opts* opts, stride_server** out);
+/* Copies `data`; returns a request id. */
+int stride_server_submit(stride_server* s, const uint8_t* data, size_t len, uint64_t* req_id);
+/* Waits up to timeout_ms (<0 = forever) for the request to finish. */
+int stride_server_wait(stride_server* s, uint64_t req_id, int timeout_ms, stride_result* out);
+/* Frees the request's arena space. */
+int stride_server_release(stride_server* s, uint64_t req_id);
+int stride_server_stats(stride_server* s, uint64_t* launches, uint64_t* completed,
+                        uint64_t* arena_peak_bytes);
+void stride_server_destroy(stride_server* s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* STRIDE_GB300_H */

@@ -1,0 +1,8 @@
+"""GB300 (sm_103a) decoder for the STRIDE "DPR4" v3 mesh bitstream.
+
+``ParaDeltaV5GpuDecoder`` is the drop-in for the reference class of the same
+name (utils/paradelta_v5_cuda.py:580-718); ``BatchDecoder`` decodes many
+streams in one launch; ``StrideServer`` is the continuous-batching service.
+"""
+from .decoder import ParaDeltaV5GpuDecoder, decode_to_device  # noqa: F401
+from ._lib import StrideDeviceError, StrideFormatError  # noqa: F401

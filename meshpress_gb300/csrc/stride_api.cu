@@ -1,0 +1,430 @@
+// C ABI of the single-mesh decoder (include/stride_gb300.h): host header
+// parse, device buffers, enqueue and status.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+
+#include "stride_common.cuh"
+#include "stride_gb300.h"
+#include "stride_internal.h"
+
+namespace stride {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_last_error = buf;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(STRIDE_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+static uint32_t be32(const uint8_t* p) {
+    return (static_cast<uint32_t>(p[0]) << 24) | (static_cast<uint32_t>(p[1]) << 16) |
+           (static_cast<uint32_t>(p[2]) << 8) | p[3];
+}
+
+static float bef32(const uint8_t* p) {
+    const uint32_t u = be32(p);
+    float f;
+    std::memcpy(&f, &u, 4);
+    return f;
+}
+
+// Global header of a DPR4 v3 stream (encoder/paradelta_v5_dup.py:412-447,
+// read back at :472-501).
+int parse_header(const uint8_t* data, size_t len, MeshParams* p, char* why, size_t why_len) {
+    auto say = [&](int code, const char* msg) {
+        if (why && why_len) snprintf(why, why_len, "%s", msg);
+        return code;
+    };
+    std::memset(p, 0, sizeof(*p));
+    if (!data) return say(STRIDE_ERR_ARG, "null stream");
+    if (len < kHeaderBytes) return say(STRIDE_ERR_TRUNCATED, "stream shorter than the 86-byte DPR4 header");
+    if (be32(data) != kMagic) {
+        char m[96];
+        snprintf(m, sizeof(m), "bad magic 0x%08X (expected DPR4 0x44505234)", be32(data));
+        return say(STRIDE_ERR_MAGIC, m);
+    }
+    if (data[4] != kVersion) {
+        char m[64];
+        snprintf(m, sizeof(m), "DPR4 version %u (expected 3)", data[4]);
+        return say(STRIDE_ERR_VERSION, m);
+    }
+    float center[3], gmin[3], grange[3];
+    for (int i = 0; i < 3; i++) center[i] = bef32(data + 6 + 4 * i);
+    const float scale = bef32(data + 18);
+    for (int i = 0; i < 3; i++) gmin[i] = bef32(data + 26 + 4 * i);
+    for (int i = 0; i < 3; i++) grange[i] = bef32(data + 38 + 4 * i);
+    for (int i = 0; i < 3; i++) p->g_bits[i] = data[50 + i];
+    for (int i = 0; i < 9; i++) {
+        const uint32_t v = (static_cast<uint32_t>(data[53 + 2 * i]) << 8) | data[54 + 2 * i];
+        p->pred_n[i] = (v & 0x8000u) ? static_cast<int32_t>(v) - 0x10000 : static_cast<int32_t>(v);
+    }
+    for (int i = 0; i < 3; i++) p->pred_k[i] = data[71 + i];
+    p->n_v = be32(data + 74);
+    p->n_t = be32(data + 78);
+    p->n_meshlets = be32(data + 82);
+    const unsigned long long table_end = kHeaderBytes + 4ull * p->n_meshlets;
+    if (table_end > len) return say(STRIDE_ERR_TRUNCATED, "offset table runs past the end of the stream");
+    if (len * 8ull >= (1ull << 32) - 4096) return say(STRIDE_ERR_UNSUPPORTED, "stream longer than 512 MB");
+    if (p->n_meshlets == 0) return say(STRIDE_ERR_CORRUPT, "stream has no meshlets");
+    for (int d = 0; d < 3; d++) {
+        if (p->g_bits[d] > static_cast<uint32_t>(kMaxGBits))
+            return say(STRIDE_ERR_UNSUPPORTED, "more than 24 bits per axis");
+        if (p->pred_k[d] > 30) return say(STRIDE_ERR_UNSUPPORTED, "predictor shift K above 30");
+        p->code_max[d] = (1u << p->g_bits[d]) - 1u;
+        p->pred_half[d] = p->pred_k[d] ? (1 << (p->pred_k[d] - 1)) : 0;
+        // the int32 IRLP sum of in-range codes must not overflow
+        long long bound = 0;
+        for (int j = 0; j < 3; j++) bound += std::llabs(static_cast<long long>(p->pred_n[3 * d + j]));
+        bound = bound * static_cast<long long>(p->code_max[d]) + p->pred_half[d];
+        if (bound >= (1ll << 31)) return say(STRIDE_ERR_UNSUPPORTED, "IRLP weights overflow int32 arithmetic");
+        stride_dequant_setup(&p->dq[d], center[d], scale, gmin[d], grange[d], p->g_bits[d]);
+    }
+    p->nbits = len * 8ull;
+    p->body_bit = static_cast<uint32_t>(table_end * 8ull);
+    p->anchor_bits = p->g_bits[0] + p->g_bits[1] + p->g_bits[2];
+    p->meshlet_begin = 0;
+    p->blob_off = 0;
+    p->v_offset = 0;
+    p->t_offset = 0;
+    return STRIDE_OK;
+}
+
+size_t blob_alloc_bytes(size_t len) { return (len + kBlobPad + 255) & ~static_cast<size_t>(255); }
+
+int status_to_code(const Status& st, uint32_t* bad_meshlet) {
+    if (st.err == 0ull) return STRIDE_OK;
+    const int code = static_cast<int>(st.err >> 32);
+    if (bad_meshlet) *bad_meshlet = static_cast<uint32_t>(st.err & 0xFFFFFFFFull);
+    switch (code) {
+        case kErrOffset: return STRIDE_ERR_OFFSET;
+        case kErrCorrupt: return STRIDE_ERR_CORRUPT;
+        case kErrUnsupported: return STRIDE_ERR_UNSUPPORTED;
+        case kErrTimeout: return STRIDE_ERR_TIMEOUT;
+        default: return STRIDE_ERR_CORRUPT;
+    }
+}
+
+const char* status_message(int code) {
+    switch (code) {
+        case STRIDE_ERR_OFFSET: return "meshlet offset table out of order or out of range";
+        case STRIDE_ERR_CORRUPT: return "meshlet payload inconsistent with its header or the offset table";
+        case STRIDE_ERR_UNSUPPORTED: return "meshlet outside this decoder's limits (>256 vertices/triangles, k>24)";
+        case STRIDE_ERR_TIMEOUT: return "a bounded device wait gave up";
+        default: return "decode failed";
+    }
+}
+
+}  // namespace stride
+
+using namespace stride;
+
+struct stride_handle {
+    int device = 0;
+    size_t len = 0, cap_bytes = 0;
+    uint32_t cap_meshlets = 0;
+    uint8_t* d_blob = nullptr;
+    MeshParams params;
+    MeshParams* d_params = nullptr;
+    MeshletDesc* d_descs = nullptr;
+    uint2* d_blk_sums = nullptr;
+    ulonglong2* d_blk_prefix = nullptr;
+    Status* d_status = nullptr;
+    uint32_t* d_idx = nullptr;
+    float* d_pos = nullptr;
+    size_t cap_v = 0, cap_t = 0;
+    cudaEvent_t done = nullptr;
+    bool launched = false;
+    LaunchCfg cfg;
+};
+
+static void free_buffers(stride_handle* h) {
+    cudaFree(h->d_blob);
+    cudaFree(h->d_params);
+    cudaFree(h->d_descs);
+    cudaFree(h->d_blk_sums);
+    cudaFree(h->d_blk_prefix);
+    cudaFree(h->d_status);
+    cudaFree(h->d_idx);
+    cudaFree(h->d_pos);
+    h->d_blob = nullptr;
+    h->d_params = nullptr;
+    h->d_descs = nullptr;
+    h->d_blk_sums = nullptr;
+    h->d_blk_prefix = nullptr;
+    h->d_status = nullptr;
+    h->d_idx = nullptr;
+    h->d_pos = nullptr;
+}
+
+static int ensure_capacity(stride_handle* h, size_t len, uint32_t n_meshlets) {
+    cudaError_t e;
+    if (blob_alloc_bytes(len) > h->cap_bytes) {
+        cudaFree(h->d_blob);
+        h->d_blob = nullptr;
+        h->cap_bytes = blob_alloc_bytes(len);
+        if ((e = cudaMalloc(&h->d_blob, h->cap_bytes)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(stream)");
+    }
+    if (n_meshlets > h->cap_meshlets) {
+        cudaFree(h->d_descs);
+        cudaFree(h->d_blk_sums);
+        cudaFree(h->d_blk_prefix);
+        h->d_descs = nullptr;
+        h->d_blk_sums = nullptr;
+        h->d_blk_prefix = nullptr;
+        const uint32_t nb = parse_blocks(n_meshlets);
+        if ((e = cudaMalloc(&h->d_descs, sizeof(MeshletDesc) * n_meshlets)) != cudaSuccess ||
+            (e = cudaMalloc(&h->d_blk_sums, sizeof(uint2) * nb)) != cudaSuccess ||
+            (e = cudaMalloc(&h->d_blk_prefix, sizeof(ulonglong2) * nb)) != cudaSuccess)
+            return cuda_fail(e, "cudaMalloc(scratch)");
+        h->cap_meshlets = n_meshlets;
+    }
+    return STRIDE_OK;
+}
+
+extern "C" {
+
+const char* stride_last_error_message(void) { return g_last_error.c_str(); }
+
+const char* stride_error_string(int code) {
+    switch (code) {
+        case STRIDE_OK: return "ok";
+        case STRIDE_ERR_ARG: return "bad argument";
+        case STRIDE_ERR_MAGIC: return "bad magic";
+        case STRIDE_ERR_VERSION: return "unsupported version";
+        case STRIDE_ERR_TRUNCATED: return "truncated stream";
+        case STRIDE_ERR_OFFSET: return "bad meshlet offset table";
+        case STRIDE_ERR_CORRUPT: return "corrupt meshlet payload";
+        case STRIDE_ERR_UNSUPPORTED: return "unsupported stream parameters";
+        case STRIDE_ERR_CUDA: return "CUDA error";
+        case STRIDE_ERR_TIMEOUT: return "timeout";
+        case STRIDE_ERR_NOMEM: return "out of memory";
+        case STRIDE_ERR_BUSY: return "busy";
+        default: return "unknown error";
+    }
+}
+
+int stride_device_info(int* sm_count, int* arch) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (sm_count) *sm_count = device_sm_count();
+    if (arch) *arch = 103;
+    return STRIDE_OK;
+}
+
+static void fill_info(const MeshParams& p, size_t len, stride_info_t* info) {
+    std::memset(info, 0, sizeof(*info));
+    info->n_meshlets = p.n_meshlets;
+    for (int i = 0; i < 3; i++) {
+        info->g_bits[i] = p.g_bits[i];
+        info->center[i] = static_cast<float>(p.dq[i].center);
+        info->pred_k[i] = p.pred_k[i];
+    }
+    for (int i = 0; i < 9; i++) info->pred_n[i] = p.pred_n[i];
+    info->scale = static_cast<float>(p.dq[0].scale);
+    info->n_v = p.n_v;
+    info->n_t = p.n_t;
+    info->nbytes = len;
+}
+
+int stride_inspect(const uint8_t* data, size_t len, stride_info_t* info) {
+    if (!info) return fail(STRIDE_ERR_ARG, "null info");
+    MeshParams p;
+    char why[256] = {0};
+    const int rc = parse_header(data, len, &p, why, sizeof(why));
+    if (rc) return fail(rc, "%s", why);
+    fill_info(p, len, info);
+    return STRIDE_OK;
+}
+
+int stride_open(const uint8_t* data, size_t len, stride_handle** out) {
+    if (!out) return fail(STRIDE_ERR_ARG, "null output handle");
+    *out = nullptr;
+    MeshParams p;
+    char why[256] = {0};
+    int rc = parse_header(data, len, &p, why, sizeof(why));
+    if (rc) return fail(rc, "%s", why);
+    stride_handle* h = new stride_handle();
+    cudaGetDevice(&h->device);
+    h->params = p;
+    h->len = len;
+    cudaError_t e;
+    if ((rc = ensure_capacity(h, len, p.n_meshlets)) != STRIDE_OK) {
+        free_buffers(h);
+        delete h;
+        return rc;
+    }
+    if ((e = cudaMalloc(&h->d_params, sizeof(MeshParams))) != cudaSuccess ||
+        (e = cudaMalloc(&h->d_status, sizeof(Status))) != cudaSuccess ||
+        (e = cudaMemcpy(h->d_blob, data, len, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemset(h->d_blob + len, 0, h->cap_bytes - len)) != cudaSuccess ||
+        (e = cudaMemcpy(h->d_params, &h->params, sizeof(MeshParams), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemset(h->d_status, 0, sizeof(Status))) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&h->done, cudaEventDisableTiming)) != cudaSuccess) {
+        free_buffers(h);
+        delete h;
+        return cuda_fail(e, "stride_open");
+    }
+    *out = h;
+    return STRIDE_OK;
+}
+
+int stride_reload(stride_handle* h, const uint8_t* data, size_t len, void* stream) {
+    if (!h) return fail(STRIDE_ERR_ARG, "null handle");
+    MeshParams p;
+    char why[256] = {0};
+    int rc = parse_header(data, len, &p, why, sizeof(why));
+    if (rc) return fail(rc, "%s", why);
+    if ((rc = ensure_capacity(h, len, p.n_meshlets)) != STRIDE_OK) return rc;
+    h->params = p;
+    h->len = len;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(h->d_blob, data, len, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(h->d_blob + len, 0, std::min<size_t>(h->cap_bytes - len, kBlobPad), s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(h->d_params, &h->params, sizeof(MeshParams), cudaMemcpyHostToDevice, s)) !=
+            cudaSuccess)
+        return cuda_fail(e, "stride_reload");
+    return STRIDE_OK;
+}
+
+int stride_info(const stride_handle* h, stride_info_t* info) {
+    if (!h || !info) return fail(STRIDE_ERR_ARG, "null argument");
+    fill_info(h->params, h->len, info);
+    return STRIDE_OK;
+}
+
+static DecodeArgs handle_args(stride_handle* h, uint32_t* d_idx, float* d_pos, int32_t* d_codes) {
+    DecodeArgs a;
+    a.arena = h->d_blob;
+    a.meshes = h->d_params;
+    a.meshlet_mesh = nullptr;
+    a.total_meshlets = h->params.n_meshlets;
+    a.n_meshes = 1;
+    a.descs = h->d_descs;
+    a.blk_sums = h->d_blk_sums;
+    a.blk_prefix = h->d_blk_prefix;
+    a.status = h->d_status;
+    a.idx = d_idx;
+    a.pos = d_pos;
+    a.codes = d_codes;
+    a.wide_codes = h->params.g_bits[0] > 16 || h->params.g_bits[1] > 16 || h->params.g_bits[2] > 16;
+    return a;
+}
+
+int stride_decode_timed(stride_handle* h, void* stream, uint32_t* d_idx, float* d_pos, float* parse_ms,
+                        float* decode_ms) {
+    if (!h || !d_idx || !d_pos) return fail(STRIDE_ERR_ARG, "null argument");
+    cudaEvent_t ev[3];
+    for (auto& e : ev) cudaEventCreate(&e);
+    void* evp[3] = {ev[0], ev[1], ev[2]};
+    int rc = enqueue_decode(handle_args(h, d_idx, d_pos, nullptr), h->cfg, stream, evp);
+    if (rc == STRIDE_OK) {
+        cudaEventRecord(h->done, static_cast<cudaStream_t>(stream));
+        h->launched = true;
+        cudaError_t e = cudaEventSynchronize(ev[2]);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "stride_decode_timed");
+        } else {
+            float a = 0.f, b = 0.f;
+            cudaEventElapsedTime(&a, ev[0], ev[1]);
+            cudaEventElapsedTime(&b, ev[1], ev[2]);
+            if (parse_ms) *parse_ms = a;
+            if (decode_ms) *decode_ms = b;
+        }
+    } else {
+        rc = fail(rc, "decode launch failed");
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    return rc;
+}
+
+int stride_decode(stride_handle* h, void* stream, uint32_t* d_idx, float* d_pos, int32_t* d_codes) {
+    if (!h) return fail(STRIDE_ERR_ARG, "null handle");
+    if ((!d_idx && h->params.n_t) || (!d_pos && h->params.n_v)) return fail(STRIDE_ERR_ARG, "null output pointer");
+    const int rc = enqueue_decode(handle_args(h, d_idx, d_pos, d_codes), h->cfg, stream);
+    if (rc) return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    cudaError_t e = cudaEventRecord(h->done, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
+    h->launched = true;
+    return STRIDE_OK;
+}
+
+int stride_status(stride_handle* h, int wait, uint32_t* bad_meshlet) {
+    if (!h) return fail(STRIDE_ERR_ARG, "null handle");
+    if (!h->launched) return STRIDE_OK;
+    cudaError_t e = wait ? cudaEventSynchronize(h->done) : cudaEventQuery(h->done);
+    if (e == cudaErrorNotReady) return STRIDE_ERR_BUSY;
+    if (e != cudaSuccess) return cuda_fail(e, "decode");
+    Status st;
+    if ((e = cudaMemcpy(&st, h->d_status, sizeof(st), cudaMemcpyDeviceToHost)) != cudaSuccess)
+        return cuda_fail(e, "cudaMemcpy(status)");
+    uint32_t bad = 0;
+    const int rc = status_to_code(st, &bad);
+    if (bad_meshlet) *bad_meshlet = bad;
+    if (rc) return fail(rc, "%s (meshlet %u)", status_message(rc), bad);
+    return STRIDE_OK;
+}
+
+int stride_decode_host(stride_handle* h, void* stream, uint32_t* h_idx, float* h_pos) {
+    if (!h || (!h_idx && h->params.n_t) || (!h_pos && h->params.n_v)) return fail(STRIDE_ERR_ARG, "null argument");
+    cudaError_t e;
+    if (h->params.n_v > h->cap_v) {
+        cudaFree(h->d_pos);
+        h->d_pos = nullptr;
+        if ((e = cudaMalloc(&h->d_pos, 12 * h->params.n_v)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(pos)");
+        h->cap_v = h->params.n_v;
+    }
+    if (h->params.n_t > h->cap_t) {
+        cudaFree(h->d_idx);
+        h->d_idx = nullptr;
+        if ((e = cudaMalloc(&h->d_idx, 12 * h->params.n_t)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(idx)");
+        h->cap_t = h->params.n_t;
+    }
+    int rc = stride_decode(h, stream, h->d_idx, h->d_pos, nullptr);
+    if (rc) return rc;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if ((e = cudaMemcpyAsync(h_idx, h->d_idx, 12 * h->params.n_t, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemcpyAsync(h_pos, h->d_pos, 12 * h->params.n_v, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaEventRecord(h->done, s)) != cudaSuccess)
+        return cuda_fail(e, "stride_decode_host copy");
+    return stride_status(h, 1, nullptr);
+}
+
+int stride_set_config(stride_handle* h, const stride_launch_cfg* c) {
+    if (!h || !c) return fail(STRIDE_ERR_ARG, "null argument");
+    LaunchCfg cfg;
+    cfg.warps_per_cta = c->warps_per_cta;
+    cfg.persistent = c->persistent;
+    cfg.ctas_per_sm = c->ctas_per_sm;
+    cfg.stage_bytes = c->stage_bytes;
+    cfg.code_bytes = c->code_bytes;
+    const bool wide = h->params.g_bits[0] > 16 || h->params.g_bits[1] > 16 || h->params.g_bits[2] > 16;
+    if (check_config(cfg, wide)) return fail(STRIDE_ERR_ARG, "launch configuration not launchable");
+    h->cfg = cfg;
+    return STRIDE_OK;
+}
+
+void stride_close(stride_handle* h) {
+    if (!h) return;
+    if (h->launched) cudaEventSynchronize(h->done);
+    if (h->done) cudaEventDestroy(h->done);
+    free_buffers(h);
+    delete h;
+}
+
+}  // extern "C"

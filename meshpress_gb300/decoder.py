@@ -1,0 +1,160 @@
+"""Drop-in replacement for the reference ``ParaDeltaV5GpuDecoder``.
+
+Reference: utils/paradelta_v5_cuda.py:580-718.  Same class name, constructor
+(``data``, ``meshlets_per_block`` in [1, 16]) and ``decode()`` /
+``decode_to_host()`` methods, plus ``decode_to_device()``.  The input is the
+DPR4 v3 bitstream that ``STRIDEEncoder`` writes
+(encoder/paradelta_v5_dup.py:316-464); a PLDT (v4/v5) stream is rejected
+with ``ValueError`` like any other bad magic (utils/paradelta_v5_cuda.py:520).
+
+Everything runs in ``libstride_gb300.so`` through its C ABI; PyTorch only
+provides device memory and the current stream.  There is no CPU fallback:
+without a CUDA device the constructor raises ``RuntimeError`` (the reference
+raises ``RuntimeError("cupy not installed")`` in the same place, :598-599).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream_handle(stream=None) -> int:
+    torch = _torch()
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return int(s.cuda_stream)
+
+
+class ParaDeltaV5GpuDecoder:
+    """GPU decoder for one STRIDE (DPR4 v3) stream.
+
+    Attributes kept from the reference: ``n_meshlets``, ``n_v_total``,
+    ``n_t_total``, ``meshlets_per_block`` (accepted for compatibility; the
+    reference kernel ignores it too, utils/paradelta_v5_cuda.py:259-260).
+    """
+
+    def __init__(self, data: bytes, meshlets_per_block: int = 1):
+        if meshlets_per_block < 1 or meshlets_per_block > 16:
+            raise ValueError("meshlets_per_block must be in [1, 16]")
+        torch = _torch()
+        if not torch.cuda.is_available():
+            raise RuntimeError("CUDA device not available: the STRIDE decoder runs on the GPU only")
+        self.meshlets_per_block = int(meshlets_per_block)
+        self._lib = _lib.load()
+        self._data = bytes(data)
+        torch.cuda.init()
+        h = ctypes.c_void_p()
+        _lib.check(self._lib.stride_open(self._data, len(self._data), ctypes.byref(h)), "stride_open")
+        self._h = h
+        info = _lib.StrideInfo()
+        _lib.check(self._lib.stride_info(self._h, ctypes.byref(info)), "stride_info")
+        self.info = info
+        self.n_meshlets = int(info.n_meshlets)
+        self.n_v_total = int(info.n_v)
+        self.n_t_total = int(info.n_t)
+        self.g_bits = tuple(int(b) for b in info.g_bits)
+        self.d_verts = None
+        self.d_tris = None
+        self._device = torch.cuda.current_device()
+
+    # -- launch configuration ------------------------------------------------
+    def set_launch_config(self, cfg: _lib.LaunchCfg):
+        _lib.check(self._lib.stride_set_config(self._h, ctypes.byref(cfg)), "stride_set_config")
+
+    # -- decoding --------------------------------------------------------------
+    def _outputs(self):
+        torch = _torch()
+        if self.d_tris is None:
+            self.d_tris = torch.empty((self.n_t_total, 3), dtype=torch.uint32, device=f"cuda:{self._device}")
+            self.d_verts = torch.empty((self.n_v_total, 3), dtype=torch.float32, device=f"cuda:{self._device}")
+        return self.d_tris, self.d_verts
+
+    def decode_into(self, d_idx, d_pos, *, codes=None, stream=None, check: bool = True):
+        """Decode into caller-provided CUDA tensors (uint32 (n_t, 3), float32
+        (n_v, 3)); ``codes`` optionally receives the int32 (n_v, 3) codes."""
+        torch = _torch()
+        assert d_idx.is_cuda and d_pos.is_cuda and d_idx.is_contiguous() and d_pos.is_contiguous()
+        assert d_idx.numel() >= 3 * self.n_t_total and d_pos.numel() >= 3 * self.n_v_total
+        cptr = None
+        if codes is not None:
+            assert codes.dtype == torch.int32 and codes.is_cuda and codes.numel() >= 3 * self.n_v_total
+            cptr = ctypes.c_void_p(codes.data_ptr())
+        rc = self._lib.stride_decode(self._h, ctypes.c_void_p(_stream_handle(stream)),
+                                     ctypes.c_void_p(d_idx.data_ptr()), ctypes.c_void_p(d_pos.data_ptr()), cptr)
+        _lib.check(rc, "stride_decode")
+        if check:
+            self.check()
+
+    def check(self):
+        """Wait for the last decode and raise if the stream was invalid."""
+        bad = ctypes.c_uint32()
+        _lib.check(self._lib.stride_status(self._h, 1, ctypes.byref(bad)), "stride decode")
+
+    def decode_to_device(self, *, stream=None, check: bool = True):
+        """-> (triangles torch.uint32 (n_t, 3), positions torch.float32 (n_v, 3))
+        in world space, resident on the GPU.  The tensors are reused by later
+        calls, like the reference's output arrays (:686-690)."""
+        tris, verts = self._outputs()
+        self.decode_into(tris, verts, stream=stream, check=check)
+        return tris, verts
+
+    def decode(self, *, stream=None, check: bool = True):
+        """Reference order: -> (positions (n_v, 3) float32, triangles (n_t, 3))
+        as CUDA tensors (the reference returns normalised positions and int32
+        triangles, :712; this decoder returns world-space positions and
+        uint32 triangles)."""
+        tris, verts = self.decode_to_device(stream=stream, check=check)
+        return verts, tris
+
+    def decode_to_host(self, out=None, *, stream=None):
+        """-> (positions np.float32 (n_v, 3), triangles np.uint32 (n_t, 3)),
+        copied to host memory (reference :714-718).  ``out`` may supply the two
+        host arrays (pinned memory makes the copies asynchronous)."""
+        if out is None:
+            pos = np.empty((self.n_v_total, 3), np.float32)
+            idx = np.empty((self.n_t_total, 3), np.uint32)
+        else:
+            pos, idx = out
+        rc = self._lib.stride_decode_host(self._h, ctypes.c_void_p(_stream_handle(stream)),
+                                          ctypes.c_void_p(idx.ctypes.data), ctypes.c_void_p(pos.ctypes.data))
+        _lib.check(rc, "stride_decode_host")
+        return pos, idx
+
+    def reload(self, data: bytes, *, stream=None):
+        """Swap in a new stream (device buffers are reused when large enough)."""
+        self._data = bytes(data)
+        rc = self._lib.stride_reload(self._h, self._data, len(self._data), ctypes.c_void_p(_stream_handle(stream)))
+        _lib.check(rc, "stride_reload")
+        info = _lib.StrideInfo()
+        _lib.check(self._lib.stride_info(self._h, ctypes.byref(info)), "stride_info")
+        self.info = info
+        self.n_meshlets = int(info.n_meshlets)
+        if int(info.n_v) != self.n_v_total or int(info.n_t) != self.n_t_total:
+            self.d_verts = self.d_tris = None
+        self.n_v_total = int(info.n_v)
+        self.n_t_total = int(info.n_t)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._lib.stride_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def decode_to_device(data: bytes):
+    """One-shot helper: -> (triangles torch.uint32, positions torch.float32)."""
+    dec = ParaDeltaV5GpuDecoder(data)
+    tris, verts = dec.decode_to_device()
+    return tris.clone(), verts.clone()

@@ -1,0 +1,8 @@
+"""CPU oracle for the STRIDE (DPR4 v3) decoder -- test infrastructure only.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` import this package, and only as the checker.  The product path
+(``meshpress_gb300``) never imports it.
+"""
+from .oracle import (OracleError, bitcodec_read, decode, decode_mt,  # noqa: F401
+                     parse_header, build, library_path)

@@ -1,0 +1,164 @@
+"""ctypes binding of the C oracle (``stride_oracle.c``).
+
+TEST INFRASTRUCTURE ONLY.  The C file restates the reference CPU decoder
+``decode_dup`` (encoder/paradelta_v5_dup.py:471-618); this module builds it
+with gcc (no FMA contraction, so the float64 dequantisation rounds exactly
+like numpy) and exposes it as numpy functions.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from dataclasses import dataclass
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, "stride_oracle.c")
+LIB = os.path.join(HERE, "libstride_oracle.so")
+
+_lib = None
+
+
+class OracleError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"oracle error {code}: {msg}")
+        self.code = code
+
+
+def build(force: bool = False) -> str:
+    """Compile the oracle with gcc (-O2, no FMA contraction)."""
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+        cmd = ["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math",
+               "-fPIC", "-shared", "-pthread", SRC, "-o", LIB + ".tmp", "-lm"]
+        subprocess.run(cmd, check=True)
+        os.replace(LIB + ".tmp", LIB)
+    return LIB
+
+
+def library_path() -> str:
+    return LIB
+
+
+class _Header(ctypes.Structure):
+    _fields_ = [("magic", ctypes.c_uint32), ("version", ctypes.c_uint32),
+                ("code_width", ctypes.c_uint32),
+                ("center", ctypes.c_float * 3), ("scale", ctypes.c_float),
+                ("per_coord_err", ctypes.c_float), ("g_min", ctypes.c_float * 3),
+                ("g_range", ctypes.c_float * 3), ("g_bits", ctypes.c_uint32 * 3),
+                ("pred_n", ctypes.c_int32 * 9), ("pred_k", ctypes.c_uint32 * 3),
+                ("n_v_total", ctypes.c_uint32), ("n_t", ctypes.c_uint32),
+                ("n_meshlets", ctypes.c_uint32), ("body_bit", ctypes.c_uint64)]
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        build()
+        lib = ctypes.CDLL(LIB)
+        u8p = ctypes.POINTER(ctypes.c_uint8)
+        lib.so_error.restype = ctypes.c_char_p
+        lib.so_error.argtypes = [ctypes.c_int]
+        lib.so_parse_header.argtypes = [u8p, ctypes.c_uint64, ctypes.POINTER(_Header)]
+        lib.so_decode.argtypes = [u8p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
+                                  ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64,
+                                  ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+        lib.so_decode_mt.argtypes = [u8p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+        lib.so_bitcodec_read.argtypes = [u8p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
+                                         ctypes.c_int32, ctypes.c_void_p]
+        _lib = lib
+    return _lib
+
+
+def _buf(data: bytes):
+    arr = np.frombuffer(data, dtype=np.uint8)
+    return arr, arr.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8))
+
+
+def _check(rc: int):
+    if rc != 0:
+        raise OracleError(rc, _load().so_error(rc).decode())
+
+
+@dataclass
+class Header:
+    code_width: int
+    center: np.ndarray
+    scale: float
+    per_coord_err: float
+    g_min: np.ndarray
+    g_range: np.ndarray
+    g_bits: np.ndarray
+    pred_n: np.ndarray
+    pred_k: np.ndarray
+    n_v_total: int
+    n_t: int
+    n_meshlets: int
+
+
+def parse_header(data: bytes) -> Header:
+    lib = _load()
+    arr, p = _buf(data)
+    h = _Header()
+    _check(lib.so_parse_header(p, len(arr), ctypes.byref(h)))
+    return Header(int(h.code_width), np.array(h.center[:], np.float32), float(h.scale),
+                  float(h.per_coord_err), np.array(h.g_min[:], np.float32),
+                  np.array(h.g_range[:], np.float32), np.array(h.g_bits[:], np.int64),
+                  np.array(h.pred_n[:], np.int64).reshape(3, 3), np.array(h.pred_k[:], np.int64),
+                  int(h.n_v_total), int(h.n_t), int(h.n_meshlets))
+
+
+def decode(data: bytes, *, with_codes: bool = False, slack: int = 1 << 16):
+    """Sequential decode -> (pos float32 (n_v, 3), idx int64 (n_t, 3)[, codes int64])."""
+    lib = _load()
+    h = parse_header(data)
+    arr, p = _buf(data)
+    cap_v = h.n_v_total + slack
+    cap_t = h.n_t + slack
+    pos = np.empty((cap_v, 3), np.float32)
+    idx = np.empty((cap_t, 3), np.int64)
+    codes = np.empty((cap_v, 3), np.int64) if with_codes else None
+    nv = ctypes.c_uint64()
+    nt = ctypes.c_uint64()
+    _check(lib.so_decode(p, len(arr), pos.ctypes.data, idx.ctypes.data,
+                         codes.ctypes.data if codes is not None else None,
+                         cap_v, cap_t, ctypes.byref(nv), ctypes.byref(nt)))
+    out = (pos[:nv.value], idx[:nt.value])
+    if with_codes:
+        out = out + (codes[:nv.value],)
+    return out
+
+
+def decode_mt(data: bytes, n_threads: int = 0, *, out=None):
+    """Meshlet-parallel decode on ``n_threads`` host threads (0 = all cores)."""
+    lib = _load()
+    h = parse_header(data)
+    arr, p = _buf(data)
+    if n_threads <= 0:
+        n_threads = os.cpu_count() or 1
+    if out is None:
+        pos = np.empty((h.n_v_total, 3), np.float32)
+        idx = np.empty((h.n_t, 3), np.int64)
+    else:
+        pos, idx = out
+    nv = ctypes.c_uint64()
+    nt = ctypes.c_uint64()
+    _check(lib.so_decode_mt(p, len(arr), pos.ctypes.data, idx.ctypes.data,
+                            pos.shape[0], idx.shape[0], n_threads,
+                            ctypes.byref(nv), ctypes.byref(nt)))
+    return pos[:nv.value], idx[:nt.value]
+
+
+def bitcodec_read(data: bytes, ops):
+    """Read fields: ops = [(kind, k), ...], kind 'fixed' | 'rice' | 'eg'."""
+    lib = _load()
+    arr, p = _buf(data)
+    kinds = np.array([{"fixed": 0, "rice": 1, "eg": 2}[o[0]] for o in ops], np.int32)
+    ks = np.array([o[1] for o in ops], np.int32)
+    out = np.zeros(len(ops), np.uint64)
+    _check(lib.so_bitcodec_read(p, len(arr), kinds.ctypes.data, ks.ctypes.data,
+                                len(ops), out.ctypes.data))
+    return [int(x) for x in out]

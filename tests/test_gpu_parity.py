@@ -1,0 +1,226 @@
+"""GPU decode through the C ABI, bit-exact against the oracle and the golden
+vectors of the reference decoder.
+
+Parity bar: triangle indices equal, float32 positions bit-identical, integer
+codes equal (exactness, no tolerance).
+"""
+import numpy as np
+import pytest
+
+import oracle
+from meshpress_gb300 import _lib, encoder, synth
+from tests import _golden, _meshes
+
+pytestmark = pytest.mark.gpu
+
+B12 = synth.bbox_bits_error(12)
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from meshpress_gb300 import _build
+    _build.build_decoder()
+    oracle.build()
+    return torch
+
+
+def gpu_decode(torch, data, cfg=None, codes=True):
+    from meshpress_gb300 import ParaDeltaV5GpuDecoder
+    dec = ParaDeltaV5GpuDecoder(data)
+    if cfg is not None:
+        dec.set_launch_config(cfg)
+    idx = torch.full((dec.n_t_total, 3), 0x7FFFFFFF, dtype=torch.int32, device="cuda")
+    pos = torch.full((dec.n_v_total, 3), float("nan"), dtype=torch.float32, device="cuda")
+    c = torch.full((dec.n_v_total, 3), -1, dtype=torch.int32, device="cuda") if codes else None
+    dec.decode_into(idx, pos, codes=c)
+    out = (pos.cpu().numpy(), idx.cpu().numpy().view(np.uint32))
+    if codes:
+        out = out + (c.cpu().numpy(),)
+    dec.close()
+    return out
+
+
+def assert_same_as_oracle(data, pos, idx, codes=None):
+    opos, oidx, ocodes = oracle.decode(data, with_codes=True)
+    bad = np.nonzero(pos.view(np.uint32) != opos.view(np.uint32))[0]
+    assert bad.size == 0, f"{bad.size} position rows differ (first {bad[:5]})"
+    assert np.array_equal(idx.astype(np.int64), oidx)
+    if codes is not None:
+        assert np.array_equal(codes.astype(np.int64), ocodes)
+
+
+@pytest.mark.parametrize("name", _golden.names())
+def test_golden_vectors_bit_exact(torch_cuda, name):
+    g = _golden.load(name)
+    pos, idx, codes = gpu_decode(torch_cuda, g["data"])
+    _golden.check_against(g, pos, idx, codes)
+
+
+def test_decode_to_host_and_device_agree(torch_cuda):
+    from meshpress_gb300 import ParaDeltaV5GpuDecoder
+    g = _golden.load("grid129_b12")
+    dec = ParaDeltaV5GpuDecoder(g["data"])
+    pos, idx = dec.decode_to_host()
+    assert pos.dtype == np.float32 and idx.dtype == np.uint32
+    _golden.check_against(g, pos, idx)
+    tris, verts = dec.decode_to_device()
+    assert tris.dtype == torch_cuda.uint32 and verts.dtype == torch_cuda.float32
+    assert np.array_equal(verts.cpu().numpy().view(np.uint32), pos.view(np.uint32))
+    assert np.array_equal(tris.view(torch_cuda.int32).cpu().numpy().view(np.uint32), idx)
+    # repeated decodes reuse buffers and stay identical
+    for _ in range(3):
+        p2, i2 = dec.decode_to_host()
+        assert np.array_equal(p2.view(np.uint32), pos.view(np.uint32)) and np.array_equal(i2, idx)
+
+
+ENC_CASES = {
+    "grid129_b12": (lambda: synth.heightfield_grid(129, seed=1), dict(precision_error=B12, precision_mode="bbox_frac")),
+    "grid257_b10": (lambda: synth.noise_heightfield(257, seed=5), dict(precision_error=synth.bbox_bits_error(10),
+                                                                      precision_mode="bbox_frac")),
+    "grid257_b14": (lambda: synth.noise_heightfield(257, seed=5), dict(precision_error=synth.bbox_bits_error(14),
+                                                                      precision_mode="bbox_frac")),
+    "grid257_b16": (lambda: synth.noise_heightfield(257, seed=5), dict(precision_error=synth.bbox_bits_error(16),
+                                                                      precision_mode="bbox_frac")),
+    "grid129_b20_wide": (lambda: synth.heightfield_grid(129, seed=6),
+                         dict(precision_error=synth.bbox_bits_error(20), precision_mode="bbox_frac")),
+    "ico5_shuffled_b12": (lambda: synth.icosphere(5, seed=2), dict(precision_error=B12, precision_mode="bbox_frac")),
+    "torus_b12_canon": (lambda: synth.torus(120, 45, R=4.0, r=1.0),
+                        dict(precision_error=B12, precision_mode="bbox_frac", predictor="canonical")),
+    "grid65_world": (lambda: synth.heightfield_grid(65, seed=2), dict(precision_error=0.0005)),
+    "small_meshlets": (lambda: synth.icosphere(4, seed=8), dict(precision_error=B12, precision_mode="bbox_frac",
+                                                               max_verts=40, max_tris=64)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(ENC_CASES))
+def test_encoded_meshes_match_oracle(torch_cuda, name):
+    make, kw = ENC_CASES[name]
+    V, T = make()
+    e = encoder.encode(V, T, **kw)
+    pos, idx, codes = gpu_decode(torch_cuda, e.data)
+    assert_same_as_oracle(e.data, pos, idx, codes)
+    assert np.array_equal(codes, e.codes)  # codes equal the encoder's input codes
+    assert _meshes.same_triangle_set(T, idx.astype(np.int64), e.l2g)
+    assert _meshes.crack_free(pos, e.l2g)
+    if name.startswith(("ico", "torus", "small")):
+        assert _meshes.welded_is_closed_manifold(pos, idx)
+
+
+def _cfg(w, pers, stage, code, per_sm=0):
+    c = _lib.LaunchCfg()
+    c.warps_per_cta, c.persistent, c.ctas_per_sm, c.stage_bytes, c.code_bytes = w, pers, per_sm, stage, code
+    return c
+
+
+@pytest.mark.parametrize("cfg", [
+    (1, 0, 20 * 1024, 40 * 1024), (2, 0, 16 * 1024, 32 * 1024), (4, 1, 12 * 1024, 24 * 1024),
+    (1, 1, 1024, 2048),          # tiny stage: whole groups fall back to global reads
+    (2, 0, 64 * 1024, 2048),     # tiny code store: one meshlet per round
+], ids=["w1", "w2", "w4p", "global_reads", "one_per_round"])
+def test_launch_shapes_give_identical_output(torch_cuda, cfg):
+    V, T = synth.icosphere(5, seed=11)
+    e = encoder.encode(V, T, precision_error=B12, precision_mode="bbox_frac")
+    pos, idx, codes = gpu_decode(torch_cuda, e.data, cfg=_cfg(*cfg))
+    assert_same_as_oracle(e.data, pos, idx, codes)
+
+
+def test_config_sweep_large_heightfield(torch_cuda):
+    """2049 x 2049 heightfield (8,388,608 triangles) at 12 bits: full-size
+    bit-exact decode against the oracle."""
+    V, T = synth.noise_heightfield(2049, seed=3)
+    e = encoder.encode(V, T, precision_error=B12, precision_mode="bbox_frac")
+    pos, idx, codes = gpu_decode(torch_cuda, e.data)
+    opos, oidx = oracle.decode_mt(e.data, 0)
+    assert np.array_equal(pos.view(np.uint32), opos.view(np.uint32))
+    assert np.array_equal(idx.astype(np.int64), oidx)
+    assert np.array_equal(codes, e.codes)
+    assert _meshes.crack_free(pos, e.l2g)
+
+
+def test_icosphere_level8(torch_cuda):
+    """Displaced, vertex-shuffled icosphere at level 8 (1,310,720 triangles)."""
+    V, T = synth.icosphere(8, seed=2)
+    e = encoder.encode(V, T, precision_error=B12, precision_mode="bbox_frac")
+    pos, idx, codes = gpu_decode(torch_cuda, e.data)
+    opos, oidx = oracle.decode_mt(e.data, 0)
+    assert np.array_equal(pos.view(np.uint32), opos.view(np.uint32))
+    assert np.array_equal(idx.astype(np.int64), oidx)
+    assert _meshes.welded_is_closed_manifold(pos, idx)
+
+
+# ---------------------------------------------------------------- errors ----
+
+def test_rejects_bad_magic_and_version(torch_cuda):
+    from meshpress_gb300 import ParaDeltaV5GpuDecoder
+    data = bytearray(_golden.load("grid33_b12")["data"])
+    bad = bytearray(data)
+    bad[0:4] = (0x504C4454).to_bytes(4, "big")
+    with pytest.raises(ValueError):
+        ParaDeltaV5GpuDecoder(bytes(bad))
+    bad = bytearray(data)
+    bad[4] = 4
+    with pytest.raises(ValueError):
+        ParaDeltaV5GpuDecoder(bytes(bad))
+    with pytest.raises(ValueError):
+        ParaDeltaV5GpuDecoder(bytes(data), meshlets_per_block=17)
+
+
+def _try_gpu(torch, data):
+    try:
+        return gpu_decode(torch, data, codes=False), None
+    except _lib.StrideFormatError as e:
+        return None, e
+
+
+def _try_oracle(data):
+    try:
+        return oracle.decode(data), None
+    except oracle.OracleError as e:
+        return None, e
+
+
+def test_truncated_and_offset_corruption(torch_cuda):
+    g = _golden.load("grid129_b12")
+    data = g["data"]
+    r, e = _try_gpu(torch_cuda, data[: len(data) - 200])
+    assert r is None and e is not None
+    bad = bytearray(data)
+    off = 86 + 4 * 5
+    bad[off:off + 4] = (int.from_bytes(bad[off:off + 4], "big") + 3).to_bytes(4, "big")
+    r, e = _try_gpu(torch_cuda, bytes(bad))
+    assert r is None and e.code in (_lib.STRIDE_ERR_OFFSET, _lib.STRIDE_ERR_CORRUPT)
+    bad = bytearray(data)
+    bad[86:90] = (0).to_bytes(4, "big")
+    r, e = _try_gpu(torch_cuda, bytes(bad))
+    assert r is None and e.code == _lib.STRIDE_ERR_OFFSET
+
+
+def test_bit_flip_fuzz(torch_cuda):
+    """Random single-bit corruptions: the GPU either rejects the stream or
+    returns exactly what the reference semantics (oracle) return; whenever
+    the oracle rejects, the GPU rejects too."""
+    g = _golden.load("grid33_b12")
+    data = g["data"]
+    rng = np.random.default_rng(123)
+    hdr_bits = (86 + 4 * 8) * 8
+    accepted = rejected = 0
+    for _ in range(120):
+        b = bytearray(data)
+        bit = int(rng.integers(hdr_bits, len(b) * 8))
+        b[bit >> 3] ^= 0x80 >> (bit & 7)
+        b = bytes(b)
+        gr, ge = _try_gpu(torch_cuda, b)
+        orr, oe = _try_oracle(b)
+        if oe is not None:
+            assert ge is not None, f"bit {bit}: oracle rejects ({oe}) but GPU accepted"
+        if ge is None:
+            accepted += 1
+            assert orr is not None
+            assert np.array_equal(gr[0].view(np.uint32), orr[0].view(np.uint32))
+            assert np.array_equal(gr[1].astype(np.int64), orr[1])
+        else:
+            rejected += 1
+    assert rejected > 0

@@ -1,0 +1,73 @@
+"""The C-ABI library loads without a GPU, exports every entry point that
+include/stride_gb300.h declares, and validates headers on the host."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import oracle
+from meshpress_gb300 import _build, _lib
+from tests import _golden
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(REPO, "include", "stride_gb300.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^[A-Za-z_][\w \*]*?\b(stride_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_library_builds_and_exports_every_declared_symbol(built_libs):
+    names = declared_functions()
+    assert len(names) >= 25
+    lib = ctypes.CDLL(_build.decoder_library())
+    for n in names:
+        assert hasattr(lib, n), f"{n} declared but not exported"
+    assert set(names) == {s[0] for s in _lib.SIGNATURES}
+
+
+def test_inspect_matches_oracle_header(built_libs):
+    for name in _golden.names():
+        data = _golden.load(name)["data"]
+        info = _lib.inspect(data)
+        h = oracle.parse_header(data)
+        assert info.n_meshlets == h.n_meshlets
+        assert info.n_v == h.n_v_total and info.n_t == h.n_t
+        assert list(info.g_bits) == list(h.g_bits)
+        assert list(info.pred_n) == h.pred_n.reshape(-1).tolist()
+        assert list(info.pred_k) == h.pred_k.tolist()
+
+
+def test_inspect_rejects_bad_streams(built_libs):
+    data = bytearray(_golden.load("grid33_b12")["data"])
+    bad = bytearray(data)
+    bad[0:4] = (0x504C4454).to_bytes(4, "big")  # a PLDT stream is not DPR4
+    with pytest.raises(_lib.StrideFormatError) as e:
+        _lib.inspect(bytes(bad))
+    assert e.value.code == _lib.STRIDE_ERR_MAGIC
+    bad = bytearray(data)
+    bad[4] = 2
+    with pytest.raises(_lib.StrideFormatError) as e:
+        _lib.inspect(bytes(bad))
+    assert e.value.code == _lib.STRIDE_ERR_VERSION
+    with pytest.raises(_lib.StrideFormatError) as e:
+        _lib.inspect(bytes(data[:50]))
+    assert e.value.code == _lib.STRIDE_ERR_TRUNCATED
+    with pytest.raises(_lib.StrideFormatError) as e:
+        _lib.inspect(bytes(data[:90]))  # offset table cut short
+    assert e.value.code == _lib.STRIDE_ERR_TRUNCATED
+    bad = bytearray(data)
+    bad[50] = 30  # 30-bit codes
+    with pytest.raises(_lib.StrideFormatError) as e:
+        _lib.inspect(bytes(bad))
+    assert e.value.code == _lib.STRIDE_ERR_UNSUPPORTED
+
+
+def test_decoder_fails_loudly_without_library(monkeypatch):
+    monkeypatch.setattr(_build, "DECODER_LIB", "/nonexistent/libstride_gb300.so")
+    monkeypatch.setattr(_lib, "_lib", None)
+    with pytest.raises(RuntimeError):
+        _lib.load()
