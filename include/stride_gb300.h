@@ -124,11 +124,11 @@ int stride_decode_host(stride_handle* h, void* stream, uint32_t* h_idx, float* h
 int stride_status(stride_handle* h, int wait, uint32_t* bad_meshlet);
 
 /* Measurement entry point (no reference counterpart): one decode like
- * stride_decode, with CUDA events recorded on `stream` around the parse
- * kernel and around the decode kernel; waits and returns both durations in
- * milliseconds. */
-int stride_decode_timed(stride_handle* h, void* stream, uint32_t* d_idx, float* d_pos,
-                        float* parse_ms, float* decode_ms);
+ * stride_decode, with CUDA events recorded on `stream` between its three
+ * kernels; waits and writes their durations in milliseconds to
+ * kernel_ms[0] (meshlet scan), kernel_ms[1] (connectivity) and
+ * kernel_ms[2] (vertices + output). */
+int stride_decode_timed(stride_handle* h, void* stream, uint32_t* d_idx, float* d_pos, float* kernel_ms);
 
 /* Launch shape for this handle's decodes (defaults are used until set). */
 int stride_set_config(stride_handle* h, const stride_launch_cfg* cfg);

@@ -89,8 +89,7 @@ SIGNATURES = [
     ("stride_decode", _I, [_P, _P, _P, _P, _P]),
     ("stride_decode_host", _I, [_P, _P, _P, _P]),
     ("stride_status", _I, [_P, _I, ctypes.POINTER(_U32)]),
-    ("stride_decode_timed", _I, [_P, _P, _P, _P, ctypes.POINTER(ctypes.c_float),
-                                 ctypes.POINTER(ctypes.c_float)]),
+    ("stride_decode_timed", _I, [_P, _P, _P, _P, _P]),
     ("stride_set_config", _I, [_P, ctypes.POINTER(LaunchCfg)]),
     ("stride_close", None, [_P]),
     ("stride_batch_create", _I, [_P, _P, _U32, ctypes.POINTER(_P)]),

@@ -140,8 +140,11 @@ struct stride_handle {
     MeshParams params;
     MeshParams* d_params = nullptr;
     MeshletDesc* d_descs = nullptr;
-    uint2* d_blk_sums = nullptr;
-    ulonglong2* d_blk_prefix = nullptr;
+    uint4* d_blk_sums = nullptr;
+    BlockPrefix* d_blk_prefix = nullptr;
+    uint32_t* d_tri_scratch = nullptr;
+    uint32_t* d_walk_scratch = nullptr;
+    unsigned long long tri_cap = 0, walk_cap = 0;
     Status* d_status = nullptr;
     uint32_t* d_idx = nullptr;
     float* d_pos = nullptr;
@@ -157,9 +160,14 @@ static void free_buffers(stride_handle* h) {
     cudaFree(h->d_descs);
     cudaFree(h->d_blk_sums);
     cudaFree(h->d_blk_prefix);
+    cudaFree(h->d_tri_scratch);
+    cudaFree(h->d_walk_scratch);
     cudaFree(h->d_status);
     cudaFree(h->d_idx);
     cudaFree(h->d_pos);
+    h->d_tri_scratch = nullptr;
+    h->d_walk_scratch = nullptr;
+    h->tri_cap = h->walk_cap = 0;
     h->d_blob = nullptr;
     h->d_params = nullptr;
     h->d_descs = nullptr;
@@ -170,8 +178,22 @@ static void free_buffers(stride_handle* h) {
     h->d_pos = nullptr;
 }
 
-static int ensure_capacity(stride_handle* h, size_t len, uint32_t n_meshlets) {
+static int ensure_capacity(stride_handle* h, size_t len, uint32_t n_meshlets, uint64_t n_v, uint64_t n_t) {
     cudaError_t e;
+    const unsigned long long tw = tri_scratch_words(n_t, n_meshlets);
+    const unsigned long long ww = walk_scratch_words(n_v, n_meshlets);
+    if (tw > h->tri_cap) {
+        cudaFree(h->d_tri_scratch);
+        h->d_tri_scratch = nullptr;
+        if ((e = cudaMalloc(&h->d_tri_scratch, 4ull * tw)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(scratch)");
+        h->tri_cap = tw;
+    }
+    if (ww > h->walk_cap) {
+        cudaFree(h->d_walk_scratch);
+        h->d_walk_scratch = nullptr;
+        if ((e = cudaMalloc(&h->d_walk_scratch, 4ull * ww)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(scratch)");
+        h->walk_cap = ww;
+    }
     if (blob_alloc_bytes(len) > h->cap_bytes) {
         cudaFree(h->d_blob);
         h->d_blob = nullptr;
@@ -185,10 +207,10 @@ static int ensure_capacity(stride_handle* h, size_t len, uint32_t n_meshlets) {
         h->d_descs = nullptr;
         h->d_blk_sums = nullptr;
         h->d_blk_prefix = nullptr;
-        const uint32_t nb = parse_blocks(n_meshlets);
+        const uint32_t nb = scan_blocks(n_meshlets);
         if ((e = cudaMalloc(&h->d_descs, sizeof(MeshletDesc) * n_meshlets)) != cudaSuccess ||
-            (e = cudaMalloc(&h->d_blk_sums, sizeof(uint2) * nb)) != cudaSuccess ||
-            (e = cudaMalloc(&h->d_blk_prefix, sizeof(ulonglong2) * nb)) != cudaSuccess)
+            (e = cudaMalloc(&h->d_blk_sums, sizeof(uint4) * nb)) != cudaSuccess ||
+            (e = cudaMalloc(&h->d_blk_prefix, sizeof(BlockPrefix) * nb)) != cudaSuccess)
             return cuda_fail(e, "cudaMalloc(scratch)");
         h->cap_meshlets = n_meshlets;
     }
@@ -263,7 +285,7 @@ int stride_open(const uint8_t* data, size_t len, stride_handle** out) {
     h->params = p;
     h->len = len;
     cudaError_t e;
-    if ((rc = ensure_capacity(h, len, p.n_meshlets)) != STRIDE_OK) {
+    if ((rc = ensure_capacity(h, len, p.n_meshlets, p.n_v, p.n_t)) != STRIDE_OK) {
         free_buffers(h);
         delete h;
         return rc;
@@ -289,7 +311,7 @@ int stride_reload(stride_handle* h, const uint8_t* data, size_t len, void* strea
     char why[256] = {0};
     int rc = parse_header(data, len, &p, why, sizeof(why));
     if (rc) return fail(rc, "%s", why);
-    if ((rc = ensure_capacity(h, len, p.n_meshlets)) != STRIDE_OK) return rc;
+    if ((rc = ensure_capacity(h, len, p.n_meshlets, p.n_v, p.n_t)) != STRIDE_OK) return rc;
     h->params = p;
     h->len = len;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -318,6 +340,10 @@ static DecodeArgs handle_args(stride_handle* h, uint32_t* d_idx, float* d_pos, i
     a.descs = h->d_descs;
     a.blk_sums = h->d_blk_sums;
     a.blk_prefix = h->d_blk_prefix;
+    a.tri_scratch = h->d_tri_scratch;
+    a.walk_scratch = h->d_walk_scratch;
+    a.tri_cap = h->tri_cap;
+    a.walk_cap = h->walk_cap;
     a.status = h->d_status;
     a.idx = d_idx;
     a.pos = d_pos;
@@ -326,25 +352,20 @@ static DecodeArgs handle_args(stride_handle* h, uint32_t* d_idx, float* d_pos, i
     return a;
 }
 
-int stride_decode_timed(stride_handle* h, void* stream, uint32_t* d_idx, float* d_pos, float* parse_ms,
-                        float* decode_ms) {
+int stride_decode_timed(stride_handle* h, void* stream, uint32_t* d_idx, float* d_pos, float* kernel_ms) {
     if (!h || !d_idx || !d_pos) return fail(STRIDE_ERR_ARG, "null argument");
-    cudaEvent_t ev[3];
+    cudaEvent_t ev[4];
     for (auto& e : ev) cudaEventCreate(&e);
-    void* evp[3] = {ev[0], ev[1], ev[2]};
+    void* evp[4] = {ev[0], ev[1], ev[2], ev[3]};
     int rc = enqueue_decode(handle_args(h, d_idx, d_pos, nullptr), h->cfg, stream, evp);
     if (rc == STRIDE_OK) {
         cudaEventRecord(h->done, static_cast<cudaStream_t>(stream));
         h->launched = true;
-        cudaError_t e = cudaEventSynchronize(ev[2]);
+        cudaError_t e = cudaEventSynchronize(ev[3]);
         if (e != cudaSuccess) {
             rc = cuda_fail(e, "stride_decode_timed");
-        } else {
-            float a = 0.f, b = 0.f;
-            cudaEventElapsedTime(&a, ev[0], ev[1]);
-            cudaEventElapsedTime(&b, ev[1], ev[2]);
-            if (parse_ms) *parse_ms = a;
-            if (decode_ms) *decode_ms = b;
+        } else if (kernel_ms) {
+            for (int i = 0; i < 3; i++) cudaEventElapsedTime(&kernel_ms[i], ev[i], ev[i + 1]);
         }
     } else {
         rc = fail(rc, "decode launch failed");

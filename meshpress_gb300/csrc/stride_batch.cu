@@ -24,8 +24,11 @@ struct stride_batch {
     MeshParams* d_params = nullptr;
     uint32_t* d_meshlet_mesh = nullptr;
     MeshletDesc* d_descs = nullptr;
-    uint2* d_blk_sums = nullptr;
-    ulonglong2* d_blk_prefix = nullptr;
+    uint4* d_blk_sums = nullptr;
+    BlockPrefix* d_blk_prefix = nullptr;
+    uint32_t* d_tri_scratch = nullptr;
+    uint32_t* d_walk_scratch = nullptr;
+    unsigned long long tri_cap = 0, walk_cap = 0;
     Status* d_status = nullptr;
     bool wide = false;
     LaunchCfg cfg;
@@ -81,6 +84,8 @@ static void batch_free(stride_batch* b) {
     cudaFree(b->d_descs);
     cudaFree(b->d_blk_sums);
     cudaFree(b->d_blk_prefix);
+    cudaFree(b->d_tri_scratch);
+    cudaFree(b->d_walk_scratch);
     cudaFree(b->d_status);
 }
 
@@ -94,6 +99,10 @@ static DecodeArgs batch_args(const stride_batch* b, uint32_t* d_idx, float* d_po
     a.descs = b->d_descs;
     a.blk_sums = b->d_blk_sums;
     a.blk_prefix = b->d_blk_prefix;
+    a.tri_scratch = b->d_tri_scratch;
+    a.walk_scratch = b->d_walk_scratch;
+    a.tri_cap = b->tri_cap;
+    a.walk_cap = b->walk_cap;
     a.status = b->d_status;
     a.idx = d_idx;
     a.pos = d_pos;
@@ -136,13 +145,15 @@ int stride_batch_create(const uint8_t* const* blobs, const size_t* lens, uint32_
         return rc;
     }
     if (b->wide) b->cfg.code_bytes = std::max<uint32_t>(b->cfg.code_bytes, kMaxLocal * 16u);
+    b->tri_cap = tri_scratch_words(b->total_t, b->total_meshlets);
+    b->walk_cap = walk_scratch_words(b->total_v, b->total_meshlets);
     std::vector<uint8_t> arena(arena_bytes, 0);
     for (uint32_t i = 0; i < n_meshes; i++) std::memcpy(arena.data() + off[i], blobs[i], lens[i]);
     std::vector<uint32_t> mm(b->total_meshlets);
     for (uint32_t i = 0; i < n_meshes; i++)
         std::fill(mm.begin() + b->params[i].meshlet_begin,
                   mm.begin() + b->params[i].meshlet_begin + b->params[i].n_meshlets, i);
-    const uint32_t nb = parse_blocks(b->total_meshlets);
+    const uint32_t nb = scan_blocks(b->total_meshlets);
     cudaError_t e;
     if ((e = cudaMalloc(&b->d_arena, arena_bytes)) != cudaSuccess ||
         (e = cudaMalloc(&b->d_params, sizeof(MeshParams) * n_meshes)) != cudaSuccess ||
@@ -150,8 +161,10 @@ int stride_batch_create(const uint8_t* const* blobs, const size_t* lens, uint32_
             cudaSuccess ||
         (e = cudaMalloc(&b->d_descs, sizeof(MeshletDesc) * std::max<uint32_t>(1u, b->total_meshlets))) !=
             cudaSuccess ||
-        (e = cudaMalloc(&b->d_blk_sums, sizeof(uint2) * std::max<uint32_t>(1u, nb))) != cudaSuccess ||
-        (e = cudaMalloc(&b->d_blk_prefix, sizeof(ulonglong2) * std::max<uint32_t>(1u, nb))) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_blk_sums, sizeof(uint4) * std::max<uint32_t>(1u, nb))) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_blk_prefix, sizeof(BlockPrefix) * std::max<uint32_t>(1u, nb))) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_tri_scratch, 4ull * b->tri_cap)) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_walk_scratch, 4ull * b->walk_cap)) != cudaSuccess ||
         (e = cudaMalloc(&b->d_status, sizeof(Status))) != cudaSuccess ||
         (e = cudaMemcpy(b->d_arena, arena.data(), arena_bytes, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(b->d_params, b->params.data(), sizeof(MeshParams) * n_meshes, cudaMemcpyHostToDevice)) !=
@@ -257,8 +270,8 @@ int stride_batch_autotune(stride_batch* b, void* stream, uint32_t* d_idx, float*
     if (iters < 1) iters = 3;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     std::vector<LaunchCfg> cands;
-    const uint32_t stage_opts[] = {12u * 1024u, 16u * 1024u, 20u * 1024u, 24u * 1024u};
-    const uint32_t code_opts[] = {24u * 1024u, 32u * 1024u, 40u * 1024u, 48u * 1024u};
+    const uint32_t stage_opts[] = {8u * 1024u, 12u * 1024u, 16u * 1024u, 24u * 1024u};
+    const uint32_t code_opts[] = {16u * 1024u, 24u * 1024u, 32u * 1024u, 48u * 1024u};
     for (int w : {1, 2, 4})
         for (uint32_t st : stage_opts)
             for (uint32_t cb : code_opts)
@@ -268,12 +281,8 @@ int stride_batch_autotune(stride_batch* b, void* stream, uint32_t* d_idx, float*
                     c.stage_bytes = st;
                     c.code_bytes = cb;
                     c.persistent = pers;
+                    c.ctas_per_sm = 0;  // persistent grid sized by the occupancy calculator
                     if (check_config(c, b->wide)) continue;
-                    if (pers) {
-                        const size_t per_cta = decode_smem_bytes(c, b->wide);
-                        const int fit = static_cast<int>((228u * 1024u) / (per_cta + 1024u));
-                        c.ctas_per_sm = std::max(1, fit);
-                    }
                     cands.push_back(c);
                 }
     cudaEvent_t e0, e1;

@@ -25,9 +25,7 @@ constexpr int kFifo = 16;        // REUSE_BUF_SIZE (encoder/paradelta_codec.py:1
 constexpr int kReuseBits = 5;    // _REUSE_BITS (encoder/paradelta_codec.py:128)
 constexpr int kMaxResidK = 24;   // largest residual k this decoder accepts
 constexpr int kMaxGBits = 24;    // largest per-axis code width this decoder accepts
-constexpr int kScanThreads = 256;  // meshlets per parse block
-constexpr int kRing = 32;          // triangles buffered per lane between flushes
-constexpr int kRingStride = kRing + 1;
+constexpr int kScanThreads = 256;  // meshlets per scan block
 constexpr int kBlobPad = 64;       // zero bytes after every device copy of a stream
 
 // Internal status codes (negated public STRIDE_ERR_* values).
@@ -57,33 +55,40 @@ struct MeshParams {
     stride_dequant_axis dq[3];
 };
 
-// Per-meshlet decode plan written by the parse kernel (64 bytes).
+// Per-meshlet record: the scan kernel writes the first part, the
+// connectivity kernel the walk facts (64 bytes).
 struct __align__(16) MeshletDesc {
-    uint32_t conn_bit;     // first strip header
-    uint32_t anchor_bit;   // anchor codes (end of connectivity)
-    uint32_t res_bit[6];   // starts of dx, dy, dz, px, py, pz
+    uint32_t start_bit;    // meshlet header (offset table entry)
+    uint32_t end_bit;      // next meshlet's offset (or the stream end)
     uint32_t counts0;      // n_local | n_tris << 16
-    uint32_t counts1;      // n_strips | n_delta << 16
-    uint32_t counts2;      // n_para
-    uint32_t tk_delta;     // 3 x 8 bits: 0x80 = Exp-Golomb, low 6 bits = k
-    uint32_t tk_para;
-    uint32_t v_pref;       // exclusive prefix of n_local inside the parse block
-    uint32_t t_pref;       // exclusive prefix of n_tris inside the parse block
-    uint32_t end_bit;      // first bit after the meshlet
+    uint32_t n_strips;
+    uint32_t v_pref;       // exclusive prefixes inside the scan block:
+    uint32_t t_pref;       //   n_local, n_tris,
+    uint32_t tp_pref;      //   n_tris rounded up to 4 (triangle scratch),
+    uint32_t wp_pref;      //   n_local rounded up to 4 (walk scratch)
+    uint32_t anchor_bit;   // end of connectivity = anchor codes
+    uint32_t walk;         // n_kind0 | n_walk << 16
+    uint32_t pad[6];
+};
+
+struct BlockPrefix {
+    unsigned long long v, t, tp, wp;
 };
 
 struct Status {
     unsigned long long err;  // ((uint64)code << 32) | meshlet; first error wins
-    unsigned int ticket;     // parse blocks finished (last one scans block sums)
-    unsigned int work;       // persistent decode work counter
+    unsigned int ticket;     // scan blocks finished (the last one scans block sums)
+    unsigned int work_conn;  // persistent work counters
+    unsigned int work_vert;
+    unsigned int pad[3];
 };
 
 struct LaunchCfg {
-    int warps_per_cta = 1;
-    int persistent = 0;
+    int warps_per_cta = 2;
+    int persistent = 1;
     int ctas_per_sm = 0;
-    uint32_t stage_bytes = 20 * 1024;  // per-warp payload staging
-    uint32_t code_bytes = 40 * 1024;   // per-warp integer code storage
+    uint32_t stage_bytes = 16 * 1024;  // per-warp payload staging
+    uint32_t code_bytes = 32 * 1024;   // per-warp integer code planes (vertex kernel)
 };
 
 struct DecodeArgs {
@@ -93,8 +98,12 @@ struct DecodeArgs {
     uint32_t total_meshlets;
     uint32_t n_meshes;
     MeshletDesc* descs;              // device scratch, total_meshlets
-    uint2* blk_sums;                 // device scratch, parse blocks
-    ulonglong2* blk_prefix;          // device scratch, parse blocks
+    uint4* blk_sums;                 // device scratch, scan blocks
+    BlockPrefix* blk_prefix;         // device scratch, scan blocks
+    uint32_t* tri_scratch;           // packed local triangles, 4-aligned per meshlet
+    uint32_t* walk_scratch;          // walk entries, 4-aligned per meshlet
+    unsigned long long tri_cap;      // words in tri_scratch
+    unsigned long long walk_cap;     // words in walk_scratch
     Status* status;                  // device
     uint32_t* idx;                   // device outputs
     float* pos;
@@ -102,24 +111,32 @@ struct DecodeArgs {
     bool wide_codes;                 // some mesh has g_bits > 16
 };
 
-inline uint32_t parse_blocks(uint32_t total_meshlets) {
+inline uint32_t scan_blocks(uint32_t total_meshlets) {
     return (total_meshlets + kScanThreads - 1) / kScanThreads;
+}
+
+// Scratch words needed for a stream set with these totals.
+inline unsigned long long tri_scratch_words(unsigned long long n_t, unsigned long long meshlets) {
+    return n_t + 3ull * meshlets + 4ull;
+}
+inline unsigned long long walk_scratch_words(unsigned long long n_v, unsigned long long meshlets) {
+    return n_v + 3ull * meshlets + 4ull;
 }
 
 // Host-side header parse + kernel parameters; returns 0 or a STRIDE_ERR_*.
 int parse_header(const uint8_t* data, size_t len, MeshParams* p, char* why, size_t why_len);
 
-// Enqueue parse + decode for `a` on `stream`.  When `ev` is non-null, the
-// three events are recorded before the parse kernel, between the kernels and
-// after the decode kernel.
+// Enqueue scan + connectivity + vertex kernels for `a` on `stream`.  When
+// `ev` is non-null, four events are recorded: before the scan kernel,
+// after it, after the connectivity kernel and after the vertex kernel.
 int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void* const* ev = nullptr);
 
-// STRIDE_OK when `cfg` is a launchable shape (warps 1/2/4, budgets large
-// enough for one 256-vertex meshlet, CTA shared memory <= 227 KB).
+// STRIDE_OK when `cfg` is a launchable shape.
 int check_config(const LaunchCfg& cfg, bool wide);
 
-// Smem bytes one CTA of the decode kernel needs.
-size_t decode_smem_bytes(const LaunchCfg& cfg, bool wide);
+// Shared memory one CTA of each kernel needs.
+size_t conn_smem_bytes(const LaunchCfg& cfg);
+size_t vert_smem_bytes(const LaunchCfg& cfg);
 
 int device_sm_count();
 

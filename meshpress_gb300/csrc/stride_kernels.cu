@@ -1,31 +1,35 @@
 // STRIDE (DPR4 v3) decode kernels for sm_103a.
 //
-// Two launches per decode:
+// Three launches per decode (a memset of the status word comes first):
 //
-//  1. parse_kernel -- one thread per meshlet.  Reads the meshlet's offset
-//     table entry and 48-bit header, walks its strip connectivity (token
-//     widths only; first-occurrence counting gives n_delta / n_para), skips
-//     the six residual substreams to find their start bits (the side table
-//     that the reference GPU bench reads from encoder metadata instead,
-//     bench_cpp/stride_dup_decode_bench.cu:21-43), validates everything
-//     against the offset table, and runs a device-wide exclusive scan of
-//     n_local / n_tris: a block scan plus a last-block scan of block sums.
+//  1. scan_kernel -- one thread per meshlet: offset table entry + 48-bit
+//     meshlet header (n_local, n_tris, n_strips), range checks, and a
+//     device-wide exclusive scan of n_local / n_tris (output placement) and
+//     of their multiples of four (scratch placement): block scans plus a
+//     last-block scan of the block sums.
 //
-//  2. decode_kernel -- a warp decodes 32 consecutive meshlets.  One bulk
-//     copy (cp.async.bulk + mbarrier) stages the group's payload bytes in
-//     shared memory.  Each lane then replays one meshlet: strip walk with the
-//     16-entry move-to-tail FIFO held in four registers, first-occurrence
-//     walk, IRLP prediction in int32 and residual decode from the staged
-//     bits (the serial work of decode_dup, encoder/paradelta_v5_dup.py:
-//     507-600, spread over 32 meshlets instead of one lane of a warp).
-//     Triangles go through a per-lane ring in shared memory and integer codes
-//     through per-lane shared storage; both are written out warp-cooperatively
-//     with 128-bit stores, positions after exact dequantisation
-//     (stride_dequant.h).
+//  2. conn_kernel -- a warp owns 32 consecutive meshlets, one per lane.  One
+//     bulk copy (cp.async.bulk + mbarrier) stages the group's bytes in
+//     shared memory; each lane replays its meshlet's strip connectivity
+//     (decode_dup's strip loop, encoder/paradelta_v5_dup.py:513-542) with the
+//     16-entry move-to-tail FIFO (_read_vert, encoder/paradelta_codec.py:
+//     330-340) held in registers, writes packed local triangles and the
+//     first-occurrence walk (vertex, kind, IRLP references) to scratch with
+//     16-byte stores, and records where the connectivity ends (the anchor).
+//
+//  3. vert_kernel -- same warp/lane mapping.  Each lane bulk-copies its
+//     meshlet's residual bits (anchor to end) into shared memory, skips the
+//     three delta substreams to find the first parallelogram substream, then
+//     reconstructs the integer codes one axis at a time in walk order (IRLP,
+//     encoder/paradelta_v5_dup.py:91-104 and 581-600; every walk entry reads
+//     one residual, so all lanes do the same work per step).  The warp then
+//     writes each meshlet's triangles (global ids) and positions (exact
+//     dequantisation, stride_dequant.h) with coalesced 128-bit stores.
 #include <cuda_runtime.h>
 
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 
 #include "stride_common.cuh"
 #include "stride_gb300.h"
@@ -111,184 +115,8 @@ __device__ __forceinline__ int32_t unzigzag(uint32_t u) {
     return static_cast<int32_t>((u >> 1) ^ (0u - (u & 1u)));
 }
 
-// ---------------------------------------------------------------------------
-// Parse kernel
-// ---------------------------------------------------------------------------
-__device__ int parse_meshlet(const uint8_t* __restrict__ arena, const MeshParams& P, uint32_t lm,
-                             MeshletDesc& d, uint32_t* seen /* stride kScanThreads */) {
-    const uint32_t* w = reinterpret_cast<const uint32_t*>(arena + P.blob_off);
-    const uint32_t nbits = static_cast<uint32_t>(P.nbits);
-    const uint32_t tbit = kHeaderBytes * 8u;
-    const uint32_t off = peek32<false>(w, tbit + 32u * lm);
-    const uint32_t next = (lm + 1u < P.n_meshlets) ? peek32<false>(w, tbit + 32u * (lm + 1u)) : nbits;
-    if ((lm == 0u && off != P.body_bit) || off < P.body_bit || next > nbits || next < off + 48u ||
-        off + 48u < off)
-        return kErrOffset;
-    uint32_t pos = off;
-    const uint32_t h0 = peek32<false>(w, pos);
-    const uint32_t n_local = h0 >> 16;
-    const uint32_t n_tris = h0 & 0xFFFFu;
-    const uint32_t n_strips = peek32<false>(w, pos + 32u) >> 16;
-    pos += 48u;
-    if (n_local > static_cast<uint32_t>(kMaxLocal) || n_tris > static_cast<uint32_t>(kMaxTris))
-        return kErrUnsupported;
-    if (n_strips > n_tris) return kErrCorrupt;  // every strip emits >= 1 triangle
-    const uint32_t ib = max(1u, 32u - __clz(n_local));
-#pragma unroll
-    for (int i = 0; i < 8; i++) seen[i * kScanThreads] = 0u;
-    uint32_t nseen = 0u, k0 = 0u, k1 = 0u, tris = 0u;
-    for (uint32_t s = 0; s < n_strips; s++) {
-        if (pos + 16u > next) return kErrCorrupt;
-        const uint32_t len = peek32<false>(w, pos) >> 16;
-        pos += 16u;
-        const uint32_t body = len > 1u ? len - 1u : 0u;
-        tris += 1u + body;
-        if (tris > n_tris) return kErrCorrupt;
-        const uint32_t ntok = 3u + body;
-        for (uint32_t j = 0; j < ntok; j++) {
-            uint32_t x = peek32<false>(w, pos);
-            if (j >= 3u) {
-                x <<= 1;
-                pos += 1u;
-            }
-            if (x >> 31) {
-                const uint32_t v = (x << 1) >> (32u - ib);
-                pos += 1u + ib;
-                if (v >= n_local) return kErrCorrupt;
-                uint32_t& sw = seen[(v >> 5) * kScanThreads];
-                const uint32_t bit = 1u << (v & 31u);
-                if (!(sw & bit)) {
-                    sw |= bit;
-                    nseen++;
-                    if (j < 3u) k0++; else k1++;
-                }
-            } else {
-                const uint32_t fi = (x << 1) >> 27;
-                pos += 6u;
-                if (fi >= min(nseen, static_cast<uint32_t>(kFifo))) return kErrCorrupt;
-            }
-            if (pos > next) return kErrCorrupt;
-        }
-    }
-    if (tris != n_tris) return kErrCorrupt;
-    d.anchor_bit = pos;
-    pos += P.anchor_bits;
-    uint32_t tk[6];
-#pragma unroll
-    for (int i = 0; i < 6; i++) {
-        const uint32_t t = peek32<false>(w, pos) >> 16;
-        pos += 16u;
-        const uint32_t k = t & 0xFFu;
-        if (k > static_cast<uint32_t>(kMaxResidK)) return kErrUnsupported;
-        tk[i] = ((t >> 8) == 1u ? 0u : 0x80u) | k;
-    }
-    if (pos > next) return kErrCorrupt;
-    const uint32_t n_delta = k0 ? k0 - 1u : 0u;
-    const uint32_t n_para = k1;
-#pragma unroll 1
-    for (int s = 0; s < 6; s++) {
-        d.res_bit[s] = pos;
-        const uint32_t n = s < 3 ? n_delta : n_para;
-        for (uint32_t i = 0; i < n; i++) {
-            uint32_t u;
-            const int e = read_code<false>(w, 0u, pos, tk[s], next, u);
-            if (e) return e;
-        }
-    }
-    if ((lm + 1u < P.n_meshlets) ? (pos != next) : (pos > next)) return kErrCorrupt;
-    d.conn_bit = off + 48u;
-    d.counts0 = n_local | (n_tris << 16);
-    d.counts1 = n_strips | (n_delta << 16);
-    d.counts2 = n_para;
-    d.tk_delta = tk[0] | (tk[1] << 8) | (tk[2] << 16);
-    d.tk_para = tk[3] | (tk[4] << 8) | (tk[5] << 16);
-    d.end_bit = pos;
-    return 0;
-}
-
-// Exclusive scan over the block; returns the thread's prefix and the total.
-__device__ __forceinline__ unsigned long long block_scan(unsigned long long x, unsigned long long* wsum,
-                                                         unsigned long long& total) {
-    const int lane = threadIdx.x & 31;
-    const int warp = threadIdx.x >> 5;
-    constexpr int kWarps = kScanThreads / 32;
-    unsigned long long inc = x;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const unsigned long long t = __shfl_up_sync(kFull, inc, o);
-        if (lane >= o) inc += t;
-    }
-    if (lane == 31) wsum[warp] = inc;
-    __syncthreads();
-    if (warp == 0) {
-        unsigned long long v = lane < kWarps ? wsum[lane] : 0ull;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const unsigned long long t = __shfl_up_sync(kFull, v, o);
-            if (lane >= o) v += t;
-        }
-        if (lane < kWarps) wsum[lane] = v;
-    }
-    __syncthreads();
-    const unsigned long long excl = inc - x + (warp ? wsum[warp - 1] : 0ull);
-    total = wsum[kWarps - 1];
-    __syncthreads();
-    return excl;
-}
-
-__global__ void __launch_bounds__(kScanThreads) parse_kernel(DecodeArgs a) {
-    __shared__ uint32_t seen[8 * kScanThreads];
-    __shared__ unsigned long long wsum[kScanThreads / 32];
-    __shared__ int is_last;
-    const uint32_t tid = threadIdx.x;
-    const uint32_t m = blockIdx.x * kScanThreads + tid;
-    uint32_t nl = 0u, nt = 0u;
-    MeshletDesc d;
-    bool ok = false;
-    if (m < a.total_meshlets) {
-        const uint32_t mi = a.meshlet_mesh ? __ldg(a.meshlet_mesh + m) : 0u;
-        const MeshParams& P = a.meshes[mi];
-        const int e = parse_meshlet(a.arena, P, m - P.meshlet_begin, d, seen + tid);
-        if (e) {
-            report(a.status, e, m);
-        } else {
-            ok = true;
-            nl = d.counts0 & 0xFFFFu;
-            nt = d.counts0 >> 16;
-        }
-    }
-    const unsigned long long x = (static_cast<unsigned long long>(nt) << 32) | nl;
-    unsigned long long total;
-    const unsigned long long ex = block_scan(x, wsum, total);
-    if (ok) {
-        d.v_pref = static_cast<uint32_t>(ex);
-        d.t_pref = static_cast<uint32_t>(ex >> 32);
-        uint4* dst = reinterpret_cast<uint4*>(a.descs + m);
-        const uint4* src = reinterpret_cast<const uint4*>(&d);
-        dst[0] = src[0];
-        dst[1] = src[1];
-        dst[2] = src[2];
-        dst[3] = src[3];
-    }
-    if (tid == 0) a.blk_sums[blockIdx.x] = make_uint2(static_cast<uint32_t>(total), static_cast<uint32_t>(total >> 32));
-    // The last block to finish turns the block sums into block prefixes.
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) is_last = atomicAdd(&a.status->ticket, 1u) == gridDim.x - 1u;
-    __syncthreads();
-    if (!is_last) return;
-    __threadfence();
-    unsigned long long cv = 0ull, ct = 0ull;
-    for (uint32_t base = 0; base < gridDim.x; base += kScanThreads) {
-        const uint32_t i = base + tid;
-        const uint2 s = i < gridDim.x ? __ldcg(a.blk_sums + i) : make_uint2(0u, 0u);
-        unsigned long long tv, tt;
-        const unsigned long long ev = block_scan(s.x, wsum, tv);
-        const unsigned long long et = block_scan(s.y, wsum, tt);
-        if (i < gridDim.x) a.blk_prefix[i] = make_ulonglong2(cv + ev, ct + et);
-        cv += tv;
-        ct += tt;
-    }
+__device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int src) {
+    return __shfl_sync(kFull, v, src);
 }
 
 // ---------------------------------------------------------------------------
@@ -303,12 +131,15 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
-    unsigned long long gsrc;
-    asm volatile("cvta.to.global.u64 %0, %1;" : "=l"(gsrc) : "l"(src));
+__device__ __forceinline__ void mbar_expect(uint64_t* bar, uint32_t bytes) {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
                  : "memory");
+}
+
+__device__ __forceinline__ void bulk_copy(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    unsigned long long gsrc;
+    asm volatile("cvta.to.global.u64 %0, %1;" : "=l"(gsrc) : "l"(src));
     asm volatile(
         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
             smem_addr(dst)),
@@ -357,13 +188,425 @@ __device__ __forceinline__ void warp_store_words(uint32_t* dst, uint32_t n, F f,
     if (static_cast<uint32_t>(lane) < n - t0) dst[t0 + lane] = f(t0 + lane);
 }
 
-__device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int src) {
-    return __shfl_sync(kFull, v, src);
+// ---------------------------------------------------------------------------
+// 1. scan kernel
+// ---------------------------------------------------------------------------
+__device__ int scan_meshlet(const uint8_t* __restrict__ arena, const MeshParams& P, uint32_t lm, MeshletDesc& d) {
+    const uint32_t* w = reinterpret_cast<const uint32_t*>(arena + P.blob_off);
+    const uint32_t nbits = static_cast<uint32_t>(P.nbits);
+    const uint32_t tbit = kHeaderBytes * 8u;
+    const uint32_t off = peek32<false>(w, tbit + 32u * lm);
+    const uint32_t next = (lm + 1u < P.n_meshlets) ? peek32<false>(w, tbit + 32u * (lm + 1u)) : nbits;
+    // decode_dup reads meshlets back to back from the end of the table, so
+    // the table must start there and increase (paradelta_v5_dup.py:496-507)
+    if ((lm == 0u && off != P.body_bit) || off < P.body_bit || next > nbits || off > nbits - 48u ||
+        next < off + 48u)
+        return kErrOffset;
+    const uint32_t h0 = peek32<false>(w, off);
+    const uint32_t n_local = h0 >> 16;
+    const uint32_t n_tris = h0 & 0xFFFFu;
+    const uint32_t n_strips = peek32<false>(w, off + 32u) >> 16;
+    if (n_local > static_cast<uint32_t>(kMaxLocal) || n_tris > static_cast<uint32_t>(kMaxTris))
+        return kErrUnsupported;
+    if (n_strips > n_tris) return kErrCorrupt;  // every strip emits >= 1 triangle
+    d.start_bit = off;
+    d.end_bit = next;
+    d.counts0 = n_local | (n_tris << 16);
+    d.n_strips = n_strips;
+    return 0;
+}
+
+// Exclusive scan over the block; returns the thread's prefix and the total.
+__device__ __forceinline__ unsigned long long block_scan(unsigned long long x, unsigned long long* wsum,
+                                                         unsigned long long& total) {
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    constexpr int kWarps = kScanThreads / 32;
+    unsigned long long inc = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned long long t = __shfl_up_sync(kFull, inc, o);
+        if (lane >= o) inc += t;
+    }
+    if (lane == 31) wsum[warp] = inc;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned long long v = lane < kWarps ? wsum[lane] : 0ull;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned long long t = __shfl_up_sync(kFull, v, o);
+            if (lane >= o) v += t;
+        }
+        if (lane < kWarps) wsum[lane] = v;
+    }
+    __syncthreads();
+    const unsigned long long excl = inc - x + (warp ? wsum[warp - 1] : 0ull);
+    total = wsum[kWarps - 1];
+    __syncthreads();
+    return excl;
+}
+
+__global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a) {
+    __shared__ unsigned long long wsum[kScanThreads / 32];
+    __shared__ int is_last;
+    const uint32_t tid = threadIdx.x;
+    const uint32_t m = blockIdx.x * kScanThreads + tid;
+    uint32_t nl = 0u, nt = 0u;
+    MeshletDesc d;
+    memset(&d, 0, sizeof(d));
+    if (m < a.total_meshlets) {
+        const uint32_t mi = a.meshlet_mesh ? __ldg(a.meshlet_mesh + m) : 0u;
+        const MeshParams& P = a.meshes[mi];
+        const int e = scan_meshlet(a.arena, P, m - P.meshlet_begin, d);
+        if (e) {
+            report(a.status, e, m);
+            d.counts0 = 0u;  // keeps the prefixes finite; the decode is abandoned
+        } else {
+            nl = d.counts0 & 0xFFFFu;
+            nt = d.counts0 >> 16;
+        }
+    }
+    unsigned long long t1, t2;
+    const unsigned long long e1 = block_scan((static_cast<unsigned long long>(nt) << 32) | nl, wsum, t1);
+    const unsigned long long e2 =
+        block_scan((static_cast<unsigned long long>((nt + 3u) & ~3u) << 32) | ((nl + 3u) & ~3u), wsum, t2);
+    if (m < a.total_meshlets) {
+        d.v_pref = static_cast<uint32_t>(e1);
+        d.t_pref = static_cast<uint32_t>(e1 >> 32);
+        d.wp_pref = static_cast<uint32_t>(e2);
+        d.tp_pref = static_cast<uint32_t>(e2 >> 32);
+        uint4* dst = reinterpret_cast<uint4*>(a.descs + m);
+        const uint4* src = reinterpret_cast<const uint4*>(&d);
+        dst[0] = src[0];
+        dst[1] = src[1];
+        dst[2] = src[2];
+        dst[3] = src[3];
+    }
+    if (tid == 0)
+        a.blk_sums[blockIdx.x] = make_uint4(static_cast<uint32_t>(t1), static_cast<uint32_t>(t1 >> 32),
+                                            static_cast<uint32_t>(t2 >> 32), static_cast<uint32_t>(t2));
+    // The last block to finish turns the block sums into block prefixes.
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) is_last = atomicAdd(&a.status->ticket, 1u) == gridDim.x - 1u;
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    BlockPrefix carry = {0ull, 0ull, 0ull, 0ull};
+    for (uint32_t base = 0; base < gridDim.x; base += kScanThreads) {
+        const uint32_t i = base + tid;
+        const uint4 s = i < gridDim.x ? __ldcg(a.blk_sums + i) : make_uint4(0u, 0u, 0u, 0u);
+        // per-chunk sums stay below 2^32 (256 blocks x 65536), so pack pairs
+        unsigned long long ta, tb;
+        const unsigned long long ea = block_scan((static_cast<unsigned long long>(s.y) << 32) | s.x, wsum, ta);
+        const unsigned long long eb = block_scan((static_cast<unsigned long long>(s.z) << 32) | s.w, wsum, tb);
+        if (i < gridDim.x) {
+            BlockPrefix p;
+            p.v = carry.v + (ea & 0xFFFFFFFFull);
+            p.t = carry.t + (ea >> 32);
+            p.tp = carry.tp + (eb >> 32);
+            p.wp = carry.wp + (eb & 0xFFFFFFFFull);
+            a.blk_prefix[i] = p;
+        }
+        carry.v += ta & 0xFFFFFFFFull;
+        carry.t += ta >> 32;
+        carry.tp += tb >> 32;
+        carry.wp += tb & 0xFFFFFFFFull;
+    }
 }
 
 // ---------------------------------------------------------------------------
-// Integer code storage: 8 bytes per vertex (16-bit codes) or 16 (wider).
+// Move-to-tail FIFO of 16 local ids in registers.  Byte i of (f0..f3) is
+// deque position i with the newest entry at byte 15; m0..m3 hold 0x80 at
+// the valid bytes [16 - len, 16).  Deque index fi (0 = oldest) is byte
+// 16 - len + fi.
 // ---------------------------------------------------------------------------
+struct Fifo {
+    uint32_t f0 = 0, f1 = 0, f2 = 0, f3 = 0;
+    uint32_t m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+    uint32_t len = 0;
+
+    __device__ __forceinline__ uint32_t at(uint32_t p) const {
+        const uint32_t w = (p & 8u) ? ((p & 4u) ? f3 : f2) : ((p & 4u) ? f1 : f0);
+        return __byte_perm(w, 0u, 0x4440u | (p & 3u));
+    }
+    // exact zero-byte flags of f ^ v at the valid bytes
+    __device__ __forceinline__ static uint32_t match(uint32_t f, uint32_t vv, uint32_t m) {
+        const uint32_t x = f ^ vv;
+        const uint32_t b = (x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu;
+        return ~(b | x) & m;
+    }
+    // byte position of v among the valid entries, or 16
+    __device__ __forceinline__ uint32_t find(uint32_t v) const {
+        const uint32_t vv = __byte_perm(v, 0u, 0u);
+        const uint32_t t0 = match(f0, vv, m0), t1 = match(f1, vv, m1);
+        const uint32_t t2 = match(f2, vv, m2), t3 = match(f3, vv, m3);
+        const uint32_t u = (t0 >> 7) | (t1 >> 6) | (t2 >> 5) | (t3 >> 4);  // bit 8j+i: word i, byte j
+        const uint32_t b = __ffs(u) - 1u;
+        return u ? 4u * (b & 7u) + (b >> 3) : 16u;
+    }
+    // remove the byte at p, shift the newer bytes down, append v as newest
+    __device__ __forceinline__ void remove_append(uint32_t p, uint32_t v) {
+        const uint32_t w = p >> 2;
+        const uint32_t k4 = (p & 3u) * 4u;
+        const uint32_t tsel = 0x4321u - (0x1111u & ((1u << k4) - 1u));
+        const uint32_t s0 = w > 0u ? 0x3210u : tsel;
+        const uint32_t s1 = w > 1u ? 0x3210u : (w == 1u ? tsel : 0x4321u);
+        const uint32_t s2 = w > 2u ? 0x3210u : (w == 2u ? tsel : 0x4321u);
+        const uint32_t s3 = w == 3u ? tsel : 0x4321u;
+        const uint32_t g0 = __byte_perm(f0, f1, s0), g1 = __byte_perm(f1, f2, s1);
+        const uint32_t g2 = __byte_perm(f2, f3, s2), g3 = __byte_perm(f3, v, s3);
+        const uint32_t n0 = __byte_perm(m0, m1, s0), n1 = __byte_perm(m1, m2, s1);
+        const uint32_t n2 = __byte_perm(m2, m3, s2), n3 = __byte_perm(m3, 0x80u, s3);
+        f0 = g0; f1 = g1; f2 = g2; f3 = g3;
+        m0 = n0; m1 = n1; m2 = n2; m3 = n3;
+    }
+};
+
+// 4-entry register buffer flushed to 16-byte aligned scratch.
+struct Quad {
+    uint32_t q0 = 0, q1 = 0, q2 = 0, q3 = 0;
+    __device__ __forceinline__ void put(uint32_t slot, uint32_t v) {
+        q0 = slot == 0u ? v : q0;
+        q1 = slot == 1u ? v : q1;
+        q2 = slot == 2u ? v : q2;
+        q3 = slot == 3u ? v : q3;
+    }
+};
+
+__device__ __forceinline__ void quad_tail(const Quad& q, uint32_t cnt, uint32_t* base) {
+    // the (cnt & 3) entries after the last full quad
+    const uint32_t r = cnt & 3u;
+    uint32_t* p = base + (cnt - r);
+    if (r > 0u) p[0] = q.q0;
+    if (r > 1u) p[1] = q.q1;
+    if (r > 2u) p[2] = q.q2;
+}
+
+// ---------------------------------------------------------------------------
+// 2. connectivity kernel
+// ---------------------------------------------------------------------------
+__host__ __device__ constexpr uint32_t align16(uint32_t x) { return (x + 15u) & ~15u; }
+
+__host__ __device__ inline uint32_t conn_warp_bytes(uint32_t stage_bytes) {
+    return align16(stage_bytes + 32u) + 8u * 32u * 4u + 16u;
+}
+
+__host__ __device__ inline uint32_t vert_stage_bytes(uint32_t stage_bytes) { return stage_bytes / 2u; }
+
+__host__ __device__ inline uint32_t vert_warp_bytes(uint32_t stage_bytes, uint32_t code_bytes) {
+    return align16(vert_stage_bytes(stage_bytes) + 32u) + align16(code_bytes) + 3u * 8u * 4u + 16u + 16u;
+}
+
+struct GroupLane {
+    uint32_t m;
+    bool valid;
+    MeshletDesc d;
+    uint32_t mi;
+    const MeshParams* P;
+    unsigned long long v_base, t_base, tp_base, wp_base;
+    unsigned long long blob_off;
+};
+
+__device__ __forceinline__ void load_group_lane(const DecodeArgs& a, uint32_t g, int lane, GroupLane& L) {
+    L.m = g * 32u + lane;
+    L.valid = L.m < a.total_meshlets;
+    if (L.valid) {
+        const uint4* src = reinterpret_cast<const uint4*>(a.descs + L.m);
+        uint4* dst = reinterpret_cast<uint4*>(&L.d);
+        dst[0] = __ldcg(src);
+        dst[1] = __ldcg(src + 1);
+        dst[2] = __ldcg(src + 2);
+        dst[3] = __ldcg(src + 3);
+        const BlockPrefix& bp = a.blk_prefix[L.m / kScanThreads];
+        L.v_base = bp.v + L.d.v_pref;
+        L.t_base = bp.t + L.d.t_pref;
+        L.tp_base = bp.tp + L.d.tp_pref;
+        L.wp_base = bp.wp + L.d.wp_pref;
+    } else {
+        memset(&L.d, 0, sizeof(L.d));
+        L.v_base = L.t_base = L.tp_base = L.wp_base = 0ull;
+    }
+    L.mi = (L.valid && a.meshlet_mesh) ? __ldg(a.meshlet_mesh + L.m) : 0u;
+    L.P = a.meshes + L.mi;
+    L.blob_off = L.valid ? L.P->blob_off : 0ull;
+}
+
+template <bool kShared>
+__device__ void conn_lane(const DecodeArgs& a, const GroupLane& L, bool act, const uint32_t* w, uint32_t rbase,
+                          uint32_t* seen, int lane) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) seen[i * 32 + lane] = 0u;
+    __syncwarp();
+    const uint32_t n_local = L.d.counts0 & 0xFFFFu;
+    const uint32_t n_tris = L.d.counts0 >> 16;
+    const uint32_t ib = max(1u, 32u - __clz(n_local));
+    const uint32_t end = L.d.end_bit;
+    uint32_t* tri_out = a.tri_scratch + L.tp_base;
+    uint32_t* walk_out = a.walk_scratch + L.wp_base;
+    uint32_t cpos = L.d.start_bit + 48u;
+    uint32_t strips_left = L.d.n_strips;
+    uint32_t tok_left = 0u, tok_idx = 0u, tris = 0u;
+    uint32_t p0 = 0u, p1 = 0u, p2 = 0u;
+    uint32_t tcnt = 0u, wcnt = 0u, kind0 = 0u;
+    Fifo fifo;
+    Quad tq, wq;
+    bool bad = false;
+    bool running = act && strips_left > 0u;
+    // One token per iteration, every lane on the same straight-line path:
+    // the strip header, edge code, vertex kind and walk bookkeeping are all
+    // selects and predicated stores, so lanes never split on them.
+    while (__any_sync(kFull, running)) {
+        if (running) {
+            // a 32-bit window holds a strip header (16 bits) plus the next
+            // token (at most 1 + 9 bits), or an edge code plus a token
+            const uint32_t x0 = peek32<kShared>(w, cpos + rbase);
+            const bool hdr = tok_left == 0u;  // strip header (paradelta_v5_dup.py:519)
+            const uint32_t len = x0 >> 16;
+            const uint32_t sbody = len > 1u ? len - 1u : 0u;
+            tok_left = hdr ? 3u + sbody : tok_left;
+            tok_idx = hdr ? 0u : tok_idx;
+            strips_left -= hdr ? 1u : 0u;
+            tris += hdr ? 1u + sbody : 0u;
+            cpos += hdr ? 16u : 0u;
+            uint32_t x = hdr ? (x0 << 16) : x0;
+            const bool body = tok_idx >= 3u;
+            const uint32_t ec = x >> 31;  // edge code of a strip-body token (:528)
+            x = body ? (x << 1) : x;
+            cpos += body ? 1u : 0u;
+            const bool raw = (x >> 31) != 0u;
+            const uint32_t rid = (x << 1) >> (32u - ib);
+            const uint32_t fi = (x << 1) >> 27;
+            cpos += raw ? 1u + ib : 6u;
+            // decode_dup raises IndexError on both (FIFO index, local id)
+            const bool invalid = (raw ? rid >= n_local : fi >= fifo.len) || tris > n_tris;
+            const uint32_t v = raw ? (rid & 0xFFu) : fifo.at((16u - fifo.len + fi) & 15u);
+            const uint32_t at = fifo.find(v);
+            const uint32_t rm = at < 16u ? at : (fifo.len >= 15u ? 0u : 15u - fifo.len);
+            fifo.remove_append(rm, v);
+            fifo.len += (at == 16u && fifo.len < 16u) ? 1u : 0u;
+            // edge code 0 -> (p1, p2 | p0), 1 -> (p0, p2 | p1)  (:530-535)
+            const uint32_t cref = ec ? p1 : p0;
+            const uint32_t q0 = body ? (ec ? p0 : p1) : (tok_idx == 0u ? v : p0);
+            const uint32_t q1 = body ? p2 : (tok_idx == 1u ? v : p1);
+            const uint32_t q2 = (body || tok_idx == 2u) ? v : p2;
+            p0 = q0;
+            p1 = q1;
+            p2 = q2;
+            const bool emit = (body || tok_idx == 2u) && !invalid;
+            const uint32_t ts = tcnt & 3u;
+            if (emit) tq.put(ts, q0 | (q1 << 8) | (q2 << 16));
+            if (emit && ts == 3u) *reinterpret_cast<uint4*>(tri_out + tcnt - 3u) = make_uint4(tq.q0, tq.q1, tq.q2, tq.q3);
+            tcnt += emit ? 1u : 0u;
+            // first occurrence -> next walk entry (:523-541).  Roots are 'none'
+            // (stored as v,v,v,v); strip bodies 'para' with (a, b, c) = (p0, p1, cref).
+            uint32_t* sp = seen + (v >> 5) * 32u + lane;
+            const uint32_t sw = *sp;
+            const uint32_t bit = 1u << (v & 31u);
+            const bool isnew = !(sw & bit) && !invalid;
+            if (isnew) *sp = sw | bit;
+            const uint32_t e = body ? (v | (q0 << 8) | (q1 << 16) | (cref << 24)) : v * 0x01010101u;
+            const uint32_t ws = wcnt & 3u;
+            if (isnew) wq.put(ws, e);
+            if (isnew && ws == 3u) *reinterpret_cast<uint4*>(walk_out + wcnt - 3u) = make_uint4(wq.q0, wq.q1, wq.q2, wq.q3);
+            wcnt += isnew ? 1u : 0u;
+            kind0 += (isnew && !body) ? 1u : 0u;
+            tok_idx++;
+            tok_left--;
+            bad = bad || invalid || cpos > end;
+            running = !bad && !(tok_left == 0u && strips_left == 0u);
+        }
+    }
+    if (act) {
+        quad_tail(tq, tcnt, tri_out);
+        quad_tail(wq, wcnt, walk_out);
+        if (bad || tris != n_tris) {
+            report(a.status, kErrCorrupt, L.m);
+        } else {
+            a.descs[L.m].anchor_bit = cpos;
+            a.descs[L.m].walk = kind0 | (wcnt << 16);
+        }
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(W * 32) conn_kernel(DecodeArgs a, uint32_t stage_bytes, int persistent) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    if (*reinterpret_cast<volatile unsigned long long*>(&a.status->err) != 0ull) return;
+    uint8_t* base = smem + warp * conn_warp_bytes(stage_bytes);
+    uint32_t* stage = reinterpret_cast<uint32_t*>(base);
+    uint32_t* seen = reinterpret_cast<uint32_t*>(base + align16(stage_bytes + 32u));
+    uint64_t* bar = reinterpret_cast<uint64_t*>(seen + 8 * 32);
+    if (lane == 0) mbar_init(bar);
+    __syncwarp();
+    uint32_t phase = 0u;
+    const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
+    uint32_t g = blockIdx.x * W + warp;
+    if (persistent) {
+        uint32_t t = 0u;
+        if (lane == 0) t = atomicAdd(&a.status->work_conn, 1u);
+        g = __shfl_sync(kFull, t, 0);
+    }
+    while (g < n_groups) {
+        GroupLane L;
+        load_group_lane(a, g, lane, L);
+        bool ok = L.valid;
+        if (ok) {
+            const unsigned long long tpc = L.tp_base + (((L.d.counts0 >> 16) + 3u) & ~3u);
+            const unsigned long long wpc = L.wp_base + (((L.d.counts0 & 0xFFFFu) + 3u) & ~3u);
+            if (tpc > a.tri_cap || wpc > a.walk_cap) {  // header totals disagree with the meshlets
+                report(a.status, kErrCorrupt, L.m);
+                ok = false;
+            }
+        }
+        const unsigned long long start_b = L.blob_off + (L.d.start_bit >> 3);
+        const unsigned long long end16 = (L.blob_off + ((L.d.end_bit + 7u) >> 3) + 15ull) & ~15ull;
+        uint32_t todo = __ballot_sync(kFull, ok);
+        while (todo) {
+            const int first = __ffs(todo) - 1;
+            const bool in = (todo >> lane) & 1u;
+            const unsigned long long s0 = shfl64(start_b, first) & ~15ull;
+            const bool fit = in && (end16 - s0) <= stage_bytes;
+            uint32_t rmask = __ballot_sync(kFull, fit);
+            const bool staged = rmask != 0u;
+            if (!staged) rmask = 1u << first;  // larger than the stage: read from global memory
+            todo &= ~rmask;
+            const bool act = (rmask >> lane) & 1u;
+            if (staged) {
+                const int last = 31 - __clz(rmask);
+                const uint32_t bytes = static_cast<uint32_t>(shfl64(end16, last) - s0);
+                __syncwarp();
+                if (lane == 0) {
+                    mbar_expect(bar, bytes);
+                    bulk_copy(stage, a.arena + s0, bytes, bar);
+                }
+                if (!mbar_wait(bar, phase)) {
+                    if (lane == 0) report(a.status, kErrTimeout, L.m);
+                    mbar_wait(bar, phase);
+                    return;
+                }
+                phase ^= 1u;
+                conn_lane<true>(a, L, act, stage, static_cast<uint32_t>(L.blob_off * 8ull - s0 * 8ull), seen, lane);
+            } else {
+                conn_lane<false>(a, L, act, reinterpret_cast<const uint32_t*>(a.arena + L.blob_off), 0u, seen,
+                                 lane);
+            }
+            __syncwarp();
+        }
+        if (!persistent) break;
+        uint32_t t = 0u;
+        if (lane == 0) t = atomicAdd(&a.status->work_conn, 1u);
+        g = __shfl_sync(kFull, t, 0);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 3. vertex kernel
+// ---------------------------------------------------------------------------
+// Integer codes of one meshlet, 8 bytes per vertex (x | y << 16, z) for codes
+// of up to 16 bits, 16 bytes (x, y, z, 0) above.
 template <bool kWide>
 struct Codes {
     static constexpr uint32_t kBytes = kWide ? 16u : 8u;
@@ -399,61 +642,6 @@ struct Codes {
     }
 };
 
-// ---------------------------------------------------------------------------
-// 16-entry move-to-tail FIFO (_read_vert, encoder/paradelta_codec.py:330-340)
-// in four registers: byte 15 is the newest entry, the valid entries are bytes
-// [16 - len, 16), so the deque index fi (0 = oldest) is byte 16 - len + fi.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ uint32_t low_bytes_mask(uint32_t p, uint32_t word) {
-    // bytes [0, p) of the 16-byte value, restricted to 32-bit word `word`
-    const int sh = min(max(static_cast<int>(p) - static_cast<int>(4u * word), 0), 4) * 8;
-    return static_cast<uint32_t>((1ull << sh) - 1ull);
-}
-
-struct Fifo {
-    uint32_t f0 = 0, f1 = 0, f2 = 0, f3 = 0, len = 0;
-    __device__ __forceinline__ uint32_t at(uint32_t p) const {
-        const uint32_t w = (p & 8u) ? ((p & 4u) ? f3 : f2) : ((p & 4u) ? f1 : f0);
-        return (w >> ((p & 3u) * 8u)) & 0xFFu;
-    }
-    // byte position of v among the valid entries, or 16
-    __device__ __forceinline__ uint32_t find(uint32_t v) const {
-        const uint32_t vv = v * 0x01010101u;
-        const uint32_t lo = 16u - len;
-        const uint32_t e0 = __vcmpeq4(f0, vv) & ~low_bytes_mask(lo, 0);
-        const uint32_t e1 = __vcmpeq4(f1, vv) & ~low_bytes_mask(lo, 1);
-        const uint32_t e2 = __vcmpeq4(f2, vv) & ~low_bytes_mask(lo, 2);
-        const uint32_t e3 = __vcmpeq4(f3, vv) & ~low_bytes_mask(lo, 3);
-        if (e0) return (__ffs(e0) - 1) >> 3;
-        if (e1) return 4u + ((__ffs(e1) - 1) >> 3);
-        if (e2) return 8u + ((__ffs(e2) - 1) >> 3);
-        if (e3) return 12u + ((__ffs(e3) - 1) >> 3);
-        return 16u;
-    }
-    // remove the byte at p, shift the newer bytes down, append v as newest
-    __device__ __forceinline__ void remove_append(uint32_t p, uint32_t v) {
-        const uint32_t s0 = __funnelshift_r(f0, f1, 8);
-        const uint32_t s1 = __funnelshift_r(f1, f2, 8);
-        const uint32_t s2 = __funnelshift_r(f2, f3, 8);
-        const uint32_t s3 = (f3 >> 8) | (v << 24);
-        const uint32_t k0 = low_bytes_mask(p, 0), k1 = low_bytes_mask(p, 1);
-        const uint32_t k2 = low_bytes_mask(p, 2), k3 = low_bytes_mask(p, 3);
-        f0 = (f0 & k0) | (s0 & ~k0);
-        f1 = (f1 & k1) | (s1 & ~k1);
-        f2 = (f2 & k2) | (s2 & ~k2);
-        f3 = (f3 & k3) | (s3 & ~k3);
-    }
-};
-
-struct WarpSmem {
-    uint32_t* stage;
-    uint8_t* codes;
-    uint32_t* ring;
-    uint32_t* seen;
-    float* dqc;  // 3 axes x 8 floats: a_hi a_lo b_hi b_lo err konst zero_bits pad
-    uint64_t* bar;
-};
-
 __device__ __forceinline__ float dequant_value(const float* c, const MeshParams* P, uint32_t axis, uint32_t q) {
     if (__float_as_uint(c[6])) return c[5];
     stride_dequant_axis t;
@@ -467,230 +655,241 @@ __device__ __forceinline__ float dequant_value(const float* c, const MeshParams*
     return stride_dequant_exact(&P->dq[axis], q);
 }
 
-__device__ __forceinline__ void flush_tris(const WarpSmem& S, uint32_t& rcnt, unsigned long long& t_next,
-                                           uint32_t vloc, uint32_t* __restrict__ idx_out, int lane) {
-    __syncwarp();
+template <bool kShared>
+__device__ __noinline__ bool residual_slow(const uint32_t* w, uint32_t rbase, uint32_t* pos, uint32_t tk,
+                                           uint32_t limit, uint32_t* u) {
+    return read_code<kShared>(w, rbase, *pos, tk, limit, *u) == 0;
+}
+
+// Residual of one axis: Rice/EG codeword at `pos` with a straight-line fast
+// path (prefix and value inside one 32-bit window) and the general reader
+// out of line.  Returns false on a malformed codeword.
+template <bool kShared>
+__device__ __forceinline__ bool residual(const uint32_t* w, uint32_t rbase, uint32_t& pos, uint32_t tk,
+                                         uint32_t limit, int32_t& r) {
+    const uint32_t x = peek32<kShared>(w, pos + rbase);
+    const uint32_t z = __clz(x);
+    const uint32_t k = tk & 0x3Fu;
+    const bool eg = (tk & 0x80u) != 0u;
+    const uint32_t nb = (eg ? z : 0u) + k;
+    const uint32_t t = __funnelshift_lc(0u, x, z + 1u);      // bits after the terminator
+    const uint32_t val = __funnelshift_rc(t, 0u, 32u - nb);  // the top nb of them
+    const uint32_t base = eg ? ((1u << (z & 31u)) - 1u) : z;
+    uint32_t u = (base << k) + val;
+    bool ok = true;
+    if (z + 1u + nb > 32u) {  // long prefix or long value: rare
+        uint32_t p = pos;
+        ok = residual_slow<kShared>(w, rbase, &p, tk, limit, &u);
+        pos = p;
+    } else {
+        pos += z + 1u + nb;
+    }
+    r = unzigzag(u);
+    return ok;
+}
+
+// Skip n codewords (substream boundaries are not stored in the stream).
+template <bool kShared>
+__device__ __forceinline__ bool skip_codes(const uint32_t* w, uint32_t rbase, uint32_t& pos, uint32_t tk,
+                                           uint32_t n, uint32_t limit) {
+    const uint32_t k = tk & 0x3Fu;
+    const bool eg = (tk & 0x80u) != 0u;
+    bool ok = true;
+    for (uint32_t i = 0; i < n; i++) {
+        const uint32_t x = peek32<kShared>(w, pos + rbase);
+        const uint32_t z = __clz(x);
+        if (x != 0u) {
+            pos += z + 1u + (eg ? z : 0u) + k;
+        } else {
+            uint32_t p = pos, u;
+            ok = ok && residual_slow<kShared>(w, rbase, &p, tk, limit, &u);
+            pos = p;
+        }
+    }
+    return ok && pos <= limit;
+}
+
+// Decode the integer codes of the active lane's meshlet: anchor, the six
+// (tag, k) headers, then one pass over the walk with a cursor per residual
+// substream (paradelta_v5_dup.py:544-600).  The loop body is straight-line:
+// root and parallelogram vertices differ only in selects.
+template <bool kShared, bool kWide>
+__device__ void vert_lane(const DecodeArgs& a, const GroupLane& L, bool act, const uint32_t* w, uint32_t rbase,
+                          uint8_t* codes, uint32_t code_off, bool& bad) {
+    using C = Codes<kWide>;
+    if (!act) return;
+    const uint32_t n_local = L.d.counts0 & 0xFFFFu;
+    const uint32_t n_kind0 = L.d.walk & 0xFFFFu;
+    const uint32_t n_walk = L.d.walk >> 16;
+    const uint32_t n_delta = n_kind0 ? n_kind0 - 1u : 0u;
+    const uint32_t n_para = n_walk - n_kind0;
+    const uint32_t end = L.d.end_bit;
+    uint8_t* my = codes + code_off;
+    {  // vertices the walk never reaches keep code 0
+        uint4* z = reinterpret_cast<uint4*>(my);
+        const uint32_t nz = (n_local * C::kBytes + 15u) >> 4;
+        for (uint32_t i = 0; i < nz; i++) z[i] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    const MeshParams* P = L.P;
+    uint32_t pos = L.d.anchor_bit;
+    const uint32_t gb0 = P->g_bits[0], gb1 = P->g_bits[1], gb2 = P->g_bits[2];
+    const int32_t an0 = gb0 ? static_cast<int32_t>(peek32<kShared>(w, pos + rbase) >> (32u - gb0)) : 0;
+    pos += gb0;
+    const int32_t an1 = gb1 ? static_cast<int32_t>(peek32<kShared>(w, pos + rbase) >> (32u - gb1)) : 0;
+    pos += gb1;
+    const int32_t an2 = gb2 ? static_cast<int32_t>(peek32<kShared>(w, pos + rbase) >> (32u - gb2)) : 0;
+    pos += gb2;
+    uint32_t tk[6];
+#pragma unroll
+    for (int i = 0; i < 6; i++) {
+        const uint32_t t = peek32<kShared>(w, pos + rbase) >> 16;
+        pos += 16u;
+        const uint32_t k = t & 0xFFu;
+        if (k > static_cast<uint32_t>(kMaxResidK)) bad = true;
+        tk[i] = ((t >> 8) == 1u ? 0u : 0x80u) | (k & 0x3Fu);
+    }
+    if (bad) return;
+    // substream starts: dx dy dz px py pz follow each other
+    uint32_t cdx = pos, cdy, cdz, cpx, cpy, cpz;
+    bool ok = skip_codes<kShared>(w, rbase, pos, tk[0], n_delta, end);
+    cdy = pos;
+    ok = skip_codes<kShared>(w, rbase, pos, tk[1], n_delta, end) && ok;
+    cdz = pos;
+    ok = skip_codes<kShared>(w, rbase, pos, tk[2], n_delta, end) && ok;
+    cpx = pos;
+    ok = skip_codes<kShared>(w, rbase, pos, tk[3], n_para, end) && ok;
+    cpy = pos;
+    ok = skip_codes<kShared>(w, rbase, pos, tk[4], n_para, end) && ok;
+    cpz = pos;
+    if (!ok) {
+        bad = true;
+        return;
+    }
+    const int32_t nx0 = P->pred_n[0], nx1 = P->pred_n[1], nx2 = P->pred_n[2];
+    const int32_t ny0 = P->pred_n[3], ny1 = P->pred_n[4], ny2 = P->pred_n[5];
+    const int32_t nz0 = P->pred_n[6], nz1 = P->pred_n[7], nz2 = P->pred_n[8];
+    const int32_t kx = P->pred_k[0], ky = P->pred_k[1], kz = P->pred_k[2];
+    const int32_t hx = P->pred_half[0], hy = P->pred_half[1], hz = P->pred_half[2];
+    const uint32_t mx = P->code_max[0], mmy = P->code_max[1], mz = P->code_max[2];
+    const uint32_t tdx = tk[0], tdy = tk[1], tdz = tk[2], tpx = tk[3], tpy = tk[4], tpz = tk[5];
+    const uint32_t* walk = a.walk_scratch + L.wp_base;
+    uint4 qn = __ldcg(reinterpret_cast<const uint4*>(walk));
+    uint4 q = qn;
+    int32_t px = 0, py = 0, pz = 0;
+    bool first = true;
+    bool fail = false;
+    for (uint32_t i = 0; i < n_walk; i++) {
+        const uint32_t s = i & 3u;
+        if (s == 0u) {
+            q = qn;
+            if (i + 4u < n_walk) qn = __ldcg(reinterpret_cast<const uint4*>(walk + i + 4u));
+        }
+        const uint32_t e = s == 0u ? q.x : (s == 1u ? q.y : (s == 2u ? q.z : q.w));
+        const uint32_t v = e & 0xFFu;
+        const uint32_t ra = (e >> 8) & 0xFFu, rb = (e >> 16) & 0xFFu, rc = e >> 24;
+        const bool para = ra != v;
+        const bool anchor = first && !para;  // the first walk vertex is the anchor
+        first = first && para;
+        // IRLP over (a, b, c) (:91-104); for root entries the references
+        // are the vertex itself and the result is discarded
+        int32_t ax, ay, az, bx, by, bz, ccx, ccy, ccz;
+        C::load(my, ra, ax, ay, az);
+        C::load(my, rb, bx, by, bz);
+        C::load(my, rc, ccx, ccy, ccz);
+        const int32_t qx = para ? (nx0 * ax + nx1 * bx + nx2 * ccx + hx) >> kx : px;
+        const int32_t qy = para ? (ny0 * ay + ny1 * by + ny2 * ccy + hy) >> ky : py;
+        const int32_t qz = para ? (nz0 * az + nz1 * bz + nz2 * ccz + hz) >> kz : pz;
+        uint32_t p0 = para ? cpx : cdx, p1 = para ? cpy : cdy, p2 = para ? cpz : cdz;
+        int32_t rx, ry, rz;
+        bool okr = residual<kShared>(w, rbase, p0, para ? tpx : tdx, end, rx);
+        okr = residual<kShared>(w, rbase, p1, para ? tpy : tdy, end, ry) && okr;
+        okr = residual<kShared>(w, rbase, p2, para ? tpz : tdz, end, rz) && okr;
+        cpx = para ? p0 : cpx;
+        cpy = para ? p1 : cpy;
+        cpz = para ? p2 : cpz;
+        const bool dcommit = !para && !anchor;
+        cdx = dcommit ? p0 : cdx;
+        cdy = dcommit ? p1 : cdy;
+        cdz = dcommit ? p2 : cdz;
+        const int32_t cx = anchor ? an0 : qx + rx;
+        const int32_t cy = anchor ? an1 : qy + ry;
+        const int32_t cz = anchor ? an2 : qz + rz;
+        // codes of a valid stream lie in [0, 2^g_bits)
+        fail = fail || !(okr || anchor) || static_cast<uint32_t>(cx) > mx || static_cast<uint32_t>(cy) > mmy ||
+               static_cast<uint32_t>(cz) > mz;
+        C::store(my, v, cx, cy, cz);
+        px = cx;
+        py = cy;
+        pz = cz;
+    }
+    bad = bad || fail;
+    // the last substream must end where the next meshlet starts (:507)
+    if (!bad) {
+        const bool last_of_mesh = L.m - P->meshlet_begin + 1u == P->n_meshlets;
+        if (last_of_mesh ? cpz > end : cpz != end) bad = true;
+    }
+}
+
+template <bool kWide>
+__device__ void emit_round(const DecodeArgs& a, const GroupLane& L, uint32_t rmask, const uint8_t* codes,
+                           uint32_t code_off, float* dqc, int lane) {
+    using C = Codes<kWide>;
+    const uint32_t vloc = static_cast<uint32_t>(L.v_base - (L.valid ? L.P->v_offset : 0ull));
+    uint32_t cached = 0xFFFFFFFFu;
     for (int j = 0; j < 32; j++) {
-        const uint32_t c = __shfl_sync(kFull, rcnt, j);
-        if (c == 0u) continue;
-        const unsigned long long tb = shfl64(t_next, j);
-        const uint32_t vb = __shfl_sync(kFull, vloc, j);
-        const uint32_t* rj = S.ring + j * kRingStride;
+        if (!((rmask >> j) & 1u)) continue;
+        const uint32_t c0 = __shfl_sync(kFull, L.d.counts0, j);
+        const uint32_t nv = c0 & 0xFFFFu, nt = c0 >> 16;
+        const unsigned long long vb = shfl64(L.v_base, j);
+        const unsigned long long tb = shfl64(L.t_base, j);
+        const unsigned long long tpb = shfl64(L.tp_base, j);
+        const uint32_t vl = __shfl_sync(kFull, vloc, j);
+        const uint32_t off = __shfl_sync(kFull, code_off, j);
+        const uint32_t mj = __shfl_sync(kFull, L.mi, j);
+        const MeshParams* Pj = a.meshes + mj;
+        // triangles: packed local ids -> global ids
+        const uint32_t* tsrc = a.tri_scratch + tpb;
         warp_store_words(
-            idx_out + 3ull * tb, 3u * c,
+            a.idx + 3ull * tb, 3u * nt,
             [&](uint32_t i) {
                 const uint32_t t = i / 3u;
                 const uint32_t k = i - 3u * t;
-                return vb + ((rj[t] >> (8u * k)) & 0xFFu);
+                return vl + ((__ldcg(tsrc + t) >> (8u * k)) & 0xFFu);
             },
             lane);
-    }
-    t_next += rcnt;
-    rcnt = 0u;
-    __syncwarp();
-}
-
-template <bool kShared>
-__device__ __forceinline__ int read_axis(const uint32_t* w, uint32_t rbase, bool para, uint32_t& cd, uint32_t& cp,
-                                         uint32_t tkd, uint32_t tkp, uint32_t limit, int32_t& r) {
-    uint32_t p = para ? cp : cd;
-    uint32_t u = 0u;
-    const int e = read_code<kShared>(w, rbase, p, para ? tkp : tkd, limit, u);
-    if (para) cp = p; else cd = p;
-    r = unzigzag(u);
-    return e;
-}
-
-// Decode the meshlets of the lanes in `act` (one per lane) from the word
-// array `w` (staged shared memory or the global stream).
-template <bool kShared, bool kWide>
-__device__ void decode_lanes(const DecodeArgs& a, const WarpSmem& S, const MeshletDesc& d, const MeshParams* P,
-                             uint32_t mi, bool act, uint32_t m, uint32_t round_mask, uint32_t round_code_bytes,
-                             uint32_t code_off, const uint32_t* w, uint32_t rbase,
-                             unsigned long long v_base, unsigned long long t_base, int lane) {
-    using C = Codes<kWide>;
-    // clear first-occurrence bits and the integer codes of this round
-#pragma unroll
-    for (int i = 0; i < 8; i++) S.seen[i * 32 + lane] = 0u;
-    for (uint32_t i = lane; i < round_code_bytes / 8u; i += 32u) reinterpret_cast<uint2*>(S.codes)[i] = make_uint2(0u, 0u);
-    __syncwarp();
-
-    uint8_t* my_codes = S.codes + code_off;
-    const uint32_t n_local = d.counts0 & 0xFFFFu;
-    const uint32_t n_strips = d.counts1 & 0xFFFFu;
-    const uint32_t ib = max(1u, 32u - __clz(n_local));
-    const uint32_t limit = d.end_bit;
-    int32_t pn0 = 0, pn1 = 0, pn2 = 0, pn3 = 0, pn4 = 0, pn5 = 0, pn6 = 0, pn7 = 0, pn8 = 0;
-    int32_t pk0 = 0, pk1 = 0, pk2 = 0, ph0 = 0, ph1 = 0, ph2 = 0;
-    uint32_t cm0 = 0, cm1 = 0, cm2 = 0, gb0 = 0, gb1 = 0, gb2 = 0;
-    unsigned long long v_off = 0ull;
-    if (act) {
-        pn0 = P->pred_n[0]; pn1 = P->pred_n[1]; pn2 = P->pred_n[2];
-        pn3 = P->pred_n[3]; pn4 = P->pred_n[4]; pn5 = P->pred_n[5];
-        pn6 = P->pred_n[6]; pn7 = P->pred_n[7]; pn8 = P->pred_n[8];
-        pk0 = P->pred_k[0]; pk1 = P->pred_k[1]; pk2 = P->pred_k[2];
-        ph0 = P->pred_half[0]; ph1 = P->pred_half[1]; ph2 = P->pred_half[2];
-        cm0 = P->code_max[0]; cm1 = P->code_max[1]; cm2 = P->code_max[2];
-        gb0 = P->g_bits[0]; gb1 = P->g_bits[1]; gb2 = P->g_bits[2];
-        v_off = P->v_offset;
-    }
-    const uint32_t tkd = d.tk_delta, tkp = d.tk_para;
-    uint32_t c0 = d.res_bit[0], c1 = d.res_bit[1], c2 = d.res_bit[2];
-    uint32_t c3 = d.res_bit[3], c4 = d.res_bit[4], c5 = d.res_bit[5];
-    // anchor: raw codes of g_bits each (paradelta_v5_dup.py:545-546)
-    int32_t ax = 0, ay = 0, az = 0;
-    if (act) {
-        uint32_t p = d.anchor_bit;
-        if (gb0) { ax = static_cast<int32_t>(peek32<kShared>(w, p + rbase) >> (32u - gb0)); p += gb0; }
-        if (gb1) { ay = static_cast<int32_t>(peek32<kShared>(w, p + rbase) >> (32u - gb1)); p += gb1; }
-        if (gb2) { az = static_cast<int32_t>(peek32<kShared>(w, p + rbase) >> (32u - gb2)); }
-    }
-
-    uint32_t cpos = d.conn_bit;
-    uint32_t strips_left = n_strips;
-    uint32_t tok_left = 0u, tok_idx = 0u;
-    uint32_t p0 = 0u, p1 = 0u, p2 = 0u;
-    Fifo fifo;
-    bool have_anchor = false;
-    int32_t prx = 0, pry = 0, prz = 0;
-    uint32_t rcnt = 0u;
-    unsigned long long t_next = t_base;
-    const uint32_t vloc = static_cast<uint32_t>(v_base - v_off);
-    bool running = act && n_strips > 0u;
-    bool bad = false;
-    uint32_t* my_ring = S.ring + lane * kRingStride;
-
-    while (__any_sync(kFull, running)) {
-        if (running) {
-            if (tok_left == 0u) {  // strip header (paradelta_v5_dup.py:519)
-                const uint32_t len = peek32<kShared>(w, cpos + rbase) >> 16;
-                cpos += 16u;
-                tok_left = 3u + (len > 1u ? len - 1u : 0u);
-                tok_idx = 0u;
-                strips_left--;
-            }
-            uint32_t x = peek32<kShared>(w, cpos + rbase);
-            const bool body = tok_idx >= 3u;
-            const uint32_t ec = body ? (x >> 31) : 0u;
-            if (body) {
-                x <<= 1;
-                cpos += 1u;
-            }
-            const bool raw = (x >> 31) != 0u;
-            const uint32_t rid = min((x << 1) >> (32u - ib), 255u);
-            const uint32_t fi = (x << 1) >> 27;
-            cpos += raw ? 1u + ib : 6u;
-            const uint32_t v = raw ? rid : fifo.at((16u - fifo.len + fi) & 15u);
-            const uint32_t at = fifo.find(v);
-            const uint32_t rm = at < 16u ? at : (fifo.len == 16u ? 0u : 15u - fifo.len);
-            fifo.remove_append(rm, v);
-            fifo.len = min(fifo.len + (at == 16u ? 1u : 0u), 16u);
-            uint32_t c_ref = 0u;
-            if (body) {  // edge code: 0 -> (p1, p2, p0), 1 -> (p0, p2, p1)  (:530-535)
-                const uint32_t na = ec ? p0 : p1;
-                c_ref = ec ? p1 : p0;
-                p0 = na;
-                p1 = p2;
-                p2 = v;
-            } else {
-                p0 = tok_idx == 0u ? v : p0;
-                p1 = tok_idx == 1u ? v : p1;
-                p2 = tok_idx == 2u ? v : p2;
-            }
-            if (body || tok_idx == 2u) {
-                my_ring[rcnt] = p0 | (p1 << 8) | (p2 << 16);
-                rcnt++;
-            }
-            tok_idx++;
-            tok_left--;
-            if (tok_left == 0u && strips_left == 0u) running = false;
-            // first occurrence -> next vertex of the walk (:523-541, :581-600)
-            uint32_t& sw = S.seen[(v >> 5) * 32u + lane];
-            const uint32_t bit = 1u << (v & 31u);
-            if (!(sw & bit)) {
-                sw |= bit;
-                int32_t cx, cy, cz;
-                if (!body && !have_anchor) {
-                    cx = ax;
-                    cy = ay;
-                    cz = az;
-                    have_anchor = true;
-                } else {
-                    int32_t qx = prx, qy = pry, qz = prz;
-                    if (body) {  // IRLP (:91-104) over (a, b, c) = (p0, p1, c_ref)
-                        int32_t axx, ayy, azz, bx, by, bz, cxx, cyy, czz;
-                        C::load(my_codes, p0, axx, ayy, azz);
-                        C::load(my_codes, p1, bx, by, bz);
-                        C::load(my_codes, c_ref, cxx, cyy, czz);
-                        qx = (pn0 * axx + pn1 * bx + pn2 * cxx + ph0) >> pk0;
-                        qy = (pn3 * ayy + pn4 * by + pn5 * cyy + ph1) >> pk1;
-                        qz = (pn6 * azz + pn7 * bz + pn8 * czz + ph2) >> pk2;
-                    }
-                    int32_t rx, ry, rz;
-                    int e = read_axis<kShared>(w, rbase, body, c0, c3, tkd & 0xFFu, tkp & 0xFFu, limit, rx);
-                    e |= read_axis<kShared>(w, rbase, body, c1, c4, (tkd >> 8) & 0xFFu, (tkp >> 8) & 0xFFu, limit, ry);
-                    e |= read_axis<kShared>(w, rbase, body, c2, c5, (tkd >> 16) & 0xFFu, (tkp >> 16) & 0xFFu, limit, rz);
-                    const long long lx = static_cast<long long>(qx) + rx;
-                    const long long ly = static_cast<long long>(qy) + ry;
-                    const long long lz = static_cast<long long>(qz) + rz;
-                    if (e || lx < 0 || ly < 0 || lz < 0 || lx > cm0 || ly > cm1 || lz > cm2) bad = true;
-                    cx = static_cast<int32_t>(lx < 0 ? 0 : (lx > cm0 ? cm0 : lx));
-                    cy = static_cast<int32_t>(ly < 0 ? 0 : (ly > cm1 ? cm1 : ly));
-                    cz = static_cast<int32_t>(lz < 0 ? 0 : (lz > cm2 ? cm2 : lz));
-                }
-                C::store(my_codes, v, cx, cy, cz);
-                prx = cx;
-                pry = cy;
-                prz = cz;
-            }
-        }
-        if (__any_sync(kFull, rcnt == static_cast<uint32_t>(kRing))) flush_tris(S, rcnt, t_next, vloc, a.idx, lane);
-    }
-    flush_tris(S, rcnt, t_next, vloc, a.idx, lane);
-    if (bad) report(a.status, kErrCorrupt, m);
-
-    // positions (and optionally codes), one meshlet at a time, whole warp
-    uint32_t cached = 0xFFFFFFFFu;
-    for (int j = 0; j < 32; j++) {
-        if (!((round_mask >> j) & 1u)) continue;
-        const uint32_t n = __shfl_sync(kFull, n_local, j);
-        const unsigned long long vb = shfl64(v_base, j);
-        const uint32_t off = __shfl_sync(kFull, code_off, j);
-        const uint32_t mj = __shfl_sync(kFull, mi, j);
-        const MeshParams* Pj = a.meshes + mj;
         if (mj != cached) {
             __syncwarp();
             if (lane < 24) {
-                const uint32_t ax_ = lane >> 3, f = lane & 7u;
-                const stride_dequant_axis& q = Pj->dq[ax_];
+                const uint32_t ax = lane >> 3, f = lane & 7u;
+                const stride_dequant_axis& dq = Pj->dq[ax];
                 float val;
                 switch (f) {
-                    case 0: val = q.a_hi; break;
-                    case 1: val = q.a_lo; break;
-                    case 2: val = q.b_hi; break;
-                    case 3: val = q.b_lo; break;
-                    case 4: val = q.err; break;
-                    case 5: val = q.konst; break;
-                    case 6: val = __uint_as_float(static_cast<uint32_t>(q.zero_bits)); break;
+                    case 0: val = dq.a_hi; break;
+                    case 1: val = dq.a_lo; break;
+                    case 2: val = dq.b_hi; break;
+                    case 3: val = dq.b_lo; break;
+                    case 4: val = dq.err; break;
+                    case 5: val = dq.konst; break;
+                    case 6: val = __uint_as_float(static_cast<uint32_t>(dq.zero_bits)); break;
                     default: val = 0.f; break;
                 }
-                S.dqc[lane] = val;
+                dqc[lane] = val;
             }
             __syncwarp();
             cached = mj;
         }
-        const uint8_t* cj = S.codes + off;
+        const uint8_t* cj = codes + off;
         warp_store_words(
-            reinterpret_cast<uint32_t*>(a.pos + 3ull * vb), 3u * n,
+            reinterpret_cast<uint32_t*>(a.pos + 3ull * vb), 3u * nv,
             [&](uint32_t i) {
                 const uint32_t vv = i / 3u;
                 const uint32_t k = i - 3u * vv;
-                return __float_as_uint(dequant_value(S.dqc + 8u * k, Pj, k, C::component(cj, vv, k)));
+                return __float_as_uint(dequant_value(dqc + 8u * k, Pj, k, C::component(cj, vv, k)));
             },
             lane);
         if (a.codes) {
             warp_store_words(
-                reinterpret_cast<uint32_t*>(a.codes + 3ull * vb), 3u * n,
+                reinterpret_cast<uint32_t*>(a.codes + 3ull * vb), 3u * nv,
                 [&](uint32_t i) {
                     const uint32_t vv = i / 3u;
                     return C::component(cj, vv, i - 3u * vv);
@@ -701,171 +900,178 @@ __device__ void decode_lanes(const DecodeArgs& a, const WarpSmem& S, const Meshl
     __syncwarp();
 }
 
-__host__ __device__ constexpr uint32_t align16(uint32_t x) { return (x + 15u) & ~15u; }
-
-__host__ __device__ inline uint32_t warp_smem_bytes(uint32_t stage_bytes, uint32_t code_bytes) {
-    return align16(stage_bytes + 32u) + align16(code_bytes) + align16(kRingStride * 32u * 4u) + 8u * 32u * 4u +
-           3u * 8u * 4u + 16u;
-}
-
-template <bool kWide>
-__device__ bool process_group(const DecodeArgs& a, const WarpSmem& S, uint32_t g, uint32_t stage_bytes,
-                              uint32_t code_bytes, uint32_t& phase, int lane) {
-    using C = Codes<kWide>;
-    const uint32_t m = g * 32u + lane;
-    const bool valid = m < a.total_meshlets;
-    MeshletDesc d;
-    if (valid) {
-        const uint4* src = reinterpret_cast<const uint4*>(a.descs + m);
-        uint4* dst = reinterpret_cast<uint4*>(&d);
-        dst[0] = __ldg(src);
-        dst[1] = __ldg(src + 1);
-        dst[2] = __ldg(src + 2);
-        dst[3] = __ldg(src + 3);
-    } else {
-        memset(&d, 0, sizeof(d));
-    }
-    const uint32_t mi = (valid && a.meshlet_mesh) ? __ldg(a.meshlet_mesh + m) : 0u;
-    const MeshParams* P = a.meshes + mi;
-    const uint32_t n_local = d.counts0 & 0xFFFFu;
-    const uint32_t n_tris = d.counts0 >> 16;
-    unsigned long long v_base = 0ull, t_base = 0ull;
-    bool ok = false;
-    unsigned long long blob_off = 0ull;
-    if (valid) {
-        const ulonglong2 bp = a.blk_prefix[m / kScanThreads];
-        v_base = bp.x + d.v_pref;
-        t_base = bp.y + d.t_pref;
-        const unsigned long long vo = P->v_offset, to = P->t_offset, nv = P->n_v, nt = P->n_t;
-        ok = v_base >= vo && v_base + n_local <= vo + nv && t_base >= to && t_base + n_tris <= to + nt;
-        if (ok && m - P->meshlet_begin + 1u == P->n_meshlets)
-            ok = v_base + n_local == vo + nv && t_base + n_tris == to + nt;
-        if (!ok) report(a.status, kErrCorrupt, m);
-        blob_off = P->blob_off;
-    }
-    const unsigned long long start_b = blob_off + ((d.conn_bit - 48u) >> 3);
-    const unsigned long long end16 = (blob_off + ((d.end_bit + 7u) >> 3) + 15ull) & ~15ull;
-    const uint32_t csz = n_local * C::kBytes;
-    uint32_t todo = __ballot_sync(kFull, ok);
-    while (todo) {
-        const int first = __ffs(todo) - 1;
-        const bool in = (todo >> lane) & 1u;
-        uint32_t cum = in ? csz : 0u;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t t = __shfl_up_sync(kFull, cum, o);
-            if (lane >= o) cum += t;
-        }
-        const unsigned long long s0 = shfl64(start_b, first) & ~15ull;
-        const bool fit = in && cum <= code_bytes && (end16 - s0) <= stage_bytes;
-        uint32_t rmask = __ballot_sync(kFull, fit);
-        const bool staged = rmask != 0u;
-        if (!staged) rmask = 1u << first;  // a meshlet larger than the stage: read it from global memory
-        todo &= ~rmask;
-        const bool act = (rmask >> lane) & 1u;
-        const uint32_t last = 31 - __clz(rmask);
-        const uint32_t round_bytes = __shfl_sync(kFull, cum, last);
-        const uint32_t code_off = act ? cum - csz : 0u;
-        if (staged) {
-            const unsigned long long e_last = shfl64(end16, last);
-            const uint32_t bytes = static_cast<uint32_t>(e_last - s0);
-            __syncwarp();
-            if (lane == 0) bulk_load(S.stage, a.arena + s0, bytes, S.bar);
-            if (!mbar_wait(S.bar, phase)) {
-                if (lane == 0) report(a.status, kErrTimeout, m);
-                mbar_wait(S.bar, phase);  // give the copy in flight one more bounded wait
-                return false;
-            }
-            phase ^= 1u;
-            const uint32_t rbase = static_cast<uint32_t>(blob_off * 8ull - s0 * 8ull);
-            decode_lanes<true, kWide>(a, S, d, P, mi, act, m, rmask, round_bytes, code_off, S.stage, rbase, v_base,
-                                      t_base, lane);
-        } else {
-            const uint32_t* gw = reinterpret_cast<const uint32_t*>(a.arena + blob_off);
-            decode_lanes<false, kWide>(a, S, d, P, mi, act, m, rmask, round_bytes, code_off, gw, 0u, v_base,
-                                       t_base, lane);
-        }
-    }
-    return true;
-}
-
 template <int W, bool kWide>
-__global__ void __launch_bounds__(W * 32) decode_kernel(DecodeArgs a, uint32_t stage_bytes, uint32_t code_bytes,
-                                                        int persistent) {
+__global__ void __launch_bounds__(W * 32) vert_kernel(DecodeArgs a, uint32_t stage_bytes, uint32_t code_bytes,
+                                                      int persistent) {
     extern __shared__ __align__(128) uint8_t smem[];
     const int warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     if (*reinterpret_cast<volatile unsigned long long*>(&a.status->err) != 0ull) return;
-    const uint32_t per_warp = warp_smem_bytes(stage_bytes, code_bytes);
-    uint8_t* base = smem + warp * per_warp;
-    WarpSmem S;
-    S.stage = reinterpret_cast<uint32_t*>(base);
-    S.codes = base + align16(stage_bytes + 32u);
-    S.ring = reinterpret_cast<uint32_t*>(S.codes + align16(code_bytes));
-    S.seen = S.ring + align16(kRingStride * 32u * 4u) / 4u;
-    S.dqc = reinterpret_cast<float*>(S.seen + 8 * 32);
-    S.bar = reinterpret_cast<uint64_t*>(S.dqc + 24);
-    if (lane == 0) mbar_init(S.bar);
+    const uint32_t vstage = vert_stage_bytes(stage_bytes);
+    uint8_t* base = smem + warp * vert_warp_bytes(stage_bytes, code_bytes);
+    uint32_t* stage = reinterpret_cast<uint32_t*>(base);
+    uint8_t* codes = base + align16(vstage + 32u);
+    float* dqc = reinterpret_cast<float*>(codes + align16(code_bytes));
+    uint64_t* bar = reinterpret_cast<uint64_t*>(dqc + 24);
+    if (lane == 0) mbar_init(bar);
     __syncwarp();
     uint32_t phase = 0u;
     const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
-    uint32_t g;
+    uint32_t g = blockIdx.x * W + warp;
     if (persistent) {
         uint32_t t = 0u;
-        if (lane == 0) t = atomicAdd(&a.status->work, 1u);
+        if (lane == 0) t = atomicAdd(&a.status->work_vert, 1u);
         g = __shfl_sync(kFull, t, 0);
-    } else {
-        g = blockIdx.x * W + warp;
     }
     while (g < n_groups) {
-        if (!process_group<kWide>(a, S, g, stage_bytes, code_bytes, phase, lane)) return;
+        GroupLane L;
+        load_group_lane(a, g, lane, L);
+        const uint32_t n_local = L.d.counts0 & 0xFFFFu;
+        const uint32_t n_tris = L.d.counts0 >> 16;
+        bool ok = L.valid;
+        if (ok) {
+            const unsigned long long vo = L.P->v_offset, to = L.P->t_offset, nv = L.P->n_v, nt = L.P->n_t;
+            ok = L.v_base >= vo && L.v_base + n_local <= vo + nv && L.t_base >= to && L.t_base + n_tris <= to + nt;
+            if (ok && L.m - L.P->meshlet_begin + 1u == L.P->n_meshlets)
+                ok = L.v_base + n_local == vo + nv && L.t_base + n_tris == to + nt;
+            if (!ok) report(a.status, kErrCorrupt, L.m);
+        }
+        // this lane's residual bits: anchor .. end, 16-byte aligned
+        const unsigned long long src16 = (L.blob_off + (L.d.anchor_bit >> 3)) & ~15ull;
+        const unsigned long long end16 = (L.blob_off + ((L.d.end_bit + 7u) >> 3) + 15ull) & ~15ull;
+        const uint32_t ssz = ok ? static_cast<uint32_t>(end16 - src16) : 0u;
+        const uint32_t csz = (n_local * Codes<kWide>::kBytes + 15u) & ~15u;
+        uint32_t todo = __ballot_sync(kFull, ok);
+        while (todo) {
+            const int first = __ffs(todo) - 1;
+            const bool in = (todo >> lane) & 1u;
+            uint32_t cc = in ? csz : 0u, cs = in ? ssz : 0u;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t1 = __shfl_up_sync(kFull, cc, o);
+                const uint32_t t2 = __shfl_up_sync(kFull, cs, o);
+                if (lane >= o) {
+                    cc += t1;
+                    cs += t2;
+                }
+            }
+            const bool fit = in && cc <= code_bytes && cs <= vstage;
+            uint32_t rmask = __ballot_sync(kFull, fit);
+            const bool staged = rmask != 0u;
+            if (!staged) {  // one meshlet whose residuals exceed the stage: global reads
+                rmask = 1u << first;
+                cc = in ? csz : 0u;
+            }
+            todo &= ~rmask;
+            const bool act = (rmask >> lane) & 1u;
+            const uint32_t code_off = act ? cc - csz : 0u;
+            bool bad = false;
+            if (staged) {
+                const int last = 31 - __clz(rmask);
+                const uint32_t total = __shfl_sync(kFull, cs, last);
+                const uint32_t dst_off = act ? cs - ssz : 0u;
+                __syncwarp();
+                if (lane == 0) mbar_expect(bar, total);
+                __syncwarp();
+                if (act && ssz) bulk_copy(reinterpret_cast<uint8_t*>(stage) + dst_off, a.arena + src16, ssz, bar);
+                if (!mbar_wait(bar, phase)) {
+                    if (lane == 0) report(a.status, kErrTimeout, L.m);
+                    mbar_wait(bar, phase);
+                    return;
+                }
+                phase ^= 1u;
+                const uint32_t rbase = static_cast<uint32_t>(L.blob_off * 8ull - src16 * 8ull + dst_off * 8ull);
+                vert_lane<true, kWide>(a, L, act, stage, rbase, codes, code_off, bad);
+            } else {
+                vert_lane<false, kWide>(a, L, act, reinterpret_cast<const uint32_t*>(a.arena + L.blob_off), 0u,
+                                        codes, code_off, bad);
+            }
+            if (act && bad) report(a.status, kErrCorrupt, L.m);
+            __syncwarp();
+            emit_round<kWide>(a, L, rmask, codes, code_off, dqc, lane);
+        }
         if (!persistent) break;
         uint32_t t = 0u;
-        if (lane == 0) t = atomicAdd(&a.status->work, 1u);
+        if (lane == 0) t = atomicAdd(&a.status->work_vert, 1u);
         g = __shfl_sync(kFull, t, 0);
     }
 }
 
-template <int W, bool kWide>
-cudaError_t launch_decode_t(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s) {
-    const size_t smem = static_cast<size_t>(W) * warp_smem_bytes(cfg.stage_bytes, cfg.code_bytes);
-    // opt in to large dynamic shared memory once per (device, kernel)
-    static size_t configured[64] = {0};
+// ---------------------------------------------------------------------------
+// launch plumbing
+// ---------------------------------------------------------------------------
+template <class K>
+cudaError_t opt_in_smem(K kernel, size_t smem, size_t* configured) {
     int dev = 0;
     cudaGetDevice(&dev);
     dev = dev < 0 || dev >= 64 ? 0 : dev;
     if (configured[dev] < smem) {
-        cudaError_t e = cudaFuncSetAttribute(decode_kernel<W, kWide>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             static_cast<int>(smem));
+        cudaError_t e =
+            cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
         configured[dev] = smem;
     }
-    const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
+    return cudaSuccess;
+}
+
+template <class K>
+uint32_t grid_for(K kernel, int threads, size_t smem, const LaunchCfg& cfg, uint32_t n_groups, int W) {
     uint32_t grid = (n_groups + W - 1) / W;
     if (cfg.persistent) {
-        const int per_sm = cfg.ctas_per_sm > 0 ? cfg.ctas_per_sm : 4;
+        int per_sm = cfg.ctas_per_sm;
+        if (per_sm <= 0) {
+            per_sm = 1;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+            if (per_sm < 1) per_sm = 1;
+        }
         const uint32_t cap = static_cast<uint32_t>(per_sm * device_sm_count());
         if (grid > cap) grid = cap;
     }
+    return grid;
+}
+
+template <int W>
+cudaError_t launch_conn(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s) {
+    static size_t configured[64] = {0};
+    const size_t smem = static_cast<size_t>(W) * conn_warp_bytes(cfg.stage_bytes);
+    cudaError_t e = opt_in_smem(conn_kernel<W>, smem, configured);
+    if (e != cudaSuccess) return e;
+    const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
+    const uint32_t grid = grid_for(conn_kernel<W>, W * 32, smem, cfg, n_groups, W);
     if (grid == 0) return cudaSuccess;
-    decode_kernel<W, kWide><<<grid, W * 32, smem, s>>>(a, cfg.stage_bytes, cfg.code_bytes, cfg.persistent);
+    conn_kernel<W><<<grid, W * 32, smem, s>>>(a, cfg.stage_bytes, cfg.persistent);
     return cudaGetLastError();
 }
 
-template <bool kWide>
-cudaError_t launch_decode_w(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s) {
-    switch (cfg.warps_per_cta) {
-        case 1: return launch_decode_t<1, kWide>(a, cfg, s);
-        case 2: return launch_decode_t<2, kWide>(a, cfg, s);
-        case 4: return launch_decode_t<4, kWide>(a, cfg, s);
-        default: return cudaErrorInvalidValue;
-    }
+template <int W, bool kWide>
+cudaError_t launch_vert(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s) {
+    static size_t configured[64] = {0};
+    const size_t smem = static_cast<size_t>(W) * vert_warp_bytes(cfg.stage_bytes, cfg.code_bytes);
+    cudaError_t e = opt_in_smem(vert_kernel<W, kWide>, smem, configured);
+    if (e != cudaSuccess) return e;
+    const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
+    const uint32_t grid = grid_for(vert_kernel<W, kWide>, W * 32, smem, cfg, n_groups, W);
+    if (grid == 0) return cudaSuccess;
+    vert_kernel<W, kWide><<<grid, W * 32, smem, s>>>(a, cfg.stage_bytes, cfg.code_bytes, cfg.persistent);
+    return cudaGetLastError();
+}
+
+template <int W>
+cudaError_t launch_pair(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s, void* const* ev) {
+    cudaError_t e = launch_conn<W>(a, cfg, s);
+    if (e != cudaSuccess) return e;
+    if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[2]), s);
+    return a.wide_codes ? launch_vert<W, true>(a, cfg, s) : launch_vert<W, false>(a, cfg, s);
 }
 
 }  // namespace
 
-size_t decode_smem_bytes(const LaunchCfg& cfg, bool /*wide*/) {
-    return static_cast<size_t>(cfg.warps_per_cta) * warp_smem_bytes(cfg.stage_bytes, cfg.code_bytes);
+size_t conn_smem_bytes(const LaunchCfg& cfg) {
+    return static_cast<size_t>(cfg.warps_per_cta) * conn_warp_bytes(cfg.stage_bytes);
+}
+
+size_t vert_smem_bytes(const LaunchCfg& cfg) {
+    return static_cast<size_t>(cfg.warps_per_cta) * vert_warp_bytes(cfg.stage_bytes, cfg.code_bytes);
 }
 
 int device_sm_count() {
@@ -883,8 +1089,8 @@ int device_sm_count() {
 
 int check_config(const LaunchCfg& cfg, bool wide) {
     if (cfg.warps_per_cta != 1 && cfg.warps_per_cta != 2 && cfg.warps_per_cta != 4) return STRIDE_ERR_ARG;
-    if (cfg.code_bytes < kMaxLocal * (wide ? 16u : 8u) || cfg.stage_bytes < 1024u) return STRIDE_ERR_ARG;
-    if (decode_smem_bytes(cfg, wide) > 227u * 1024u) return STRIDE_ERR_ARG;
+    if (cfg.code_bytes < kMaxLocal * (wide ? 16u : 8u) || cfg.stage_bytes < 256u) return STRIDE_ERR_ARG;
+    if (conn_smem_bytes(cfg) > 227u * 1024u || vert_smem_bytes(cfg) > 227u * 1024u) return STRIDE_ERR_ARG;
     return STRIDE_OK;
 }
 
@@ -894,16 +1100,22 @@ int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void
     if (cudaMemsetAsync(a.status, 0, sizeof(Status), s) != cudaSuccess) return STRIDE_ERR_CUDA;
     if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[0]), s);
     if (a.total_meshlets != 0) {
-        const uint32_t nb = parse_blocks(a.total_meshlets);
-        parse_kernel<<<nb, kScanThreads, 0, s>>>(a);
+        scan_kernel<<<scan_blocks(a.total_meshlets), kScanThreads, 0, s>>>(a);
         if (cudaGetLastError() != cudaSuccess) return STRIDE_ERR_CUDA;
     }
     if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[1]), s);
     if (a.total_meshlets != 0) {
-        const cudaError_t e = a.wide_codes ? launch_decode_w<true>(a, cfg, s) : launch_decode_w<false>(a, cfg, s);
+        cudaError_t e;
+        switch (cfg.warps_per_cta) {
+            case 1: e = launch_pair<1>(a, cfg, s, ev); break;
+            case 2: e = launch_pair<2>(a, cfg, s, ev); break;
+            default: e = launch_pair<4>(a, cfg, s, ev); break;
+        }
         if (e != cudaSuccess) return STRIDE_ERR_CUDA;
+    } else if (ev) {
+        cudaEventRecord(static_cast<cudaEvent_t>(ev[2]), s);
     }
-    if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[2]), s);
+    if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[3]), s);
     return STRIDE_OK;
 }
 
