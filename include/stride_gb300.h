@@ -135,6 +135,23 @@ int stride_set_config(stride_handle* h, const stride_launch_cfg* cfg);
 
 void stride_close(stride_handle* h);
 
+/* ---- decode without device allocation ------------------------------------
+ * No counterpart in the reference.  For callers that must not call the CUDA
+ * allocator after start-up -- e.g. a renderer's per-frame streaming loop,
+ * where cudaMalloc/cudaFree synchronise the device and stall other streams,
+ * or a plugin whose host application owns all device memory in its own
+ * pool.  The caller passes the stream bytes on the host and its own device
+ * output buffers (sizes from stride_inspect); the library uploads the bytes
+ * into, and does all decode work in, one fixed 64 MiB device array that
+ * every GPU loading the library reserves until process exit (enough for
+ * streams of about 5 million triangles; larger ones are rejected with
+ * STRIDE_ERR_NOMEM before any device work).  Calls nothing that allocates.
+ * Synchronous: returns after the decode finished on `stream`, with its
+ * status.  The first call on a device looks up the array's device address;
+ * make that first call before any stream capture.  All calls share the
+ * array: decodes that overlap on the GPU race and must be serialised. */
+int stride_decode_static(const uint8_t* data, size_t len, void* stream, uint32_t* d_idx, float* d_pos);
+
 /* ---- many meshes, one launch ---------------------------------------------
  * A batch holds the device copies of many streams and one device meshlet
  * queue over all of them.  Outputs are concatenated: mesh i writes its

@@ -92,6 +92,7 @@ SIGNATURES = [
     ("stride_decode_timed", _I, [_P, _P, _P, _P, _P]),
     ("stride_set_config", _I, [_P, ctypes.POINTER(LaunchCfg)]),
     ("stride_close", None, [_P]),
+    ("stride_decode_static", _I, [_P, _SZ, _P, _P, _P]),
     ("stride_batch_create", _I, [_P, _P, _U32, ctypes.POINTER(_P)]),
     ("stride_batch_info", _I, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
     ("stride_batch_offsets", _I, [_P, _P, _P]),
