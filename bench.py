@@ -56,6 +56,10 @@ def parse_args(argv=None):
     ap.add_argument("--grid", type=int, default=2049)
     ap.add_argument("--tune", type=int, default=1, help="autotune the launch shape before timing")
     ap.add_argument("--batch-meshes", type=int, default=4096)
+    ap.add_argument("--rates", default="50,200,1000,2000", help="serve: Poisson arrival rates (requests/s)")
+    ap.add_argument("--serve-seconds", type=float, default=3.0, help="serve: arrivals per rate span this long")
+    ap.add_argument("--serve-pool", type=int, default=48, help="serve: distinct encoded blobs drawn from")
+    ap.add_argument("--serve-budget-gb", type=int, default=40)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args(argv)
@@ -99,6 +103,13 @@ def barrier(device=None):
 def replica_value(units_per_rank: int, world: int, max_seconds: float) -> float:
     """Whole-job throughput of ``world`` replicas: all units / slowest rank."""
     return units_per_rank * world / max_seconds
+
+
+def shard_range(n: int, rank: int, world: int) -> range:
+    """Contiguous share of ``n`` independent meshes for ``rank`` (no exchange)."""
+    lo = n * rank // world
+    hi = n * (rank + 1) // world
+    return range(lo, hi)
 
 
 # ---------------------------------------------------------------------------
@@ -250,6 +261,54 @@ def run_reference(args):
     return 0
 
 
+def encode_specs(specs, bits: int):
+    """Build and encode mesh specs on all host cores (the encoder and most of
+    the mesh generation run outside the GIL)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    def one(sp):
+        V, T = synth.build_spec(*sp)
+        e = encoder.encode(V, T, precision_error=synth.bbox_bits_error(bits), precision_mode="bbox_frac")
+        return e.data, int(len(T)), int(e.n_v_dup)
+
+    with ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+        return list(ex.map(one, specs))
+
+
+def batch_streams(n_meshes: int, bits: int):
+    specs = synth.mixed_batch_specs(n_meshes, seed=4)
+    enc = encode_specs(specs, bits)
+    kinds = {}
+    for kind, _ in specs:
+        kinds[kind] = kinds.get(kind, 0) + 1
+    blobs = [e[0] for e in enc]
+    cfg = {"workload": f"mixed_{n_meshes}_meshes_{bits}bit", "meshes": n_meshes, "bits": bits,
+           "triangles": int(sum(e[1] for e in enc)), "vertices_dup": int(sum(e[2] for e in enc)),
+           "stream_bytes": int(sum(len(b) for b in blobs)), "kinds": kinds,
+           "sizes": "triangle counts log-uniform in [1K, 200K] (seed 4); 50% grids of random aspect, "
+                    "30% displaced icospheres L3-L7, 20% tori R/r in [2, 5]",
+           "encoder": "project encoder, fitted IRLP, max_verts=max_tris=256"}
+    return blobs, cfg
+
+
+def oracle_rate_meshes(blobs, tris, max_wall: float = 15.0):
+    """CPU oracle (sequential decoder per mesh, meshes spread over all host
+    cores) on a bounded prefix of the meshes -> (M tris/s, cores, sample)."""
+    from concurrent.futures import ThreadPoolExecutor
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    # sample: every 8th mesh (the same size mix), seconds of work
+    pick = list(range(0, len(blobs), 8))
+    acc = sum(tris[i] for i in pick)
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(cores) as ex:
+        list(ex.map(oracle.decode, [blobs[i] for i in pick]))
+    wall = time.perf_counter() - t0
+    return acc / wall / 1e6, cores, f"every 8th mesh: {len(pick)} of {len(blobs)} meshes ({acc} triangles) in " \
+                                   f"{wall:.2f} s (C restatement of decode_dup, one mesh per thread)"
+
+
 def make_stream(args):
     if args.workload == "heightfield":
         return heightfield_stream(args.grid, args.bits)
@@ -327,14 +386,16 @@ def run_single(args):
     value = replica_value(n_t, world, mean_step / 1e3) / 1e6
 
     # Dominant kernel: the slower of connectivity / vertex kernels.  Its
-    # algorithmic bytes: the stream bytes it reads plus the outputs it writes
-    # (connectivity: whole stream in; vertices: indices + positions out).
+    # algorithmic bytes: connectivity reads the whole stream and writes the
+    # indices (12 B per triangle); the vertex kernel writes the positions
+    # (12 B per vertex) from the residual bits, which are already counted in
+    # the stream.  The step's algorithmic bytes are stream + both outputs.
     alg_bytes = len(data) + 12 * (n_v + n_t)
     peak, peak_src = measured_peak()
     k = np.array(kern_ms).mean(axis=0)
     names = ("scan_kernel", "conn_kernel", "vert_kernel")
     dom = 1 + int(np.argmax(k[1:]))
-    dom_bytes = len(data) if dom == 1 else (12 * (n_v + n_t))
+    dom_bytes = (len(data) + 12 * n_t) if dom == 1 else 12 * n_v
     achieved = dom_bytes / (k[dom] / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": ncu_traffic(names[dom], cfg["workload"]),
@@ -395,12 +456,315 @@ def run_single(args):
     return 0
 
 
+def run_batch(args):
+    """Many meshes: one persistent launch over all of them (CUDA graph)
+    against one plain decode launch per mesh, same outputs."""
+    import torch
+    from meshpress_gb300 import ParaDeltaV5GpuDecoder, _lib
+    from meshpress_gb300.batch import BatchDecoder
+    rank, local, world = dist_init("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    blobs, cfg = batch_streams(args.batch_meshes, args.bits)
+    n_t_all = cfg["triangles"]
+    lib = _lib.load()
+    b = BatchDecoder(blobs)
+    launch = None
+    if args.tune:
+        best, best_ms = b.autotune(iters=2)
+        launch = dict(best.as_dict(), tuned_ms=round(best_ms, 4))
+    stream = torch.cuda.Stream(device=dev)
+    with torch.cuda.stream(stream):
+        b.capture_graph(stream)
+    stream.synchronize()
+    b.check()
+
+    # parity: every mesh bit-exact against the oracle
+    exact = None
+    if rank == 0:
+        from concurrent.futures import ThreadPoolExecutor
+        import oracle
+        oracle.build()
+        t_all = b.d_tris.cpu().numpy().view(np.uint32)
+        v_all = b.d_verts.cpu().numpy()
+
+        def same(i):
+            opos, oidx = oracle.decode(blobs[i])
+            return (np.array_equal(t_all[b.t_offset[i]:b.t_offset[i + 1]].astype(np.int64), oidx) and
+                    np.array_equal(v_all[b.v_offset[i]:b.v_offset[i + 1]].view(np.uint32), opos.view(np.uint32)))
+
+        with ThreadPoolExecutor(os.cpu_count() or 1) as ex:
+            exact = all(ex.map(same, range(len(blobs))))
+        del t_all, v_all
+
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    with torch.cuda.stream(stream):
+        for _ in range(max(args.warmup, 3)):
+            flush.fill_(1)
+            b.launch_graph(stream)
+        barrier(dev)
+        torch.cuda.synchronize()
+        clocks.start()
+        time.sleep(0.3)
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)
+            ev[k][0].record(stream)
+            b.launch_graph(stream)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    clk = clocks.stop()
+    b.check()
+    batched_ms = reduce_max(sum(a.elapsed_time(c) for a, c in ev) / args.steps, dev)
+    value = replica_value(n_t_all, world, batched_ms / 1e3) / 1e6
+    kern = np.array([b.decode_timed(stream=stream) for _ in range(3)]).mean(axis=0)
+
+    # per-mesh plain launches (one ParaDeltaV5GpuDecoder per mesh, own outputs)
+    decs = [ParaDeltaV5GpuDecoder(x) for x in blobs]
+    outs = [(torch.empty((d.n_t_total, 3), dtype=torch.int32, device=dev),
+             torch.empty((d.n_v_total, 3), dtype=torch.float32, device=dev)) for d in decs]
+    sh = ctypes.c_void_p(int(stream.cuda_stream))
+    ptrs = [(ctypes.c_void_p(t.data_ptr()), ctypes.c_void_p(v.data_ptr())) for t, v in outs]
+
+    def per_mesh_pass():
+        for d, (pt, pv) in zip(decs, ptrs):
+            _lib.check(lib.stride_decode(d._h, sh, pt, pv, None), "stride_decode")
+
+    with torch.cuda.stream(stream):
+        per_mesh_pass()
+        torch.cuda.synchronize()
+        pm_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                 for _ in range(args.steps)]
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)
+            pm_ev[k][0].record(stream)
+            per_mesh_pass()
+            pm_ev[k][1].record(stream)
+        torch.cuda.synchronize()
+    for d in decs:
+        d.check()
+    per_mesh_ms = reduce_max(sum(a.elapsed_time(c) for a, c in pm_ev) / args.steps, dev)
+    same_as_batch = (torch.equal(torch.cat([t for t, _ in outs]), b.d_tris.view(torch.int32)) and
+                     torch.equal(torch.cat([v for _, v in outs]).view(torch.int32), b.d_verts.view(torch.int32)))
+    for d in decs:
+        d.close()
+    del outs, decs
+
+    # end to end: pinned host image -> device, graph, outputs -> pinned host
+    e2e = None
+    if not args.no_e2e:
+        img = b.make_image()
+        h_img = torch.empty(img.size, dtype=torch.uint8, pin_memory=True)
+        h_img.numpy()[:] = img
+        h_t = torch.empty(b.d_tris.shape, dtype=torch.int32, pin_memory=True)
+        h_v = torch.empty(b.d_verts.shape, dtype=torch.float32, pin_memory=True)
+        ts = []
+        with torch.cuda.stream(stream):
+            for k in range(args.steps + 2):
+                t0 = time.perf_counter()
+                b.upload(h_img.data_ptr(), img.size, stream=stream)
+                b.launch_graph(stream)
+                h_t.copy_(b.d_tris.view(torch.int32), non_blocking=True)
+                h_v.copy_(b.d_verts, non_blocking=True)
+                stream.synchronize()
+                if k >= 2:
+                    ts.append(time.perf_counter() - t0)
+        b.check()
+        e2e_s = reduce_max(sum(ts) / len(ts), dev)
+        e2e = {"value": round(replica_value(n_t_all, world, e2e_s) / 1e6, 3), "unit": "M tris/s",
+               "h2d_bytes_per_step": int(img.size), "d2h_bytes_per_step": 12 * (b.n_t_total + b.n_v_total),
+               "ms_per_step": round(e2e_s * 1e3, 4),
+               "path": "BatchDecoder: stride_batch_upload (pinned arena image) + graph launch + pinned copies out"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        tris = [int(b.t_offset[i + 1] - b.t_offset[i]) for i in range(len(blobs))]
+        v, cores, sample = oracle_rate_meshes(blobs, tris)
+        cpu = {"value": round(v, 3), "unit": "M tris/s", "cores": cores, "kind": "port", "sample": sample}
+
+    if rank == 0:
+        peak, peak_src = measured_peak()
+        names = ("scan_kernel", "conn_kernel", "vert_kernel")
+        dom = 1 + int(np.argmax(kern[1:]))
+        dom_bytes = (cfg["stream_bytes"] + 12 * b.n_t_total) if dom == 1 else 12 * b.n_v_total
+        achieved = dom_bytes / (kern[dom] / 1e3) / 1e9
+        alg = cfg["stream_bytes"] + 12 * (b.n_t_total + b.n_v_total)
+        cfg = dict(cfg)
+        cfg.update(l2="inputs larger than L2 (and a 256 MiB flush before every step)", launch=launch,
+                   parallelism=f"replicas x{world}",
+                   parity="bit-exact vs CPU oracle, every mesh" if exact else f"MISMATCH ({exact})")
+        line = {
+            "metric": "decoded triangles per second", "value": round(value, 3), "unit": "M tris/s",
+            "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": round(batched_ms, 4), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "int32+f32 (exact f64 expression)",
+            "data": "synthetic (seeded mixed meshes; reference meshes not available)", "config": cfg,
+            "per_mesh": {"value": round(replica_value(n_t_all, world, per_mesh_ms / 1e3) / 1e6, 3),
+                         "unit": "M tris/s", "ms_per_step": round(per_mesh_ms, 4),
+                         "launches_per_step": 3 * len(blobs), "same_output_as_batched": bool(same_as_batch)},
+            "batched_over_per_mesh": round(per_mesh_ms / batched_ms, 3),
+            "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                         "frac": round(achieved / peak, 4), "traffic": ncu_traffic(names[dom], cfg["workload"]),
+                         "kernel": names[dom], "kernel_ms": {n: round(float(x), 4) for n, x in zip(names, kern)},
+                         "kernel_alg_bytes": int(dom_bytes), "step_alg_bytes": int(alg), "peak_source": peak_src,
+                         "step_achieved": round(alg / (batched_ms / 1e3) / 1e9, 1),
+                         "step_frac": round(alg / (batched_ms / 1e3) / 1e9 / peak, 4)},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 3 * args.steps, "clocks": clk,
+        }
+        print(json.dumps(line), flush=True)
+    b.close()
+    return 0
+
+
+def run_serve(args):
+    """Poisson arrivals into the continuous-batching server; one line per
+    arrival rate with p50/p99 latency and aggregate throughput."""
+    import threading
+    import torch
+    from meshpress_gb300 import ParaDeltaV5GpuDecoder
+    from meshpress_gb300.serve import DecodeServer
+    rank, local, world = dist_init("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    specs = synth.mixed_batch_specs(args.serve_pool, seed=5, t_min=5e3, t_max=2e6)
+    enc = encode_specs(specs, args.bits)
+    blobs = [e[0] for e in enc]
+    tris = [e[1] for e in enc]
+    # every pool entry decoded alone once, and that checked against the oracle
+    import oracle
+    oracle.build()
+    alone = []
+    pool_exact = True
+    for x in blobs:
+        d = ParaDeltaV5GpuDecoder(x)
+        t, v = d.decode_to_device()
+        alone.append((t.view(torch.int32).clone(), v.view(torch.int32).clone()))
+        if rank == 0:
+            opos, oidx = oracle.decode_mt(x, 0)
+            pool_exact = pool_exact and np.array_equal(t.cpu().numpy().view(np.uint32).astype(np.int64), oidx) \
+                and np.array_equal(v.cpu().numpy().view(np.uint32), opos.view(np.uint32))
+        d.close()
+    rates = [float(r) for r in args.rates.split(",")]
+    rng = np.random.default_rng(11)
+    with DecodeServer(4 << 30) as warm:  # first launches set kernel attributes
+        for rid in [warm.submit(x) for x in blobs[:4]]:
+            assert warm.wait(rid).ok
+            warm.release(rid)
+    for rate in rates:
+        n_req = max(20, int(rate * args.serve_seconds))
+        gaps = rng.exponential(1.0 / rate, n_req)
+        picks = rng.integers(0, len(blobs), n_req)
+        srv = DecodeServer(args.serve_budget_gb << 30, n_streams=3, max_batch=256)
+        ids = [None] * n_req
+        lat, ok = [], [0, 0]
+        first_submit = [None]
+        last_done = [0.0]
+
+        def feed():
+            t_next = time.perf_counter()
+            for i in range(n_req):
+                t_next += gaps[i]
+                dt = t_next - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                ids[i] = srv.submit(blobs[picks[i]])
+
+        th = threading.Thread(target=feed)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        th.start()
+        for i in range(n_req):
+            while ids[i] is None:
+                time.sleep(0.0002)
+            r = srv.wait(ids[i])
+            good = r.ok and torch.equal(r.tris.view(torch.int32), alone[picks[i]][0]) and \
+                torch.equal(r.verts.view(torch.int32), alone[picks[i]][1])
+            ok[0 if good else 1] += 1
+            lat.append(r.latency_ms)
+            if first_submit[0] is None:
+                first_submit[0] = r.t_submit_us
+            last_done[0] = max(last_done[0], r.t_done_us)
+            srv.release(ids[i])
+        th.join()
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        span_s = (last_done[0] - first_submit[0]) / 1e6
+        total_t = int(sum(tris[j] for j in picks))
+        if rank == 0:
+            line = {
+                "metric": "served decode latency p50/p99 and throughput", "value": round(total_t / span_s / 1e6, 3),
+                "unit": "M tris/s", "n_gpus": world, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "int32+f32 (exact f64 expression)",
+                "data": "synthetic (seeded mixed meshes)",
+                "config": {"workload": f"serve_poisson_{int(rate)}rps", "rate_rps": rate, "requests": n_req,
+                           "pool": len(blobs), "pool_triangles": int(sum(tris)),
+                           "sizes": "log-uniform [5K, 2M] triangles from the many-mesh generator (seed 5)",
+                           "hbm_budget_gb": args.serve_budget_gb, "streams": 3, "max_batch": 256},
+                "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3),
+                               "p99": round(float(np.percentile(lat, 99)), 3),
+                               "max": round(float(np.max(lat)), 3),
+                               "to": "outputs resident on the device"},
+                "achieved_rps": round(n_req / span_s, 1), "launches": st["launches"],
+                "mean_requests_per_launch": round(n_req / max(1, st["launches"]), 2),
+                "arena_peak_gb": round(st["arena_peak_bytes"] / 2 ** 30, 3),
+                "exact_responses": ok[0], "mismatched_responses": ok[1],
+                "pool_bit_exact_vs_oracle": bool(pool_exact), "wall_s": round(wall, 3),
+            }
+            print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_reference_batch(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return 0
+    blobs, cfg = batch_streams(args.batch_meshes, args.bits)
+    from concurrent.futures import ThreadPoolExecutor
+    import oracle
+    oracle.build()
+    cores = os.cpu_count() or 1
+    # bounded sample per step: every 16th mesh (the same size mix)
+    sample_blobs = blobs[::16]
+    acc = sum(oracle.parse_header(x).n_t for x in sample_blobs)
+    with ThreadPoolExecutor(cores) as ex:
+        for _ in range(max(1, args.warmup)):
+            list(ex.map(oracle.decode, sample_blobs))
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            list(ex.map(oracle.decode, sample_blobs))
+        wall = time.perf_counter() - t0
+    value = acc * args.steps / wall / 1e6
+    sample = f"per step every 16th mesh: {len(sample_blobs)} of {len(blobs)} meshes ({acc} triangles), " \
+             f"one mesh per thread"
+    line = {
+        "impl": "reference", "metric": "decoded triangles per second", "value": round(value, 3),
+        "unit": "M tris/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(wall / args.steps * 1e3, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int64+f64->f32", "data": "synthetic", "config": cfg,
+        "cpu_baseline": {"value": round(value, 3), "unit": "M tris/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": round(value, 3), "unit": "M tris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main(argv=None):
     args = parse_args(argv)
-    if args.workload in ("batch", "serve"):
-        raise SystemExit(f"workload {args.workload!r} is not wired into bench.py yet")
     if args.impl == "reference":
+        if args.workload == "batch":
+            return run_reference_batch(args)
+        if args.workload == "serve":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no serving path "
+                                                                  "(one decoder object per stream)"}))
+            return 0
         return run_reference(args)
+    if args.workload == "batch":
+        return run_batch(args)
+    if args.workload == "serve":
+        return run_serve(args)
     return run_single(args)
 
 

@@ -144,7 +144,7 @@ void stride_close(stride_handle* h);
  * output buffers (sizes from stride_inspect); the library uploads the bytes
  * into, and does all decode work in, one fixed 64 MiB device array that
  * every GPU loading the library reserves until process exit (enough for
- * streams of about 5 million triangles; larger ones are rejected with
+ * streams of about 10 million triangles; larger ones are rejected with
  * STRIDE_ERR_NOMEM before any device work).  Calls nothing that allocates.
  * Synchronous: returns after the decode finished on `stream`, with its
  * status.  The first call on a device looks up the array's device address;
@@ -169,6 +169,15 @@ int stride_batch_offsets(const stride_batch* b, uint64_t* v_offset, uint64_t* t_
 int stride_batch_set_config(stride_batch* b, const stride_launch_cfg* cfg);
 int stride_batch_get_config(const stride_batch* b, stride_launch_cfg* cfg);
 int stride_batch_decode(stride_batch* b, void* stream, uint32_t* d_idx, float* d_pos);
+/* Same decode, synchronous, with the device time of the scan, connectivity
+ * and vertex kernels (CUDA events) in kernel_ms[0..2]. */
+int stride_batch_decode_timed(stride_batch* b, void* stream, uint32_t* d_idx, float* d_pos, float* kernel_ms);
+/* The arena image: stream i sits at blob_offsets[i] of an image_bytes-long
+ * buffer (zero bytes elsewhere).  A caller that keeps such an image in
+ * (pinned) host memory replaces every stream of the batch with one
+ * asynchronous copy on `stream` through stride_batch_upload. */
+int stride_batch_image(const stride_batch* b, uint64_t* blob_offsets, uint64_t* image_bytes);
+int stride_batch_upload(stride_batch* b, void* stream, const void* image, size_t bytes);
 /* Capture the decode sequence for these output pointers into a CUDA graph
  * (replaces any earlier graph) and replay it with stride_batch_launch_graph. */
 int stride_batch_capture_graph(stride_batch* b, void* stream, uint32_t* d_idx, float* d_pos);

@@ -99,6 +99,9 @@ SIGNATURES = [
     ("stride_batch_set_config", _I, [_P, ctypes.POINTER(LaunchCfg)]),
     ("stride_batch_get_config", _I, [_P, ctypes.POINTER(LaunchCfg)]),
     ("stride_batch_decode", _I, [_P, _P, _P, _P]),
+    ("stride_batch_decode_timed", _I, [_P, _P, _P, _P, _P]),
+    ("stride_batch_image", _I, [_P, _P, ctypes.POINTER(_U64)]),
+    ("stride_batch_upload", _I, [_P, _P, _P, _SZ]),
     ("stride_batch_capture_graph", _I, [_P, _P, _P, _P]),
     ("stride_batch_launch_graph", _I, [_P, _P]),
     ("stride_batch_autotune", _I, [_P, _P, _P, _P, _I, ctypes.POINTER(LaunchCfg),

@@ -72,6 +72,38 @@ class BatchDecoder:
             self.check()
         return self.d_tris, self.d_verts
 
+    def decode_timed(self, *, stream=None):
+        """Synchronous decode; -> device milliseconds of (scan, connectivity,
+        vertex) kernels."""
+        i, p = self._ptrs()
+        ms = (ctypes.c_float * 3)()
+        _lib.check(self._lib.stride_batch_decode_timed(self._h, self._stream(stream), i, p, ms), "decode_timed")
+        self.check()
+        return tuple(float(x) for x in ms)
+
+    def image(self):
+        """-> (blob offsets (n_meshes,), image bytes): layout of the arena
+        image that ``upload`` takes."""
+        off = np.zeros(self.n_meshes, np.uint64)
+        nb = ctypes.c_uint64()
+        _lib.check(self._lib.stride_batch_image(self._h, ctypes.c_void_p(off.ctypes.data), ctypes.byref(nb)))
+        return off.astype(np.int64), int(nb.value)
+
+    def make_image(self, blobs=None) -> np.ndarray:
+        """Host arena image of ``blobs`` (default: the batch's own streams)."""
+        blobs = self._blobs if blobs is None else [bytes(b) for b in blobs]
+        off, nb = self.image()
+        img = np.zeros(nb, np.uint8)
+        for o, b in zip(off, blobs):
+            img[o:o + len(b)] = np.frombuffer(b, np.uint8)
+        return img
+
+    def upload(self, image_ptr: int, nbytes: int, *, stream=None):
+        """Replace every stream from a host image (one asynchronous copy
+        when the image is in pinned memory)."""
+        _lib.check(self._lib.stride_batch_upload(self._h, self._stream(stream), ctypes.c_void_p(image_ptr),
+                                                 int(nbytes)), "stride_batch_upload")
+
     def check(self):
         bm, bl = ctypes.c_uint32(), ctypes.c_uint32()
         _lib.check(self._lib.stride_batch_status(self._h, 1, ctypes.byref(bm), ctypes.byref(bl)), "batch decode")

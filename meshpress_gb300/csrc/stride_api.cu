@@ -142,9 +142,8 @@ struct stride_handle {
     MeshletDesc* d_descs = nullptr;
     uint4* d_blk_sums = nullptr;
     BlockPrefix* d_blk_prefix = nullptr;
-    uint32_t* d_tri_scratch = nullptr;
     uint32_t* d_walk_scratch = nullptr;
-    unsigned long long tri_cap = 0, walk_cap = 0;
+    unsigned long long walk_cap = 0;
     Status* d_status = nullptr;
     uint32_t* d_idx = nullptr;
     float* d_pos = nullptr;
@@ -160,14 +159,12 @@ static void free_buffers(stride_handle* h) {
     cudaFree(h->d_descs);
     cudaFree(h->d_blk_sums);
     cudaFree(h->d_blk_prefix);
-    cudaFree(h->d_tri_scratch);
     cudaFree(h->d_walk_scratch);
     cudaFree(h->d_status);
     cudaFree(h->d_idx);
     cudaFree(h->d_pos);
-    h->d_tri_scratch = nullptr;
     h->d_walk_scratch = nullptr;
-    h->tri_cap = h->walk_cap = 0;
+    h->walk_cap = 0;
     h->d_blob = nullptr;
     h->d_params = nullptr;
     h->d_descs = nullptr;
@@ -178,16 +175,9 @@ static void free_buffers(stride_handle* h) {
     h->d_pos = nullptr;
 }
 
-static int ensure_capacity(stride_handle* h, size_t len, uint32_t n_meshlets, uint64_t n_v, uint64_t n_t) {
+static int ensure_capacity(stride_handle* h, size_t len, uint32_t n_meshlets, uint64_t n_v) {
     cudaError_t e;
-    const unsigned long long tw = tri_scratch_words(n_t, n_meshlets);
     const unsigned long long ww = walk_scratch_words(n_v, n_meshlets);
-    if (tw > h->tri_cap) {
-        cudaFree(h->d_tri_scratch);
-        h->d_tri_scratch = nullptr;
-        if ((e = cudaMalloc(&h->d_tri_scratch, 4ull * tw)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(scratch)");
-        h->tri_cap = tw;
-    }
     if (ww > h->walk_cap) {
         cudaFree(h->d_walk_scratch);
         h->d_walk_scratch = nullptr;
@@ -285,7 +275,7 @@ int stride_open(const uint8_t* data, size_t len, stride_handle** out) {
     h->params = p;
     h->len = len;
     cudaError_t e;
-    if ((rc = ensure_capacity(h, len, p.n_meshlets, p.n_v, p.n_t)) != STRIDE_OK) {
+    if ((rc = ensure_capacity(h, len, p.n_meshlets, p.n_v)) != STRIDE_OK) {
         free_buffers(h);
         delete h;
         return rc;
@@ -311,7 +301,7 @@ int stride_reload(stride_handle* h, const uint8_t* data, size_t len, void* strea
     char why[256] = {0};
     int rc = parse_header(data, len, &p, why, sizeof(why));
     if (rc) return fail(rc, "%s", why);
-    if ((rc = ensure_capacity(h, len, p.n_meshlets, p.n_v, p.n_t)) != STRIDE_OK) return rc;
+    if ((rc = ensure_capacity(h, len, p.n_meshlets, p.n_v)) != STRIDE_OK) return rc;
     h->params = p;
     h->len = len;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -340,9 +330,7 @@ static DecodeArgs handle_args(stride_handle* h, uint32_t* d_idx, float* d_pos, i
     a.descs = h->d_descs;
     a.blk_sums = h->d_blk_sums;
     a.blk_prefix = h->d_blk_prefix;
-    a.tri_scratch = h->d_tri_scratch;
     a.walk_scratch = h->d_walk_scratch;
-    a.tri_cap = h->tri_cap;
     a.walk_cap = h->walk_cap;
     a.status = h->d_status;
     a.idx = d_idx;
@@ -354,6 +342,8 @@ static DecodeArgs handle_args(stride_handle* h, uint32_t* d_idx, float* d_pos, i
 
 int stride_decode_timed(stride_handle* h, void* stream, uint32_t* d_idx, float* d_pos, float* kernel_ms) {
     if (!h || !d_idx || !d_pos) return fail(STRIDE_ERR_ARG, "null argument");
+    if ((reinterpret_cast<uintptr_t>(d_idx) & 15u) || (reinterpret_cast<uintptr_t>(d_pos) & 3u))
+        return fail(STRIDE_ERR_ARG, "index output must be 16-byte aligned, positions 4-byte aligned");
     cudaEvent_t ev[4];
     for (auto& e : ev) cudaEventCreate(&e);
     void* evp[4] = {ev[0], ev[1], ev[2], ev[3]};
@@ -377,6 +367,9 @@ int stride_decode_timed(stride_handle* h, void* stream, uint32_t* d_idx, float* 
 int stride_decode(stride_handle* h, void* stream, uint32_t* d_idx, float* d_pos, int32_t* d_codes) {
     if (!h) return fail(STRIDE_ERR_ARG, "null handle");
     if ((!d_idx && h->params.n_t) || (!d_pos && h->params.n_v)) return fail(STRIDE_ERR_ARG, "null output pointer");
+    if ((reinterpret_cast<uintptr_t>(d_idx) & 15u) || (reinterpret_cast<uintptr_t>(d_pos) & 3u) ||
+        (reinterpret_cast<uintptr_t>(d_codes) & 3u))
+        return fail(STRIDE_ERR_ARG, "index output must be 16-byte aligned, positions and codes 4-byte aligned");
     const int rc = enqueue_decode(handle_args(h, d_idx, d_pos, d_codes), h->cfg, stream);
     if (rc) return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     cudaError_t e = cudaEventRecord(h->done, static_cast<cudaStream_t>(stream));

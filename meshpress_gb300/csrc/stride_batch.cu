@@ -18,6 +18,7 @@ using namespace stride;
 struct stride_batch {
     uint32_t n_meshes = 0;
     uint32_t total_meshlets = 0;
+    uint64_t arena_bytes = 0;
     uint64_t total_v = 0, total_t = 0;
     std::vector<MeshParams> params;
     uint8_t* d_arena = nullptr;
@@ -26,9 +27,8 @@ struct stride_batch {
     MeshletDesc* d_descs = nullptr;
     uint4* d_blk_sums = nullptr;
     BlockPrefix* d_blk_prefix = nullptr;
-    uint32_t* d_tri_scratch = nullptr;
     uint32_t* d_walk_scratch = nullptr;
-    unsigned long long tri_cap = 0, walk_cap = 0;
+    unsigned long long walk_cap = 0;
     Status* d_status = nullptr;
     bool wide = false;
     LaunchCfg cfg;
@@ -84,7 +84,6 @@ static void batch_free(stride_batch* b) {
     cudaFree(b->d_descs);
     cudaFree(b->d_blk_sums);
     cudaFree(b->d_blk_prefix);
-    cudaFree(b->d_tri_scratch);
     cudaFree(b->d_walk_scratch);
     cudaFree(b->d_status);
 }
@@ -99,9 +98,7 @@ static DecodeArgs batch_args(const stride_batch* b, uint32_t* d_idx, float* d_po
     a.descs = b->d_descs;
     a.blk_sums = b->d_blk_sums;
     a.blk_prefix = b->d_blk_prefix;
-    a.tri_scratch = b->d_tri_scratch;
     a.walk_scratch = b->d_walk_scratch;
-    a.tri_cap = b->tri_cap;
     a.walk_cap = b->walk_cap;
     a.status = b->d_status;
     a.idx = d_idx;
@@ -144,8 +141,8 @@ int stride_batch_create(const uint8_t* const* blobs, const size_t* lens, uint32_
         delete b;
         return rc;
     }
-    if (b->wide) b->cfg.code_bytes = std::max<uint32_t>(b->cfg.code_bytes, kMaxLocal * 16u);
-    b->tri_cap = tri_scratch_words(b->total_t, b->total_meshlets);
+    if (b->wide) b->cfg.code_bytes = std::max<uint32_t>(b->cfg.code_bytes, kMaxLocal * 4u);
+    b->arena_bytes = arena_bytes;
     b->walk_cap = walk_scratch_words(b->total_v, b->total_meshlets);
     std::vector<uint8_t> arena(arena_bytes, 0);
     for (uint32_t i = 0; i < n_meshes; i++) std::memcpy(arena.data() + off[i], blobs[i], lens[i]);
@@ -163,7 +160,6 @@ int stride_batch_create(const uint8_t* const* blobs, const size_t* lens, uint32_
             cudaSuccess ||
         (e = cudaMalloc(&b->d_blk_sums, sizeof(uint4) * std::max<uint32_t>(1u, nb))) != cudaSuccess ||
         (e = cudaMalloc(&b->d_blk_prefix, sizeof(BlockPrefix) * std::max<uint32_t>(1u, nb))) != cudaSuccess ||
-        (e = cudaMalloc(&b->d_tri_scratch, 4ull * b->tri_cap)) != cudaSuccess ||
         (e = cudaMalloc(&b->d_walk_scratch, 4ull * b->walk_cap)) != cudaSuccess ||
         (e = cudaMalloc(&b->d_status, sizeof(Status))) != cudaSuccess ||
         (e = cudaMemcpy(b->d_arena, arena.data(), arena_bytes, cudaMemcpyHostToDevice)) != cudaSuccess ||
@@ -214,12 +210,57 @@ int stride_batch_get_config(const stride_batch* b, stride_launch_cfg* c) {
 
 int stride_batch_decode(stride_batch* b, void* stream, uint32_t* d_idx, float* d_pos) {
     if (!b) return fail(STRIDE_ERR_ARG, "null batch");
+    if ((!d_idx && b->total_t) || (!d_pos && b->total_v)) return fail(STRIDE_ERR_ARG, "null output pointer");
+    if ((reinterpret_cast<uintptr_t>(d_idx) & 15u) || (reinterpret_cast<uintptr_t>(d_pos) & 3u))
+        return fail(STRIDE_ERR_ARG, "index output must be 16-byte aligned, positions 4-byte aligned");
     const int rc = enqueue_decode(batch_args(b, d_idx, d_pos), b->cfg, stream);
     if (rc) return fail(rc, "batch decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     cudaError_t e = cudaEventRecord(b->done, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
     b->launched = true;
     return STRIDE_OK;
+}
+
+int stride_batch_image(const stride_batch* b, uint64_t* blob_offsets, uint64_t* image_bytes) {
+    if (!b) return fail(STRIDE_ERR_ARG, "null batch");
+    if (blob_offsets)
+        for (uint32_t i = 0; i < b->n_meshes; i++) blob_offsets[i] = b->params[i].blob_off;
+    if (image_bytes) *image_bytes = b->arena_bytes;
+    return STRIDE_OK;
+}
+
+int stride_batch_upload(stride_batch* b, void* stream, const void* image, size_t bytes) {
+    if (!b || !image) return fail(STRIDE_ERR_ARG, "null argument");
+    if (bytes != b->arena_bytes)
+        return fail(STRIDE_ERR_ARG, "image is %zu bytes, the batch's arena %llu", bytes,
+                    static_cast<unsigned long long>(b->arena_bytes));
+    const cudaError_t e =
+        cudaMemcpyAsync(b->d_arena, image, bytes, cudaMemcpyHostToDevice, static_cast<cudaStream_t>(stream));
+    return e == cudaSuccess ? STRIDE_OK : cuda_fail(e, "stride_batch_upload");
+}
+
+int stride_batch_decode_timed(stride_batch* b, void* stream, uint32_t* d_idx, float* d_pos, float* kernel_ms) {
+    if (!b || !d_idx || !d_pos) return fail(STRIDE_ERR_ARG, "null argument");
+    if ((reinterpret_cast<uintptr_t>(d_idx) & 15u) || (reinterpret_cast<uintptr_t>(d_pos) & 3u))
+        return fail(STRIDE_ERR_ARG, "index output must be 16-byte aligned, positions 4-byte aligned");
+    cudaEvent_t ev[4];
+    for (auto& e : ev) cudaEventCreate(&e);
+    void* evp[4] = {ev[0], ev[1], ev[2], ev[3]};
+    int rc = enqueue_decode(batch_args(b, d_idx, d_pos), b->cfg, stream, evp);
+    if (rc == STRIDE_OK) {
+        cudaEventRecord(b->done, static_cast<cudaStream_t>(stream));
+        b->launched = true;
+        const cudaError_t e = cudaEventSynchronize(ev[3]);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(e, "stride_batch_decode_timed");
+        } else if (kernel_ms) {
+            for (int i = 0; i < 3; i++) cudaEventElapsedTime(&kernel_ms[i], ev[i], ev[i + 1]);
+        }
+    } else {
+        rc = fail(rc, "batch decode launch failed");
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+    return rc;
 }
 
 int stride_batch_capture_graph(stride_batch* b, void* stream, uint32_t* d_idx, float* d_pos) {
@@ -271,7 +312,9 @@ int stride_batch_autotune(stride_batch* b, void* stream, uint32_t* d_idx, float*
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     std::vector<LaunchCfg> cands;
     const uint32_t stage_opts[] = {8u * 1024u, 12u * 1024u, 16u * 1024u, 24u * 1024u};
-    const uint32_t code_opts[] = {16u * 1024u, 24u * 1024u, 32u * 1024u, 48u * 1024u};
+    // code plane per warp: 2 bytes per vertex (4 above 16-bit codes), 32
+    // meshlets of up to 256 vertices fill 16 KiB
+    const uint32_t code_opts[] = {6u * 1024u, 8u * 1024u, 12u * 1024u, 16u * 1024u};
     for (int w : {1, 2, 4})
         for (uint32_t st : stage_opts)
             for (uint32_t cb : code_opts)
@@ -279,7 +322,7 @@ int stride_batch_autotune(stride_batch* b, void* stream, uint32_t* d_idx, float*
                     LaunchCfg c;
                     c.warps_per_cta = w;
                     c.stage_bytes = st;
-                    c.code_bytes = cb;
+                    c.code_bytes = b->wide ? 2u * cb : cb;
                     c.persistent = pers;
                     c.ctas_per_sm = 0;  // persistent grid sized by the occupancy calculator
                     if (check_config(c, b->wide)) continue;

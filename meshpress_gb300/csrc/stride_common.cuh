@@ -64,15 +64,15 @@ struct __align__(16) MeshletDesc {
     uint32_t n_strips;
     uint32_t v_pref;       // exclusive prefixes inside the scan block:
     uint32_t t_pref;       //   n_local, n_tris,
-    uint32_t tp_pref;      //   n_tris rounded up to 4 (triangle scratch),
     uint32_t wp_pref;      //   n_local rounded up to 4 (walk scratch)
+    uint32_t pad0;
     uint32_t anchor_bit;   // end of connectivity = anchor codes
     uint32_t walk;         // n_kind0 | n_walk << 16
     uint32_t pad[6];
 };
 
 struct BlockPrefix {
-    unsigned long long v, t, tp, wp;
+    unsigned long long v, t, wp, pad;
 };
 
 struct Status {
@@ -87,8 +87,8 @@ struct LaunchCfg {
     int warps_per_cta = 2;
     int persistent = 1;
     int ctas_per_sm = 0;
-    uint32_t stage_bytes = 16 * 1024;  // per-warp payload staging
-    uint32_t code_bytes = 32 * 1024;   // per-warp integer code planes (vertex kernel)
+    uint32_t stage_bytes = 16 * 1024;  // per-warp payload staging (vertex kernel: half)
+    uint32_t code_bytes = 12 * 1024;   // per-warp integer code plane (vertex kernel)
 };
 
 struct DecodeArgs {
@@ -100,12 +100,10 @@ struct DecodeArgs {
     MeshletDesc* descs;              // device scratch, total_meshlets
     uint4* blk_sums;                 // device scratch, scan blocks
     BlockPrefix* blk_prefix;         // device scratch, scan blocks
-    uint32_t* tri_scratch;           // packed local triangles, 4-aligned per meshlet
     uint32_t* walk_scratch;          // walk entries, 4-aligned per meshlet
-    unsigned long long tri_cap;      // words in tri_scratch
     unsigned long long walk_cap;     // words in walk_scratch
     Status* status;                  // device
-    uint32_t* idx;                   // device outputs
+    uint32_t* idx;                   // device outputs (idx 16-byte aligned)
     float* pos;
     int32_t* codes;                  // optional
     bool wide_codes;                 // some mesh has g_bits > 16
@@ -115,10 +113,7 @@ inline uint32_t scan_blocks(uint32_t total_meshlets) {
     return (total_meshlets + kScanThreads - 1) / kScanThreads;
 }
 
-// Scratch words needed for a stream set with these totals.
-inline unsigned long long tri_scratch_words(unsigned long long n_t, unsigned long long meshlets) {
-    return n_t + 3ull * meshlets + 4ull;
-}
+// Walk scratch words needed for a stream set with these totals.
 inline unsigned long long walk_scratch_words(unsigned long long n_v, unsigned long long meshlets) {
     return n_v + 3ull * meshlets + 4ull;
 }

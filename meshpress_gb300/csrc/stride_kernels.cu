@@ -5,26 +5,28 @@
 //  1. scan_kernel -- one thread per meshlet: offset table entry + 48-bit
 //     meshlet header (n_local, n_tris, n_strips), range checks, and a
 //     device-wide exclusive scan of n_local / n_tris (output placement) and
-//     of their multiples of four (scratch placement): block scans plus a
-//     last-block scan of the block sums.
+//     of n_local rounded up to four (walk scratch placement): block scans
+//     plus a last-block scan of the block sums.
 //
 //  2. conn_kernel -- a warp owns 32 consecutive meshlets, one per lane.  One
 //     bulk copy (cp.async.bulk + mbarrier) stages the group's bytes in
 //     shared memory; each lane replays its meshlet's strip connectivity
 //     (decode_dup's strip loop, encoder/paradelta_v5_dup.py:513-542) with the
 //     16-entry move-to-tail FIFO (_read_vert, encoder/paradelta_codec.py:
-//     330-340) held in registers, writes packed local triangles and the
-//     first-occurrence walk (vertex, kind, IRLP references) to scratch with
-//     16-byte stores, and records where the connectivity ends (the anchor).
+//     330-340) held in registers, writes the final triangle indices (four
+//     triangles = three aligned 16-byte stores) and the first-occurrence walk
+//     (vertex, kind, IRLP references) to scratch, and records where the
+//     connectivity ends (the anchor).
 //
 //  3. vert_kernel -- same warp/lane mapping.  Each lane bulk-copies its
 //     meshlet's residual bits (anchor to end) into shared memory, skips the
-//     three delta substreams to find the first parallelogram substream, then
-//     reconstructs the integer codes one axis at a time in walk order (IRLP,
-//     encoder/paradelta_v5_dup.py:91-104 and 581-600; every walk entry reads
-//     one residual, so all lanes do the same work per step).  The warp then
-//     writes each meshlet's triangles (global ids) and positions (exact
-//     dequantisation, stride_dequant.h) with coalesced 128-bit stores.
+//     three short delta substreams, then reconstructs the integer codes one
+//     axis at a time in walk order (IRLP, encoder/paradelta_v5_dup.py:91-104
+//     and 581-600).  Each pass leaves the parallelogram cursor at the next
+//     axis' substream, so no substream boundary has to be searched for, and
+//     only one axis of codes lives in shared memory at a time: after each
+//     pass the warp writes that coordinate of every vertex (exact
+//     dequantisation, stride_dequant.h).
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -169,26 +171,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
 }
 
 // ---------------------------------------------------------------------------
-// Warp-cooperative output: n consecutive 32-bit words at dst, 16-byte
-// vector stores for the aligned body.
-// ---------------------------------------------------------------------------
-template <class F>
-__device__ __forceinline__ void warp_store_words(uint32_t* dst, uint32_t n, F f, int lane) {
-    uint32_t head = static_cast<uint32_t>((16u - (reinterpret_cast<uintptr_t>(dst) & 15u)) & 15u) >> 2;
-    if (head > n) head = n;
-    if (static_cast<uint32_t>(lane) < head) dst[lane] = f(static_cast<uint32_t>(lane));
-    const uint32_t rem = n - head;
-    const uint32_t nvec = rem >> 2;
-    uint4* v = reinterpret_cast<uint4*>(dst + head);
-    for (uint32_t i = lane; i < nvec; i += 32u) {
-        const uint32_t b = head + 4u * i;
-        v[i] = make_uint4(f(b), f(b + 1u), f(b + 2u), f(b + 3u));
-    }
-    const uint32_t t0 = head + 4u * nvec;
-    if (static_cast<uint32_t>(lane) < n - t0) dst[t0 + lane] = f(t0 + lane);
-}
-
-// ---------------------------------------------------------------------------
 // 1. scan kernel
 // ---------------------------------------------------------------------------
 __device__ int scan_meshlet(const uint8_t* __restrict__ arena, const MeshParams& P, uint32_t lm, MeshletDesc& d) {
@@ -268,13 +250,11 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a) {
     }
     unsigned long long t1, t2;
     const unsigned long long e1 = block_scan((static_cast<unsigned long long>(nt) << 32) | nl, wsum, t1);
-    const unsigned long long e2 =
-        block_scan((static_cast<unsigned long long>((nt + 3u) & ~3u) << 32) | ((nl + 3u) & ~3u), wsum, t2);
+    const unsigned long long e2 = block_scan((nl + 3u) & ~3u, wsum, t2);
     if (m < a.total_meshlets) {
         d.v_pref = static_cast<uint32_t>(e1);
         d.t_pref = static_cast<uint32_t>(e1 >> 32);
         d.wp_pref = static_cast<uint32_t>(e2);
-        d.tp_pref = static_cast<uint32_t>(e2 >> 32);
         uint4* dst = reinterpret_cast<uint4*>(a.descs + m);
         const uint4* src = reinterpret_cast<const uint4*>(&d);
         dst[0] = src[0];
@@ -284,7 +264,7 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a) {
     }
     if (tid == 0)
         a.blk_sums[blockIdx.x] = make_uint4(static_cast<uint32_t>(t1), static_cast<uint32_t>(t1 >> 32),
-                                            static_cast<uint32_t>(t2 >> 32), static_cast<uint32_t>(t2));
+                                            static_cast<uint32_t>(t2), 0u);
     // The last block to finish turns the block sums into block prefixes.
     __threadfence();
     __syncthreads();
@@ -292,26 +272,25 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a) {
     __syncthreads();
     if (!is_last) return;
     __threadfence();
-    BlockPrefix carry = {0ull, 0ull, 0ull, 0ull};
+    unsigned long long cv = 0ull, ct = 0ull, cw = 0ull;
     for (uint32_t base = 0; base < gridDim.x; base += kScanThreads) {
         const uint32_t i = base + tid;
         const uint4 s = i < gridDim.x ? __ldcg(a.blk_sums + i) : make_uint4(0u, 0u, 0u, 0u);
         // per-chunk sums stay below 2^32 (256 blocks x 65536), so pack pairs
         unsigned long long ta, tb;
         const unsigned long long ea = block_scan((static_cast<unsigned long long>(s.y) << 32) | s.x, wsum, ta);
-        const unsigned long long eb = block_scan((static_cast<unsigned long long>(s.z) << 32) | s.w, wsum, tb);
+        const unsigned long long eb = block_scan(s.z, wsum, tb);
         if (i < gridDim.x) {
             BlockPrefix p;
-            p.v = carry.v + (ea & 0xFFFFFFFFull);
-            p.t = carry.t + (ea >> 32);
-            p.tp = carry.tp + (eb >> 32);
-            p.wp = carry.wp + (eb & 0xFFFFFFFFull);
+            p.v = cv + (ea & 0xFFFFFFFFull);
+            p.t = ct + (ea >> 32);
+            p.wp = cw + eb;
+            p.pad = 0ull;
             a.blk_prefix[i] = p;
         }
-        carry.v += ta & 0xFFFFFFFFull;
-        carry.t += ta >> 32;
-        carry.tp += tb >> 32;
-        carry.wp += tb & 0xFFFFFFFFull;
+        cv += ta & 0xFFFFFFFFull;
+        ct += ta >> 32;
+        cw += tb;
     }
 }
 
@@ -363,7 +342,8 @@ struct Fifo {
     }
 };
 
-// 4-entry register buffer flushed to 16-byte aligned scratch.
+// 4-entry register buffer: four triangles (one 48-byte, 16-byte aligned
+// output quad) or four walk entries.
 struct Quad {
     uint32_t q0 = 0, q1 = 0, q2 = 0, q3 = 0;
     __device__ __forceinline__ void put(uint32_t slot, uint32_t v) {
@@ -371,6 +351,9 @@ struct Quad {
         q1 = slot == 1u ? v : q1;
         q2 = slot == 2u ? v : q2;
         q3 = slot == 3u ? v : q3;
+    }
+    __device__ __forceinline__ uint32_t get(uint32_t slot) const {
+        return slot == 0u ? q0 : (slot == 1u ? q1 : (slot == 2u ? q2 : q3));
     }
 };
 
@@ -381,6 +364,32 @@ __device__ __forceinline__ void quad_tail(const Quad& q, uint32_t cnt, uint32_t*
     if (r > 0u) p[0] = q.q0;
     if (r > 1u) p[1] = q.q1;
     if (r > 2u) p[2] = q.q2;
+}
+
+// Writes the triangles held in slots [lo, hi) of q as global vertex ids.
+// Slot s is the meshlet's triangle `first + s`, and the quad's first
+// triangle sits at a multiple of four in the output, so a full quad is
+// three aligned 16-byte stores; slots before the meshlet's first triangle
+// (lo > 0) or past its last (hi < 4) go out as single words.
+__device__ __forceinline__ void store_tris(const Quad& q, uint32_t* out, int first, int lo, int hi, uint32_t vloc) {
+    auto id = [vloc](uint32_t packed, uint32_t k) { return vloc + ((packed >> (8u * k)) & 0xFFu); };
+    if (lo == 0 && hi == 4) {
+        uint4* o = reinterpret_cast<uint4*>(out + 3ll * first);
+        o[0] = make_uint4(id(q.q0, 0), id(q.q0, 1), id(q.q0, 2), id(q.q1, 0));
+        o[1] = make_uint4(id(q.q1, 1), id(q.q1, 2), id(q.q2, 0), id(q.q2, 1));
+        o[2] = make_uint4(id(q.q2, 2), id(q.q3, 0), id(q.q3, 1), id(q.q3, 2));
+    } else {
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+            if (s >= lo && s < hi) {
+                const uint32_t p = q.get(static_cast<uint32_t>(s));
+                uint32_t* o = out + 3ll * (first + s);
+                o[0] = id(p, 0);
+                o[1] = id(p, 1);
+                o[2] = id(p, 2);
+            }
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -394,8 +403,9 @@ __host__ __device__ inline uint32_t conn_warp_bytes(uint32_t stage_bytes) {
 
 __host__ __device__ inline uint32_t vert_stage_bytes(uint32_t stage_bytes) { return stage_bytes / 2u; }
 
+// residual stage | code plane | dequantisation constants (8 words) | mbarrier
 __host__ __device__ inline uint32_t vert_warp_bytes(uint32_t stage_bytes, uint32_t code_bytes) {
-    return align16(vert_stage_bytes(stage_bytes) + 32u) + align16(code_bytes) + 3u * 8u * 4u + 16u + 16u;
+    return align16(vert_stage_bytes(stage_bytes) + 32u) + align16(code_bytes) + 32u + 16u;
 }
 
 struct GroupLane {
@@ -404,7 +414,7 @@ struct GroupLane {
     MeshletDesc d;
     uint32_t mi;
     const MeshParams* P;
-    unsigned long long v_base, t_base, tp_base, wp_base;
+    unsigned long long v_base, t_base, wp_base;
     unsigned long long blob_off;
 };
 
@@ -421,15 +431,28 @@ __device__ __forceinline__ void load_group_lane(const DecodeArgs& a, uint32_t g,
         const BlockPrefix& bp = a.blk_prefix[L.m / kScanThreads];
         L.v_base = bp.v + L.d.v_pref;
         L.t_base = bp.t + L.d.t_pref;
-        L.tp_base = bp.tp + L.d.tp_pref;
         L.wp_base = bp.wp + L.d.wp_pref;
     } else {
         memset(&L.d, 0, sizeof(L.d));
-        L.v_base = L.t_base = L.tp_base = L.wp_base = 0ull;
+        L.v_base = L.t_base = L.wp_base = 0ull;
     }
     L.mi = (L.valid && a.meshlet_mesh) ? __ldg(a.meshlet_mesh + L.m) : 0u;
     L.P = a.meshes + L.mi;
     L.blob_off = L.valid ? L.P->blob_off : 0ull;
+}
+
+// The meshlet's output ranges lie inside its mesh's (header n_v_total, n_t)
+// and the mesh's last meshlet ends exactly there; checked before anything is
+// written, so a stream whose counts disagree with its header is rejected
+// instead of writing into a neighbour's output.
+__device__ __forceinline__ bool placement_ok(const DecodeArgs& a, const GroupLane& L) {
+    const uint32_t n_local = L.d.counts0 & 0xFFFFu;
+    const uint32_t n_tris = L.d.counts0 >> 16;
+    const unsigned long long vo = L.P->v_offset, to = L.P->t_offset, nv = L.P->n_v, nt = L.P->n_t;
+    bool ok = L.v_base >= vo && L.v_base + n_local <= vo + nv && L.t_base >= to && L.t_base + n_tris <= to + nt;
+    if (ok && L.m - L.P->meshlet_begin + 1u == L.P->n_meshlets)
+        ok = L.v_base + n_local == vo + nv && L.t_base + n_tris == to + nt;
+    return ok && L.wp_base + ((n_local + 3u) & ~3u) <= a.walk_cap;
 }
 
 template <bool kShared>
@@ -442,8 +465,11 @@ __device__ void conn_lane(const DecodeArgs& a, const GroupLane& L, bool act, con
     const uint32_t n_tris = L.d.counts0 >> 16;
     const uint32_t ib = max(1u, 32u - __clz(n_local));
     const uint32_t end = L.d.end_bit;
-    uint32_t* tri_out = a.tri_scratch + L.tp_base;
+    uint32_t* tri_out = a.idx + 3ull * L.t_base;
     uint32_t* walk_out = a.walk_scratch + L.wp_base;
+    // triangle indices are relative to the mesh's first vertex
+    const uint32_t vloc = act ? static_cast<uint32_t>(L.v_base - L.P->v_offset) : 0u;
+    const uint32_t s0 = static_cast<uint32_t>(L.t_base) & 3u;  // output quad slot of triangle 0
     uint32_t cpos = L.d.start_bit + 48u;
     uint32_t strips_left = L.d.n_strips;
     uint32_t tok_left = 0u, tok_idx = 0u, tris = 0u;
@@ -493,10 +519,14 @@ __device__ void conn_lane(const DecodeArgs& a, const GroupLane& L, bool act, con
             p0 = q0;
             p1 = q1;
             p2 = q2;
+            // triangle -> output quad; a quad that fills up is written out
             const bool emit = (body || tok_idx == 2u) && !invalid;
-            const uint32_t ts = tcnt & 3u;
+            const uint32_t ts = (s0 + tcnt) & 3u;
             if (emit) tq.put(ts, q0 | (q1 << 8) | (q2 << 16));
-            if (emit && ts == 3u) *reinterpret_cast<uint4*>(tri_out + tcnt - 3u) = make_uint4(tq.q0, tq.q1, tq.q2, tq.q3);
+            if (emit && ts == 3u) {
+                const int first = static_cast<int>(tcnt) - 3;
+                store_tris(tq, tri_out, first, first < 0 ? -first : 0, 4, vloc);
+            }
             tcnt += emit ? 1u : 0u;
             // first occurrence -> next walk entry (:523-541).  Roots are 'none'
             // (stored as v,v,v,v); strip bodies 'para' with (a, b, c) = (p0, p1, cref).
@@ -508,7 +538,8 @@ __device__ void conn_lane(const DecodeArgs& a, const GroupLane& L, bool act, con
             const uint32_t e = body ? (v | (q0 << 8) | (q1 << 16) | (cref << 24)) : v * 0x01010101u;
             const uint32_t ws = wcnt & 3u;
             if (isnew) wq.put(ws, e);
-            if (isnew && ws == 3u) *reinterpret_cast<uint4*>(walk_out + wcnt - 3u) = make_uint4(wq.q0, wq.q1, wq.q2, wq.q3);
+            if (isnew && ws == 3u)
+                *reinterpret_cast<uint4*>(walk_out + wcnt - 3u) = make_uint4(wq.q0, wq.q1, wq.q2, wq.q3);
             wcnt += isnew ? 1u : 0u;
             kind0 += (isnew && !body) ? 1u : 0u;
             tok_idx++;
@@ -518,7 +549,11 @@ __device__ void conn_lane(const DecodeArgs& a, const GroupLane& L, bool act, con
         }
     }
     if (act) {
-        quad_tail(tq, tcnt, tri_out);
+        const uint32_t r = (s0 + tcnt) & 3u;  // triangles in the open quad
+        if (r) {
+            const int first = static_cast<int>(tcnt) - static_cast<int>(r);
+            store_tris(tq, tri_out, first, first < 0 ? -first : 0, static_cast<int>(r), vloc);
+        }
         quad_tail(wq, wcnt, walk_out);
         if (bad || tris != n_tris) {
             report(a.status, kErrCorrupt, L.m);
@@ -553,13 +588,9 @@ __global__ void __launch_bounds__(W * 32) conn_kernel(DecodeArgs a, uint32_t sta
         GroupLane L;
         load_group_lane(a, g, lane, L);
         bool ok = L.valid;
-        if (ok) {
-            const unsigned long long tpc = L.tp_base + (((L.d.counts0 >> 16) + 3u) & ~3u);
-            const unsigned long long wpc = L.wp_base + (((L.d.counts0 & 0xFFFFu) + 3u) & ~3u);
-            if (tpc > a.tri_cap || wpc > a.walk_cap) {  // header totals disagree with the meshlets
-                report(a.status, kErrCorrupt, L.m);
-                ok = false;
-            }
+        if (ok && !placement_ok(a, L)) {
+            report(a.status, kErrCorrupt, L.m);
+            ok = false;
         }
         const unsigned long long start_b = L.blob_off + (L.d.start_bit >> 3);
         const unsigned long long end16 = (L.blob_off + ((L.d.end_bit + 7u) >> 3) + 15ull) & ~15ull;
@@ -584,7 +615,7 @@ __global__ void __launch_bounds__(W * 32) conn_kernel(DecodeArgs a, uint32_t sta
                 }
                 if (!mbar_wait(bar, phase)) {
                     if (lane == 0) report(a.status, kErrTimeout, L.m);
-                    mbar_wait(bar, phase);
+                    mbar_wait(bar, phase);  // let the copy land before the CTA exits
                     return;
                 }
                 phase ^= 1u;
@@ -605,42 +636,10 @@ __global__ void __launch_bounds__(W * 32) conn_kernel(DecodeArgs a, uint32_t sta
 // ---------------------------------------------------------------------------
 // 3. vertex kernel
 // ---------------------------------------------------------------------------
-// Integer codes of one meshlet, 8 bytes per vertex (x | y << 16, z) for codes
-// of up to 16 bits, 16 bytes (x, y, z, 0) above.
+// One axis of a meshlet's integer codes in shared memory: 16 bits per vertex
+// for codes of up to 16 bits, 32 above.
 template <bool kWide>
-struct Codes {
-    static constexpr uint32_t kBytes = kWide ? 16u : 8u;
-    __device__ static __forceinline__ void store(uint8_t* base, uint32_t v, int32_t x, int32_t y, int32_t z) {
-        if constexpr (kWide) {
-            reinterpret_cast<int4*>(base)[v] = make_int4(x, y, z, 0);
-        } else {
-            reinterpret_cast<uint2*>(base)[v] =
-                make_uint2(static_cast<uint32_t>(x) | (static_cast<uint32_t>(y) << 16), static_cast<uint32_t>(z));
-        }
-    }
-    __device__ static __forceinline__ void load(const uint8_t* base, uint32_t v, int32_t& x, int32_t& y,
-                                                int32_t& z) {
-        if constexpr (kWide) {
-            const int4 c = reinterpret_cast<const int4*>(base)[v];
-            x = c.x;
-            y = c.y;
-            z = c.z;
-        } else {
-            const uint2 c = reinterpret_cast<const uint2*>(base)[v];
-            x = static_cast<int32_t>(c.x & 0xFFFFu);
-            y = static_cast<int32_t>(c.x >> 16);
-            z = static_cast<int32_t>(c.y);
-        }
-    }
-    __device__ static __forceinline__ uint32_t component(const uint8_t* base, uint32_t v, uint32_t k) {
-        if constexpr (kWide) {
-            return reinterpret_cast<const uint32_t*>(base)[4u * v + k];
-        } else {
-            const uint32_t* p = reinterpret_cast<const uint32_t*>(base) + 2u * v;
-            return k == 2u ? p[1] : ((p[0] >> (16u * k)) & 0xFFFFu);
-        }
-    }
-};
+using PlaneT = typename std::conditional<kWide, int32_t, uint16_t>::type;
 
 __device__ __forceinline__ float dequant_value(const float* c, const MeshParams* P, uint32_t axis, uint32_t q) {
     if (__float_as_uint(c[6])) return c[5];
@@ -663,7 +662,8 @@ __device__ __noinline__ bool residual_slow(const uint32_t* w, uint32_t rbase, ui
 
 // Residual of one axis: Rice/EG codeword at `pos` with a straight-line fast
 // path (prefix and value inside one 32-bit window) and the general reader
-// out of line.  Returns false on a malformed codeword.
+// out of line.  Returns false on a malformed codeword; `pos` never passes
+// `limit`, so a corrupt stream cannot steer reads outside the meshlet.
 template <bool kShared>
 __device__ __forceinline__ bool residual(const uint32_t* w, uint32_t rbase, uint32_t& pos, uint32_t tk,
                                          uint32_t limit, int32_t& r) {
@@ -677,13 +677,13 @@ __device__ __forceinline__ bool residual(const uint32_t* w, uint32_t rbase, uint
     const uint32_t base = eg ? ((1u << (z & 31u)) - 1u) : z;
     uint32_t u = (base << k) + val;
     bool ok = true;
+    uint32_t np = pos + z + 1u + nb;
     if (z + 1u + nb > 32u) {  // long prefix or long value: rare
-        uint32_t p = pos;
-        ok = residual_slow<kShared>(w, rbase, &p, tk, limit, &u);
-        pos = p;
-    } else {
-        pos += z + 1u + nb;
+        np = pos;
+        ok = residual_slow<kShared>(w, rbase, &np, tk, limit, &u);
     }
+    ok = ok && np <= limit;
+    pos = min(np, limit);
     r = unzigzag(u);
     return ok;
 }
@@ -698,91 +698,102 @@ __device__ __forceinline__ bool skip_codes(const uint32_t* w, uint32_t rbase, ui
     for (uint32_t i = 0; i < n; i++) {
         const uint32_t x = peek32<kShared>(w, pos + rbase);
         const uint32_t z = __clz(x);
-        if (x != 0u) {
-            pos += z + 1u + (eg ? z : 0u) + k;
-        } else {
-            uint32_t p = pos, u;
-            ok = ok && residual_slow<kShared>(w, rbase, &p, tk, limit, &u);
-            pos = p;
+        uint32_t np = pos + z + 1u + (eg ? z : 0u) + k;
+        if (x == 0u) {
+            uint32_t u;
+            np = pos;
+            ok = ok && residual_slow<kShared>(w, rbase, &np, tk, limit, &u);
         }
+        ok = ok && np <= limit;
+        pos = min(np, limit);
     }
-    return ok && pos <= limit;
+    return ok;
 }
 
-// Decode the integer codes of the active lane's meshlet: anchor, the six
-// (tag, k) headers, then one pass over the walk with a cursor per residual
-// substream (paradelta_v5_dup.py:544-600).  The loop body is straight-line:
-// root and parallelogram vertices differ only in selects.
-template <bool kShared, bool kWide>
-__device__ void vert_lane(const DecodeArgs& a, const GroupLane& L, bool act, const uint32_t* w, uint32_t rbase,
-                          uint8_t* codes, uint32_t code_off, bool& bad) {
-    using C = Codes<kWide>;
-    if (!act) return;
-    const uint32_t n_local = L.d.counts0 & 0xFFFFu;
+// Per-lane state carried across the three axis passes of one meshlet.
+struct VertLane {
+    uint32_t tk[6];   // (tag, k) of dx dy dz px py pz: bit 7 Exp-Golomb, bits 0..5 k
+    int32_t anc[3];   // anchor codes
+    uint32_t cd[3];   // start of the dx, dy, dz substreams
+    uint32_t cp;      // parallelogram cursor: px, then py, then pz
+    bool bad;
+};
+
+// Anchor, the six (tag, k) pairs and the three delta substream starts
+// (paradelta_v5_dup.py:544-579).  The parallelogram substreams follow the
+// delta ones, so finding px means skipping dx, dy and dz.
+template <bool kShared>
+__device__ __forceinline__ void vert_setup(const GroupLane& L, const uint32_t* w, uint32_t rbase, VertLane& S) {
     const uint32_t n_kind0 = L.d.walk & 0xFFFFu;
-    const uint32_t n_walk = L.d.walk >> 16;
-    const uint32_t n_delta = n_kind0 ? n_kind0 - 1u : 0u;
-    const uint32_t n_para = n_walk - n_kind0;
+    const uint32_t n_delta = n_kind0 ? n_kind0 - 1u : 0u;  // the anchor has no delta
     const uint32_t end = L.d.end_bit;
-    uint8_t* my = codes + code_off;
-    {  // vertices the walk never reaches keep code 0
-        uint4* z = reinterpret_cast<uint4*>(my);
-        const uint32_t nz = (n_local * C::kBytes + 15u) >> 4;
-        for (uint32_t i = 0; i < nz; i++) z[i] = make_uint4(0u, 0u, 0u, 0u);
-    }
     const MeshParams* P = L.P;
     uint32_t pos = L.d.anchor_bit;
-    const uint32_t gb0 = P->g_bits[0], gb1 = P->g_bits[1], gb2 = P->g_bits[2];
-    const int32_t an0 = gb0 ? static_cast<int32_t>(peek32<kShared>(w, pos + rbase) >> (32u - gb0)) : 0;
-    pos += gb0;
-    const int32_t an1 = gb1 ? static_cast<int32_t>(peek32<kShared>(w, pos + rbase) >> (32u - gb1)) : 0;
-    pos += gb1;
-    const int32_t an2 = gb2 ? static_cast<int32_t>(peek32<kShared>(w, pos + rbase) >> (32u - gb2)) : 0;
-    pos += gb2;
-    uint32_t tk[6];
+    S.bad = false;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        const uint32_t gb = P->g_bits[d];
+        S.anc[d] = gb ? static_cast<int32_t>(peek32<kShared>(w, pos + rbase) >> (32u - gb)) : 0;
+        pos += gb;
+    }
 #pragma unroll
     for (int i = 0; i < 6; i++) {
         const uint32_t t = peek32<kShared>(w, pos + rbase) >> 16;
         pos += 16u;
         const uint32_t k = t & 0xFFu;
-        if (k > static_cast<uint32_t>(kMaxResidK)) bad = true;
-        tk[i] = ((t >> 8) == 1u ? 0u : 0x80u) | (k & 0x3Fu);
+        if (k > static_cast<uint32_t>(kMaxResidK)) S.bad = true;
+        S.tk[i] = ((t >> 8) == 1u ? 0u : 0x80u) | (k & 0x3Fu);
     }
-    if (bad) return;
-    // substream starts: dx dy dz px py pz follow each other
-    uint32_t cdx = pos, cdy, cdz, cpx, cpy, cpz;
-    bool ok = skip_codes<kShared>(w, rbase, pos, tk[0], n_delta, end);
-    cdy = pos;
-    ok = skip_codes<kShared>(w, rbase, pos, tk[1], n_delta, end) && ok;
-    cdz = pos;
-    ok = skip_codes<kShared>(w, rbase, pos, tk[2], n_delta, end) && ok;
-    cpx = pos;
-    ok = skip_codes<kShared>(w, rbase, pos, tk[3], n_para, end) && ok;
-    cpy = pos;
-    ok = skip_codes<kShared>(w, rbase, pos, tk[4], n_para, end) && ok;
-    cpz = pos;
-    if (!ok) {
-        bad = true;
-        return;
+    if (pos > end) S.bad = true;
+    pos = min(pos, end);
+    bool ok = !S.bad;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        S.cd[d] = pos;
+        if (ok) ok = skip_codes<kShared>(w, rbase, pos, S.tk[d], n_delta, end);
     }
-    const int32_t nx0 = P->pred_n[0], nx1 = P->pred_n[1], nx2 = P->pred_n[2];
-    const int32_t ny0 = P->pred_n[3], ny1 = P->pred_n[4], ny2 = P->pred_n[5];
-    const int32_t nz0 = P->pred_n[6], nz1 = P->pred_n[7], nz2 = P->pred_n[8];
-    const int32_t kx = P->pred_k[0], ky = P->pred_k[1], kz = P->pred_k[2];
-    const int32_t hx = P->pred_half[0], hy = P->pred_half[1], hz = P->pred_half[2];
-    const uint32_t mx = P->code_max[0], mmy = P->code_max[1], mz = P->code_max[2];
-    const uint32_t tdx = tk[0], tdy = tk[1], tdz = tk[2], tpx = tk[3], tpy = tk[4], tpz = tk[5];
-    const uint32_t* walk = a.walk_scratch + L.wp_base;
-    uint4 qn = __ldcg(reinterpret_cast<const uint4*>(walk));
-    uint4 q = qn;
-    int32_t px = 0, py = 0, pz = 0;
+    S.cp = pos;
+    S.bad = !ok;
+}
+
+// Integer codes of axis d in walk order (IRLP, paradelta_v5_dup.py:91-104
+// and 581-600).  Every walk vertex is a root (delta from the previous walk
+// vertex, or the anchor for the first) or a parallelogram vertex predicted
+// from three earlier ones; the loop body is straight-line with selects.
+template <bool kShared, bool kWide>
+__device__ __forceinline__ void vert_axis(const DecodeArgs& a, const GroupLane& L, uint32_t d, const uint32_t* w,
+                                          uint32_t rbase, PlaneT<kWide>* plane, VertLane& S) {
+    const uint32_t n_local = L.d.counts0 & 0xFFFFu;
+    const uint32_t n_walk = L.d.walk >> 16;
+    const uint32_t end = L.d.end_bit;
+    const MeshParams* P = L.P;
+    if (n_walk < n_local) {  // vertices the walk never reaches keep code 0
+        uint4* z = reinterpret_cast<uint4*>(plane);
+        const uint32_t nz = (n_local * static_cast<uint32_t>(sizeof(PlaneT<kWide>)) + 15u) >> 4;
+        for (uint32_t i = 0; i < nz; i++) z[i] = make_uint4(0u, 0u, 0u, 0u);
+    }
+    const int32_t n0 = P->pred_n[3 * d], n1 = P->pred_n[3 * d + 1], n2 = P->pred_n[3 * d + 2];
+    const int32_t K = P->pred_k[d], half = P->pred_half[d];
+    const uint32_t cmax = P->code_max[d];
+    const uint32_t td = S.tk[d], tp = S.tk[3 + d];
+    const int32_t anc = S.anc[d];
+    uint32_t cdd = S.cd[d], cp = S.cp;
+    // walk entries (v | a << 8 | b << 16 | c << 24), two quads in flight
+    const uint4* wq = reinterpret_cast<const uint4*>(a.walk_scratch + L.wp_base);
+    const uint32_t nq = (n_walk + 3u) >> 2;
+    uint4 qa = nq > 0u ? __ldcg(wq) : make_uint4(0u, 0u, 0u, 0u);
+    uint4 qb = nq > 1u ? __ldcg(wq + 1) : qa;
+    uint4 q = qa;
+    int32_t prev = 0;
     bool first = true;
     bool fail = false;
     for (uint32_t i = 0; i < n_walk; i++) {
         const uint32_t s = i & 3u;
         if (s == 0u) {
-            q = qn;
-            if (i + 4u < n_walk) qn = __ldcg(reinterpret_cast<const uint4*>(walk + i + 4u));
+            q = qa;
+            qa = qb;
+            const uint32_t nx = (i >> 2) + 2u;
+            if (nx < nq) qb = __ldcg(wq + nx);
         }
         const uint32_t e = s == 0u ? q.x : (s == 1u ? q.y : (s == 2u ? q.z : q.w));
         const uint32_t v = e & 0xFFu;
@@ -790,114 +801,83 @@ __device__ void vert_lane(const DecodeArgs& a, const GroupLane& L, bool act, con
         const bool para = ra != v;
         const bool anchor = first && !para;  // the first walk vertex is the anchor
         first = first && para;
-        // IRLP over (a, b, c) (:91-104); for root entries the references
-        // are the vertex itself and the result is discarded
-        int32_t ax, ay, az, bx, by, bz, ccx, ccy, ccz;
-        C::load(my, ra, ax, ay, az);
-        C::load(my, rb, bx, by, bz);
-        C::load(my, rc, ccx, ccy, ccz);
-        const int32_t qx = para ? (nx0 * ax + nx1 * bx + nx2 * ccx + hx) >> kx : px;
-        const int32_t qy = para ? (ny0 * ay + ny1 * by + ny2 * ccy + hy) >> ky : py;
-        const int32_t qz = para ? (nz0 * az + nz1 * bz + nz2 * ccz + hz) >> kz : pz;
-        uint32_t p0 = para ? cpx : cdx, p1 = para ? cpy : cdy, p2 = para ? cpz : cdz;
-        int32_t rx, ry, rz;
-        bool okr = residual<kShared>(w, rbase, p0, para ? tpx : tdx, end, rx);
-        okr = residual<kShared>(w, rbase, p1, para ? tpy : tdy, end, ry) && okr;
-        okr = residual<kShared>(w, rbase, p2, para ? tpz : tdz, end, rz) && okr;
-        cpx = para ? p0 : cpx;
-        cpy = para ? p1 : cpy;
-        cpz = para ? p2 : cpz;
-        const bool dcommit = !para && !anchor;
-        cdx = dcommit ? p0 : cdx;
-        cdy = dcommit ? p1 : cdy;
-        cdz = dcommit ? p2 : cdz;
-        const int32_t cx = anchor ? an0 : qx + rx;
-        const int32_t cy = anchor ? an1 : qy + ry;
-        const int32_t cz = anchor ? an2 : qz + rz;
+        // for root entries the references are the vertex itself and the
+        // prediction is discarded
+        const int32_t ca = static_cast<int32_t>(plane[ra]);
+        const int32_t cb = static_cast<int32_t>(plane[rb]);
+        const int32_t cc = static_cast<int32_t>(plane[rc]);
+        const int32_t pred = para ? (n0 * ca + n1 * cb + n2 * cc + half) >> K : prev;
+        uint32_t p = para ? cp : cdd;
+        int32_t r;
+        const bool okr = residual<kShared>(w, rbase, p, para ? tp : td, end, r);
+        cp = para ? p : cp;
+        cdd = (!para && !anchor) ? p : cdd;
+        const int32_t code = anchor ? anc : pred + r;
         // codes of a valid stream lie in [0, 2^g_bits)
-        fail = fail || !(okr || anchor) || static_cast<uint32_t>(cx) > mx || static_cast<uint32_t>(cy) > mmy ||
-               static_cast<uint32_t>(cz) > mz;
-        C::store(my, v, cx, cy, cz);
-        px = cx;
-        py = cy;
-        pz = cz;
+        fail = fail || !(okr || anchor) || static_cast<uint32_t>(code) > cmax;
+        plane[v] = static_cast<PlaneT<kWide>>(code);
+        prev = code;
     }
-    bad = bad || fail;
-    // the last substream must end where the next meshlet starts (:507)
-    if (!bad) {
-        const bool last_of_mesh = L.m - P->meshlet_begin + 1u == P->n_meshlets;
-        if (last_of_mesh ? cpz > end : cpz != end) bad = true;
-    }
+    S.cp = cp;
+    S.bad = S.bad || fail;
 }
 
+// Axis d of every vertex of the round's meshlets -> positions (and codes),
+// the warp working through one meshlet at a time.
 template <bool kWide>
-__device__ void emit_round(const DecodeArgs& a, const GroupLane& L, uint32_t rmask, const uint8_t* codes,
-                           uint32_t code_off, float* dqc, int lane) {
-    using C = Codes<kWide>;
-    const uint32_t vloc = static_cast<uint32_t>(L.v_base - (L.valid ? L.P->v_offset : 0ull));
+__device__ void emit_axis(const DecodeArgs& a, const GroupLane& L, uint32_t rmask, const uint8_t* planes,
+                          uint32_t code_off, uint32_t d, float* dqc, int lane) {
     uint32_t cached = 0xFFFFFFFFu;
-    for (int j = 0; j < 32; j++) {
-        if (!((rmask >> j) & 1u)) continue;
-        const uint32_t c0 = __shfl_sync(kFull, L.d.counts0, j);
-        const uint32_t nv = c0 & 0xFFFFu, nt = c0 >> 16;
+    for (uint32_t mm = rmask; mm; mm &= mm - 1u) {
+        const int j = __ffs(mm) - 1;
+        const uint32_t nv = __shfl_sync(kFull, L.d.counts0, j) & 0xFFFFu;
         const unsigned long long vb = shfl64(L.v_base, j);
-        const unsigned long long tb = shfl64(L.t_base, j);
-        const unsigned long long tpb = shfl64(L.tp_base, j);
-        const uint32_t vl = __shfl_sync(kFull, vloc, j);
         const uint32_t off = __shfl_sync(kFull, code_off, j);
         const uint32_t mj = __shfl_sync(kFull, L.mi, j);
         const MeshParams* Pj = a.meshes + mj;
-        // triangles: packed local ids -> global ids
-        const uint32_t* tsrc = a.tri_scratch + tpb;
-        warp_store_words(
-            a.idx + 3ull * tb, 3u * nt,
-            [&](uint32_t i) {
-                const uint32_t t = i / 3u;
-                const uint32_t k = i - 3u * t;
-                return vl + ((__ldcg(tsrc + t) >> (8u * k)) & 0xFFu);
-            },
-            lane);
         if (mj != cached) {
             __syncwarp();
-            if (lane < 24) {
-                const uint32_t ax = lane >> 3, f = lane & 7u;
-                const stride_dequant_axis& dq = Pj->dq[ax];
-                float val;
-                switch (f) {
-                    case 0: val = dq.a_hi; break;
-                    case 1: val = dq.a_lo; break;
-                    case 2: val = dq.b_hi; break;
-                    case 3: val = dq.b_lo; break;
-                    case 4: val = dq.err; break;
-                    case 5: val = dq.konst; break;
-                    case 6: val = __uint_as_float(static_cast<uint32_t>(dq.zero_bits)); break;
-                    default: val = 0.f; break;
-                }
-                dqc[lane] = val;
-            }
+            if (lane < 8) dqc[lane] = reinterpret_cast<const float*>(&Pj->dq[d])[lane];
             __syncwarp();
             cached = mj;
         }
-        const uint8_t* cj = codes + off;
-        warp_store_words(
-            reinterpret_cast<uint32_t*>(a.pos + 3ull * vb), 3u * nv,
-            [&](uint32_t i) {
-                const uint32_t vv = i / 3u;
-                const uint32_t k = i - 3u * vv;
-                return __float_as_uint(dequant_value(dqc + 8u * k, Pj, k, C::component(cj, vv, k)));
-            },
-            lane);
+        const PlaneT<kWide>* pj = reinterpret_cast<const PlaneT<kWide>*>(planes + off);
+        float* dst = a.pos + 3ull * vb + d;
+        for (uint32_t v = lane; v < nv; v += 32u) {
+            const uint32_t q = static_cast<uint32_t>(pj[v]);
+            dst[3u * v] = dequant_value(dqc, Pj, d, q);
+        }
         if (a.codes) {
-            warp_store_words(
-                reinterpret_cast<uint32_t*>(a.codes + 3ull * vb), 3u * nv,
-                [&](uint32_t i) {
-                    const uint32_t vv = i / 3u;
-                    return C::component(cj, vv, i - 3u * vv);
-                },
-                lane);
+            int32_t* cdst = a.codes + 3ull * vb + d;
+            for (uint32_t v = lane; v < nv; v += 32u) cdst[3u * v] = static_cast<int32_t>(pj[v]);
         }
     }
     __syncwarp();
+}
+
+// One round: the active lanes decode their meshlets axis by axis, and after
+// each axis the warp writes that coordinate out of the shared code planes.
+template <bool kShared, bool kWide>
+__device__ __forceinline__ void vert_round(const DecodeArgs& a, const GroupLane& L, bool act, uint32_t rmask,
+                                           const uint32_t* w, uint32_t rbase, uint8_t* planes, uint32_t code_off,
+                                           float* dqc, int lane) {
+    VertLane S;
+    S.bad = false;
+    S.cp = 0u;
+    if (act) vert_setup<kShared>(L, w, rbase, S);
+    PlaneT<kWide>* plane = reinterpret_cast<PlaneT<kWide>*>(planes + code_off);
+    for (uint32_t d = 0; d < 3u; d++) {
+        if (act && !S.bad) vert_axis<kShared, kWide>(a, L, d, w, rbase, plane, S);
+        __syncwarp();
+        emit_axis<kWide>(a, L, rmask, planes, code_off, d, dqc, lane);
+    }
+    if (act) {
+        // the last substream must end where the next meshlet starts (:507)
+        const MeshParams* P = L.P;
+        const bool last_of_mesh = L.m - P->meshlet_begin + 1u == P->n_meshlets;
+        if (!S.bad && (last_of_mesh ? S.cp > L.d.end_bit : S.cp != L.d.end_bit)) S.bad = true;
+        if (S.bad) report(a.status, kErrCorrupt, L.m);
+    }
 }
 
 template <int W, bool kWide>
@@ -910,9 +890,9 @@ __global__ void __launch_bounds__(W * 32) vert_kernel(DecodeArgs a, uint32_t sta
     const uint32_t vstage = vert_stage_bytes(stage_bytes);
     uint8_t* base = smem + warp * vert_warp_bytes(stage_bytes, code_bytes);
     uint32_t* stage = reinterpret_cast<uint32_t*>(base);
-    uint8_t* codes = base + align16(vstage + 32u);
-    float* dqc = reinterpret_cast<float*>(codes + align16(code_bytes));
-    uint64_t* bar = reinterpret_cast<uint64_t*>(dqc + 24);
+    uint8_t* planes = base + align16(vstage + 32u);
+    float* dqc = reinterpret_cast<float*>(planes + align16(code_bytes));
+    uint64_t* bar = reinterpret_cast<uint64_t*>(dqc + 8);
     if (lane == 0) mbar_init(bar);
     __syncwarp();
     uint32_t phase = 0u;
@@ -927,20 +907,16 @@ __global__ void __launch_bounds__(W * 32) vert_kernel(DecodeArgs a, uint32_t sta
         GroupLane L;
         load_group_lane(a, g, lane, L);
         const uint32_t n_local = L.d.counts0 & 0xFFFFu;
-        const uint32_t n_tris = L.d.counts0 >> 16;
         bool ok = L.valid;
-        if (ok) {
-            const unsigned long long vo = L.P->v_offset, to = L.P->t_offset, nv = L.P->n_v, nt = L.P->n_t;
-            ok = L.v_base >= vo && L.v_base + n_local <= vo + nv && L.t_base >= to && L.t_base + n_tris <= to + nt;
-            if (ok && L.m - L.P->meshlet_begin + 1u == L.P->n_meshlets)
-                ok = L.v_base + n_local == vo + nv && L.t_base + n_tris == to + nt;
-            if (!ok) report(a.status, kErrCorrupt, L.m);
+        if (ok && !placement_ok(a, L)) {
+            report(a.status, kErrCorrupt, L.m);
+            ok = false;
         }
         // this lane's residual bits: anchor .. end, 16-byte aligned
         const unsigned long long src16 = (L.blob_off + (L.d.anchor_bit >> 3)) & ~15ull;
         const unsigned long long end16 = (L.blob_off + ((L.d.end_bit + 7u) >> 3) + 15ull) & ~15ull;
         const uint32_t ssz = ok ? static_cast<uint32_t>(end16 - src16) : 0u;
-        const uint32_t csz = (n_local * Codes<kWide>::kBytes + 15u) & ~15u;
+        const uint32_t csz = align16(n_local * static_cast<uint32_t>(sizeof(PlaneT<kWide>)));
         uint32_t todo = __ballot_sync(kFull, ok);
         while (todo) {
             const int first = __ffs(todo) - 1;
@@ -965,7 +941,6 @@ __global__ void __launch_bounds__(W * 32) vert_kernel(DecodeArgs a, uint32_t sta
             todo &= ~rmask;
             const bool act = (rmask >> lane) & 1u;
             const uint32_t code_off = act ? cc - csz : 0u;
-            bool bad = false;
             if (staged) {
                 const int last = 31 - __clz(rmask);
                 const uint32_t total = __shfl_sync(kFull, cs, last);
@@ -976,19 +951,17 @@ __global__ void __launch_bounds__(W * 32) vert_kernel(DecodeArgs a, uint32_t sta
                 if (act && ssz) bulk_copy(reinterpret_cast<uint8_t*>(stage) + dst_off, a.arena + src16, ssz, bar);
                 if (!mbar_wait(bar, phase)) {
                     if (lane == 0) report(a.status, kErrTimeout, L.m);
-                    mbar_wait(bar, phase);
+                    mbar_wait(bar, phase);  // let the copies land before the CTA exits
                     return;
                 }
                 phase ^= 1u;
                 const uint32_t rbase = static_cast<uint32_t>(L.blob_off * 8ull - src16 * 8ull + dst_off * 8ull);
-                vert_lane<true, kWide>(a, L, act, stage, rbase, codes, code_off, bad);
+                vert_round<true, kWide>(a, L, act, rmask, stage, rbase, planes, code_off, dqc, lane);
             } else {
-                vert_lane<false, kWide>(a, L, act, reinterpret_cast<const uint32_t*>(a.arena + L.blob_off), 0u,
-                                        codes, code_off, bad);
+                vert_round<false, kWide>(a, L, act, rmask, reinterpret_cast<const uint32_t*>(a.arena + L.blob_off),
+                                         0u, planes, code_off, dqc, lane);
             }
-            if (act && bad) report(a.status, kErrCorrupt, L.m);
             __syncwarp();
-            emit_round<kWide>(a, L, rmask, codes, code_off, dqc, lane);
         }
         if (!persistent) break;
         uint32_t t = 0u;
@@ -1014,15 +987,32 @@ cudaError_t opt_in_smem(K kernel, size_t smem, size_t* configured) {
     return cudaSuccess;
 }
 
+// Resident CTAs per SM of one kernel instantiation, cached per device and
+// shared-memory size (the occupancy query costs microseconds per launch).
+struct OccCache {
+    size_t smem[64] = {0};
+    int per_sm[64] = {0};
+};
+
 template <class K>
-uint32_t grid_for(K kernel, int threads, size_t smem, const LaunchCfg& cfg, uint32_t n_groups, int W) {
+uint32_t grid_for(K kernel, int threads, size_t smem, const LaunchCfg& cfg, uint32_t n_groups, int W,
+                  OccCache& cache) {
     uint32_t grid = (n_groups + W - 1) / W;
     if (cfg.persistent) {
         int per_sm = cfg.ctas_per_sm;
         if (per_sm <= 0) {
-            per_sm = 1;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
-            if (per_sm < 1) per_sm = 1;
+            int dev = 0;
+            cudaGetDevice(&dev);
+            dev = dev < 0 || dev >= 64 ? 0 : dev;
+            if (cache.per_sm[dev] > 0 && cache.smem[dev] == smem) {
+                per_sm = cache.per_sm[dev];
+            } else {
+                per_sm = 1;
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
+                if (per_sm < 1) per_sm = 1;
+                cache.per_sm[dev] = per_sm;
+                cache.smem[dev] = smem;
+            }
         }
         const uint32_t cap = static_cast<uint32_t>(per_sm * device_sm_count());
         if (grid > cap) grid = cap;
@@ -1033,11 +1023,12 @@ uint32_t grid_for(K kernel, int threads, size_t smem, const LaunchCfg& cfg, uint
 template <int W>
 cudaError_t launch_conn(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s) {
     static size_t configured[64] = {0};
+    static OccCache occ;
     const size_t smem = static_cast<size_t>(W) * conn_warp_bytes(cfg.stage_bytes);
     cudaError_t e = opt_in_smem(conn_kernel<W>, smem, configured);
     if (e != cudaSuccess) return e;
     const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
-    const uint32_t grid = grid_for(conn_kernel<W>, W * 32, smem, cfg, n_groups, W);
+    const uint32_t grid = grid_for(conn_kernel<W>, W * 32, smem, cfg, n_groups, W, occ);
     if (grid == 0) return cudaSuccess;
     conn_kernel<W><<<grid, W * 32, smem, s>>>(a, cfg.stage_bytes, cfg.persistent);
     return cudaGetLastError();
@@ -1046,11 +1037,12 @@ cudaError_t launch_conn(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t 
 template <int W, bool kWide>
 cudaError_t launch_vert(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s) {
     static size_t configured[64] = {0};
+    static OccCache occ;
     const size_t smem = static_cast<size_t>(W) * vert_warp_bytes(cfg.stage_bytes, cfg.code_bytes);
     cudaError_t e = opt_in_smem(vert_kernel<W, kWide>, smem, configured);
     if (e != cudaSuccess) return e;
     const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
-    const uint32_t grid = grid_for(vert_kernel<W, kWide>, W * 32, smem, cfg, n_groups, W);
+    const uint32_t grid = grid_for(vert_kernel<W, kWide>, W * 32, smem, cfg, n_groups, W, occ);
     if (grid == 0) return cudaSuccess;
     vert_kernel<W, kWide><<<grid, W * 32, smem, s>>>(a, cfg.stage_bytes, cfg.code_bytes, cfg.persistent);
     return cudaGetLastError();
@@ -1089,7 +1081,7 @@ int device_sm_count() {
 
 int check_config(const LaunchCfg& cfg, bool wide) {
     if (cfg.warps_per_cta != 1 && cfg.warps_per_cta != 2 && cfg.warps_per_cta != 4) return STRIDE_ERR_ARG;
-    if (cfg.code_bytes < kMaxLocal * (wide ? 16u : 8u) || cfg.stage_bytes < 256u) return STRIDE_ERR_ARG;
+    if (cfg.code_bytes < kMaxLocal * (wide ? 4u : 2u) || cfg.stage_bytes < 256u) return STRIDE_ERR_ARG;
     if (conn_smem_bytes(cfg) > 227u * 1024u || vert_smem_bytes(cfg) > 227u * 1024u) return STRIDE_ERR_ARG;
     return STRIDE_OK;
 }

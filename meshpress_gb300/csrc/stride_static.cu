@@ -58,7 +58,7 @@ int static_scratch(uint8_t** out) {
 size_t up256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
 
 struct StaticLayout {
-    size_t blob, params, descs, sums, prefix, tri, walk, status, total;
+    size_t blob, params, descs, sums, prefix, walk, status, total;
 };
 
 StaticLayout plan(size_t len, const MeshParams& p) {
@@ -74,8 +74,6 @@ StaticLayout plan(size_t len, const MeshParams& p) {
     o += up256(sizeof(uint4) * scan_blocks(p.n_meshlets));
     L.prefix = o;
     o += up256(sizeof(BlockPrefix) * scan_blocks(p.n_meshlets));
-    L.tri = o;
-    o += up256(4ull * tri_scratch_words(p.n_t, p.n_meshlets));
     L.walk = o;
     o += up256(4ull * walk_scratch_words(p.n_v, p.n_meshlets));
     L.status = o;
@@ -94,13 +92,15 @@ extern "C" int stride_decode_static(const uint8_t* data, size_t len, void* strea
     char why[256] = {0};
     int rc = parse_header(data, len, &p, why, sizeof(why));
     if (rc) return fail(rc, "%s", why);
-    if ((!d_idx && p.n_t) || (!d_pos && p.n_v)) return fail(STRIDE_ERR_ARG, "null output pointer");
     const StaticLayout L = plan(len, p);
     if (L.total > kStaticScratchBytes)
         return fail(STRIDE_ERR_NOMEM,
                     "stream needs %zu bytes of decode scratch; the allocation-free entry point has a fixed "
-                    "%zu-byte scratch (roughly 5 million triangles); use stride_open/stride_decode instead",
+                    "%zu-byte scratch (about 10 million triangles of a typical mesh); use stride_open/stride_decode instead",
                     L.total, kStaticScratchBytes);
+    if ((!d_idx && p.n_t) || (!d_pos && p.n_v)) return fail(STRIDE_ERR_ARG, "null output pointer");
+    if ((reinterpret_cast<uintptr_t>(d_idx) & 15u) || (reinterpret_cast<uintptr_t>(d_pos) & 3u))
+        return fail(STRIDE_ERR_ARG, "index output must be 16-byte aligned, positions 4-byte aligned");
     uint8_t* base = nullptr;
     if ((rc = static_scratch(&base)) != STRIDE_OK) return rc;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -120,9 +120,7 @@ extern "C" int stride_decode_static(const uint8_t* data, size_t len, void* strea
     a.descs = reinterpret_cast<MeshletDesc*>(base + L.descs);
     a.blk_sums = reinterpret_cast<uint4*>(base + L.sums);
     a.blk_prefix = reinterpret_cast<BlockPrefix*>(base + L.prefix);
-    a.tri_scratch = reinterpret_cast<uint32_t*>(base + L.tri);
     a.walk_scratch = reinterpret_cast<uint32_t*>(base + L.walk);
-    a.tri_cap = tri_scratch_words(p.n_t, p.n_meshlets);
     a.walk_cap = walk_scratch_words(p.n_v, p.n_meshlets);
     a.status = reinterpret_cast<Status*>(base + L.status);  // zeroed by enqueue_decode
     a.idx = d_idx;
@@ -130,7 +128,7 @@ extern "C" int stride_decode_static(const uint8_t* data, size_t len, void* strea
     a.codes = nullptr;
     a.wide_codes = p.g_bits[0] > 16 || p.g_bits[1] > 16 || p.g_bits[2] > 16;
     LaunchCfg cfg;
-    if (a.wide_codes) cfg.code_bytes = kMaxLocal * 16u > cfg.code_bytes ? kMaxLocal * 16u : cfg.code_bytes;
+    if (a.wide_codes) cfg.code_bytes = kMaxLocal * 4u > cfg.code_bytes ? kMaxLocal * 4u : cfg.code_bytes;
     rc = enqueue_decode(a, cfg, stream);
     if (rc) return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_fail(e, "stride_decode_static");

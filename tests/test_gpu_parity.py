@@ -116,13 +116,22 @@ def _cfg(w, pers, stage, code, per_sm=0):
 
 
 @pytest.mark.parametrize("cfg", [
-    (1, 0, 20 * 1024, 40 * 1024), (2, 0, 16 * 1024, 32 * 1024), (4, 1, 12 * 1024, 24 * 1024),
+    (1, 0, 20 * 1024, 16 * 1024), (2, 0, 16 * 1024, 8 * 1024), (4, 1, 12 * 1024, 6 * 1024),
     (1, 1, 256, 2048),           # tiny stage: meshlets fall back to global reads
-    (2, 0, 64 * 1024, 2048),     # tiny code store: one meshlet per round
+    (2, 0, 64 * 1024, 512),      # code plane of one 256-vertex meshlet: one meshlet per round
 ], ids=["w1", "w2", "w4p", "global_reads", "one_per_round"])
 def test_launch_shapes_give_identical_output(torch_cuda, cfg):
     V, T = synth.icosphere(5, seed=11)
     e = encoder.encode(V, T, precision_error=B12, precision_mode="bbox_frac")
+    pos, idx, codes = gpu_decode(torch_cuda, e.data, cfg=_cfg(*cfg))
+    assert_same_as_oracle(e.data, pos, idx, codes)
+
+
+@pytest.mark.parametrize("cfg", [(2, 1, 16 * 1024, 1024), (1, 0, 256, 32 * 1024)], ids=["one_per_round", "global_reads"])
+def test_wide_codes_launch_shapes(torch_cuda, cfg):
+    """20-bit codes (32-bit code plane) under the smallest plane and stage."""
+    V, T = synth.heightfield_grid(129, seed=6)
+    e = encoder.encode(V, T, precision_error=synth.bbox_bits_error(20), precision_mode="bbox_frac")
     pos, idx, codes = gpu_decode(torch_cuda, e.data, cfg=_cfg(*cfg))
     assert_same_as_oracle(e.data, pos, idx, codes)
 

@@ -74,7 +74,7 @@ def test_static_entry_matches_allocating_entry(torch_cuda):
 def test_static_entry_rejects_streams_beyond_its_scratch(torch_cuda):
     V, T = synth.heightfield_grid(33, seed=23)
     data = bytearray(encoder.encode(V, T, precision_error=B12, precision_mode="bbox_frac").data)
-    data[78:82] = (60_000_000).to_bytes(4, "big")  # header claims 60 M triangles
+    data[74:78] = (60_000_000).to_bytes(4, "big")  # header claims 60 M vertices (walk scratch > 64 MiB)
     lib = _lib.load()
     rc = lib.stride_decode_static(bytes(data), len(data), None, ctypes.c_void_p(1), ctypes.c_void_p(1))
     assert rc == _lib.STRIDE_ERR_NOMEM
