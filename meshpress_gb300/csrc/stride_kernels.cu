@@ -342,54 +342,16 @@ struct Fifo {
     }
 };
 
-// 4-entry register buffer: four triangles (one 48-byte, 16-byte aligned
-// output quad) or four walk entries.
-struct Quad {
-    uint32_t q0 = 0, q1 = 0, q2 = 0, q3 = 0;
-    __device__ __forceinline__ void put(uint32_t slot, uint32_t v) {
-        q0 = slot == 0u ? v : q0;
-        q1 = slot == 1u ? v : q1;
-        q2 = slot == 2u ? v : q2;
-        q3 = slot == 3u ? v : q3;
-    }
-    __device__ __forceinline__ uint32_t get(uint32_t slot) const {
-        return slot == 0u ? q0 : (slot == 1u ? q1 : (slot == 2u ? q2 : q3));
-    }
-};
-
-__device__ __forceinline__ void quad_tail(const Quad& q, uint32_t cnt, uint32_t* base) {
-    // the (cnt & 3) entries after the last full quad
-    const uint32_t r = cnt & 3u;
-    uint32_t* p = base + (cnt - r);
-    if (r > 0u) p[0] = q.q0;
-    if (r > 1u) p[1] = q.q1;
-    if (r > 2u) p[2] = q.q2;
-}
-
-// Writes the triangles held in slots [lo, hi) of q as global vertex ids.
-// Slot s is the meshlet's triangle `first + s`, and the quad's first
-// triangle sits at a multiple of four in the output, so a full quad is
-// three aligned 16-byte stores; slots before the meshlet's first triangle
-// (lo > 0) or past its last (hi < 4) go out as single words.
-__device__ __forceinline__ void store_tris(const Quad& q, uint32_t* out, int first, int lo, int hi, uint32_t vloc) {
-    auto id = [vloc](uint32_t packed, uint32_t k) { return vloc + ((packed >> (8u * k)) & 0xFFu); };
-    if (lo == 0 && hi == 4) {
-        uint4* o = reinterpret_cast<uint4*>(out + 3ll * first);
-        o[0] = make_uint4(id(q.q0, 0), id(q.q0, 1), id(q.q0, 2), id(q.q1, 0));
-        o[1] = make_uint4(id(q.q1, 1), id(q.q1, 2), id(q.q2, 0), id(q.q2, 1));
-        o[2] = make_uint4(id(q.q2, 2), id(q.q3, 0), id(q.q3, 1), id(q.q3, 2));
-    } else {
-#pragma unroll
-        for (int s = 0; s < 4; s++) {
-            if (s >= lo && s < hi) {
-                const uint32_t p = q.get(static_cast<uint32_t>(s));
-                uint32_t* o = out + 3ll * (first + s);
-                o[0] = id(p, 0);
-                o[1] = id(p, 1);
-                o[2] = id(p, 2);
-            }
-        }
-    }
+// One triangle (three global vertex ids, 12 bytes) at triangle index t of a
+// 16-byte aligned index array: one 8-byte store on an 8-byte boundary and one
+// 4-byte store, chosen by the parity of t without a branch.
+__device__ __forceinline__ void store_tri(uint32_t* tri_out, uint32_t local, bool odd, uint32_t a, uint32_t b,
+                                          uint32_t c) {
+    uint32_t* p = tri_out + 3u * local;
+    uint2* p8 = reinterpret_cast<uint2*>(p + (odd ? 1u : 0u));
+    uint32_t* p4 = p + (odd ? 0u : 2u);
+    *p8 = odd ? make_uint2(b, c) : make_uint2(a, b);
+    *p4 = odd ? a : c;
 }
 
 // ---------------------------------------------------------------------------
@@ -403,9 +365,12 @@ __host__ __device__ inline uint32_t conn_warp_bytes(uint32_t stage_bytes) {
 
 __host__ __device__ inline uint32_t vert_stage_bytes(uint32_t stage_bytes) { return stage_bytes / 2u; }
 
-// residual stage | code plane | dequantisation constants (8 words) | mbarrier
-__host__ __device__ inline uint32_t vert_warp_bytes(uint32_t stage_bytes, uint32_t code_bytes) {
-    return align16(vert_stage_bytes(stage_bytes) + 32u) + align16(code_bytes) + 32u + 16u;
+// One axis warp's code plane and dequantisation constants (8 words).
+__host__ __device__ inline uint32_t vert_axis_bytes(uint32_t code_bytes) { return align16(code_bytes) + 32u; }
+
+// Vertex CTA: residual stage | three axis regions | mbarrier.
+__host__ __device__ inline uint32_t vert_cta_bytes(uint32_t stage_bytes, uint32_t code_bytes) {
+    return align16(vert_stage_bytes(stage_bytes) + 32u) + 3u * vert_axis_bytes(code_bytes) + 16u;
 }
 
 struct GroupLane {
@@ -469,14 +434,13 @@ __device__ void conn_lane(const DecodeArgs& a, const GroupLane& L, bool act, con
     uint32_t* walk_out = a.walk_scratch + L.wp_base;
     // triangle indices are relative to the mesh's first vertex
     const uint32_t vloc = act ? static_cast<uint32_t>(L.v_base - L.P->v_offset) : 0u;
-    const uint32_t s0 = static_cast<uint32_t>(L.t_base) & 3u;  // output quad slot of triangle 0
+    const uint32_t t0odd = static_cast<uint32_t>(L.t_base) & 1u;  // parity of the first triangle's index
     uint32_t cpos = L.d.start_bit + 48u;
     uint32_t strips_left = L.d.n_strips;
     uint32_t tok_left = 0u, tok_idx = 0u, tris = 0u;
     uint32_t p0 = 0u, p1 = 0u, p2 = 0u;
     uint32_t tcnt = 0u, wcnt = 0u, kind0 = 0u;
     Fifo fifo;
-    Quad tq, wq;
     bool bad = false;
     bool running = act && strips_left > 0u;
     // One token per iteration, every lane on the same straight-line path:
@@ -505,56 +469,42 @@ __device__ void conn_lane(const DecodeArgs& a, const GroupLane& L, bool act, con
             const uint32_t fi = (x << 1) >> 27;
             cpos += raw ? 1u + ib : 6u;
             // decode_dup raises IndexError on both (FIFO index, local id)
-            const bool invalid = (raw ? rid >= n_local : fi >= fifo.len) || tris > n_tris;
+            const bool invalid = (raw ? rid >= n_local : fi >= fifo.len) | (tris > n_tris);
             const uint32_t v = raw ? (rid & 0xFFu) : fifo.at((16u - fifo.len + fi) & 15u);
             const uint32_t at = fifo.find(v);
             const uint32_t rm = at < 16u ? at : (fifo.len >= 15u ? 0u : 15u - fifo.len);
             fifo.remove_append(rm, v);
-            fifo.len += (at == 16u && fifo.len < 16u) ? 1u : 0u;
+            fifo.len += ((at == 16u) & (fifo.len < 16u)) ? 1u : 0u;
             // edge code 0 -> (p1, p2 | p0), 1 -> (p0, p2 | p1)  (:530-535)
             const uint32_t cref = ec ? p1 : p0;
             const uint32_t q0 = body ? (ec ? p0 : p1) : (tok_idx == 0u ? v : p0);
             const uint32_t q1 = body ? p2 : (tok_idx == 1u ? v : p1);
-            const uint32_t q2 = (body || tok_idx == 2u) ? v : p2;
+            const uint32_t q2 = (body | (tok_idx == 2u)) ? v : p2;
             p0 = q0;
             p1 = q1;
             p2 = q2;
-            // triangle -> output quad; a quad that fills up is written out
-            const bool emit = (body || tok_idx == 2u) && !invalid;
-            const uint32_t ts = (s0 + tcnt) & 3u;
-            if (emit) tq.put(ts, q0 | (q1 << 8) | (q2 << 16));
-            if (emit && ts == 3u) {
-                const int first = static_cast<int>(tcnt) - 3;
-                store_tris(tq, tri_out, first, first < 0 ? -first : 0, 4, vloc);
-            }
+            // triangle -> output, as global vertex ids
+            const bool emit = (body | (tok_idx == 2u)) & !invalid;
+            if (emit) store_tri(tri_out, tcnt, ((t0odd + tcnt) & 1u) != 0u, vloc + q0, vloc + q1, vloc + q2);
             tcnt += emit ? 1u : 0u;
             // first occurrence -> next walk entry (:523-541).  Roots are 'none'
             // (stored as v,v,v,v); strip bodies 'para' with (a, b, c) = (p0, p1, cref).
             uint32_t* sp = seen + (v >> 5) * 32u + lane;
             const uint32_t sw = *sp;
             const uint32_t bit = 1u << (v & 31u);
-            const bool isnew = !(sw & bit) && !invalid;
+            const bool isnew = ((sw & bit) == 0u) & !invalid;
             if (isnew) *sp = sw | bit;
             const uint32_t e = body ? (v | (q0 << 8) | (q1 << 16) | (cref << 24)) : v * 0x01010101u;
-            const uint32_t ws = wcnt & 3u;
-            if (isnew) wq.put(ws, e);
-            if (isnew && ws == 3u)
-                *reinterpret_cast<uint4*>(walk_out + wcnt - 3u) = make_uint4(wq.q0, wq.q1, wq.q2, wq.q3);
+            if (isnew) walk_out[wcnt] = e;
             wcnt += isnew ? 1u : 0u;
-            kind0 += (isnew && !body) ? 1u : 0u;
+            kind0 += (isnew & !body) ? 1u : 0u;
             tok_idx++;
             tok_left--;
-            bad = bad || invalid || cpos > end;
-            running = !bad && !(tok_left == 0u && strips_left == 0u);
+            bad = bad | invalid | (cpos > end);
+            running = !bad & ((tok_left | strips_left) != 0u);
         }
     }
     if (act) {
-        const uint32_t r = (s0 + tcnt) & 3u;  // triangles in the open quad
-        if (r) {
-            const int first = static_cast<int>(tcnt) - static_cast<int>(r);
-            store_tris(tq, tri_out, first, first < 0 ? -first : 0, static_cast<int>(r), vloc);
-        }
-        quad_tail(wq, wcnt, walk_out);
         if (bad || tris != n_tris) {
             report(a.status, kErrCorrupt, L.m);
         } else {
@@ -654,16 +604,11 @@ __device__ __forceinline__ float dequant_value(const float* c, const MeshParams*
     return stride_dequant_exact(&P->dq[axis], q);
 }
 
-template <bool kShared>
-__device__ __noinline__ bool residual_slow(const uint32_t* w, uint32_t rbase, uint32_t* pos, uint32_t tk,
-                                           uint32_t limit, uint32_t* u) {
-    return read_code<kShared>(w, rbase, *pos, tk, limit, *u) == 0;
-}
-
 // Residual of one axis: Rice/EG codeword at `pos` with a straight-line fast
-// path (prefix and value inside one 32-bit window) and the general reader
-// out of line.  Returns false on a malformed codeword; `pos` never passes
-// `limit`, so a corrupt stream cannot steer reads outside the meshlet.
+// path (prefix and value inside one 32-bit window); the general reader runs
+// inline behind the only branch, taken for codewords longer than 32 bits.
+// Returns false on a malformed codeword; `pos` never passes `limit`, so a
+// corrupt stream cannot steer reads outside the meshlet.
 template <bool kShared>
 __device__ __forceinline__ bool residual(const uint32_t* w, uint32_t rbase, uint32_t& pos, uint32_t tk,
                                          uint32_t limit, int32_t& r) {
@@ -672,15 +617,16 @@ __device__ __forceinline__ bool residual(const uint32_t* w, uint32_t rbase, uint
     const uint32_t k = tk & 0x3Fu;
     const bool eg = (tk & 0x80u) != 0u;
     const uint32_t nb = (eg ? z : 0u) + k;
+    const uint32_t len = z + 1u + nb;
     const uint32_t t = __funnelshift_lc(0u, x, z + 1u);      // bits after the terminator
     const uint32_t val = __funnelshift_rc(t, 0u, 32u - nb);  // the top nb of them
     const uint32_t base = eg ? ((1u << (z & 31u)) - 1u) : z;
     uint32_t u = (base << k) + val;
+    uint32_t np = pos + len;
     bool ok = true;
-    uint32_t np = pos + z + 1u + nb;
-    if (z + 1u + nb > 32u) {  // long prefix or long value: rare
+    if (len > 32u) {  // long prefix or long value: rare
         np = pos;
-        ok = residual_slow<kShared>(w, rbase, &np, tk, limit, &u);
+        ok = read_code<kShared>(w, rbase, np, tk, limit, u) == 0;
     }
     ok = ok && np <= limit;
     pos = min(np, limit);
@@ -698,68 +644,84 @@ __device__ __forceinline__ bool skip_codes(const uint32_t* w, uint32_t rbase, ui
     for (uint32_t i = 0; i < n; i++) {
         const uint32_t x = peek32<kShared>(w, pos + rbase);
         const uint32_t z = __clz(x);
-        uint32_t np = pos + z + 1u + (eg ? z : 0u) + k;
+        const uint32_t len = z + 1u + (eg ? z : 0u) + k;
+        uint32_t np = pos + len;
         if (x == 0u) {
             uint32_t u;
             np = pos;
-            ok = ok && residual_slow<kShared>(w, rbase, &np, tk, limit, &u);
+            ok = ok & (read_code<kShared>(w, rbase, np, tk, limit, u) == 0);
         }
-        ok = ok && np <= limit;
+        ok = ok & (np <= limit);
         pos = min(np, limit);
     }
     return ok;
 }
 
-// Per-lane state carried across the three axis passes of one meshlet.
+// Per-lane state of one axis of one meshlet.
 struct VertLane {
-    uint32_t tk[6];   // (tag, k) of dx dy dz px py pz: bit 7 Exp-Golomb, bits 0..5 k
-    int32_t anc[3];   // anchor codes
-    uint32_t cd[3];   // start of the dx, dy, dz substreams
-    uint32_t cp;      // parallelogram cursor: px, then py, then pz
+    int32_t anc;      // anchor code of the axis
+    uint32_t td, tp;  // (tag, k) of the axis' delta / parallelogram substream: bit 7 Exp-Golomb, bits 0..5 k
+    uint32_t cdd;     // delta cursor
+    uint32_t cp;      // parallelogram cursor
     bool bad;
 };
 
-// Anchor, the six (tag, k) pairs and the three delta substream starts
-// (paradelta_v5_dup.py:544-579).  The parallelogram substreams follow the
-// delta ones, so finding px means skipping dx, dy and dz.
+// Anchor, the six (tag, k) pairs, and where axis d's two substreams start
+// (paradelta_v5_dup.py:544-579): the delta substreams dx dy dz come first,
+// then px py pz, so axis d skips the three delta substreams and the d
+// parallelogram substreams before its own (substream lengths are not
+// stored, only their code counts).
 template <bool kShared>
-__device__ __forceinline__ void vert_setup(const GroupLane& L, const uint32_t* w, uint32_t rbase, VertLane& S) {
+__device__ __forceinline__ void vert_setup(const GroupLane& L, uint32_t d, const uint32_t* w, uint32_t rbase,
+                                           VertLane& S) {
     const uint32_t n_kind0 = L.d.walk & 0xFFFFu;
+    const uint32_t n_walk = L.d.walk >> 16;
     const uint32_t n_delta = n_kind0 ? n_kind0 - 1u : 0u;  // the anchor has no delta
+    const uint32_t n_para = n_walk - n_kind0;
     const uint32_t end = L.d.end_bit;
     const MeshParams* P = L.P;
     uint32_t pos = L.d.anchor_bit;
-    S.bad = false;
+    bool bad = false;
+    S.anc = 0;
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-        const uint32_t gb = P->g_bits[d];
-        S.anc[d] = gb ? static_cast<int32_t>(peek32<kShared>(w, pos + rbase) >> (32u - gb)) : 0;
+    for (uint32_t e = 0; e < 3u; e++) {
+        const uint32_t gb = P->g_bits[e];
+        const int32_t v = gb ? static_cast<int32_t>(peek32<kShared>(w, pos + rbase) >> (32u - gb)) : 0;
+        S.anc = e == d ? v : S.anc;
         pos += gb;
     }
+    uint32_t tk[6];
 #pragma unroll
     for (int i = 0; i < 6; i++) {
         const uint32_t t = peek32<kShared>(w, pos + rbase) >> 16;
         pos += 16u;
         const uint32_t k = t & 0xFFu;
-        if (k > static_cast<uint32_t>(kMaxResidK)) S.bad = true;
-        S.tk[i] = ((t >> 8) == 1u ? 0u : 0x80u) | (k & 0x3Fu);
+        bad = bad || k > static_cast<uint32_t>(kMaxResidK);
+        tk[i] = ((t >> 8) == 1u ? 0u : 0x80u) | (k & 0x3Fu);
     }
-    if (pos > end) S.bad = true;
+    S.td = d == 0u ? tk[0] : (d == 1u ? tk[1] : tk[2]);
+    S.tp = d == 0u ? tk[3] : (d == 1u ? tk[4] : tk[5]);
+    bad = bad || pos > end;
     pos = min(pos, end);
-    bool ok = !S.bad;
+    bool ok = !bad;
+    S.cdd = pos;
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-        S.cd[d] = pos;
-        if (ok) ok = skip_codes<kShared>(w, rbase, pos, S.tk[d], n_delta, end);
+    for (uint32_t e = 0; e < 3u; e++) {
+        S.cdd = e == d ? pos : S.cdd;
+        if (ok) ok = skip_codes<kShared>(w, rbase, pos, tk[e], n_delta, end);
     }
+    for (uint32_t e = 0; e < d; e++)
+        if (ok) ok = skip_codes<kShared>(w, rbase, pos, e == 0u ? tk[3] : tk[4], n_para, end);
     S.cp = pos;
     S.bad = !ok;
 }
 
 // Integer codes of axis d in walk order (IRLP, paradelta_v5_dup.py:91-104
 // and 581-600).  Every walk vertex is a root (delta from the previous walk
-// vertex, or the anchor for the first) or a parallelogram vertex predicted
-// from three earlier ones; the loop body is straight-line with selects.
+// vertex; the first one is the anchor) or a parallelogram vertex predicted
+// from three earlier ones.  Four walk entries per iteration (one 16-byte
+// load); entries past the end are masked, not branched around, and root and
+// parallelogram vertices differ only in selects.
 template <bool kShared, bool kWide>
 __device__ __forceinline__ void vert_axis(const DecodeArgs& a, const GroupLane& L, uint32_t d, const uint32_t* w,
                                           uint32_t rbase, PlaneT<kWide>* plane, VertLane& S) {
@@ -775,34 +737,16 @@ __device__ __forceinline__ void vert_axis(const DecodeArgs& a, const GroupLane& 
     const int32_t n0 = P->pred_n[3 * d], n1 = P->pred_n[3 * d + 1], n2 = P->pred_n[3 * d + 2];
     const int32_t K = P->pred_k[d], half = P->pred_half[d];
     const uint32_t cmax = P->code_max[d];
-    const uint32_t td = S.tk[d], tp = S.tk[3 + d];
-    const int32_t anc = S.anc[d];
-    uint32_t cdd = S.cd[d], cp = S.cp;
-    // walk entries (v | a << 8 | b << 16 | c << 24), two quads in flight
-    const uint4* wq = reinterpret_cast<const uint4*>(a.walk_scratch + L.wp_base);
-    const uint32_t nq = (n_walk + 3u) >> 2;
-    uint4 qa = nq > 0u ? __ldcg(wq) : make_uint4(0u, 0u, 0u, 0u);
-    uint4 qb = nq > 1u ? __ldcg(wq + 1) : qa;
-    uint4 q = qa;
+    const uint32_t td = S.td, tp = S.tp;
+    const int32_t anc = S.anc;
+    uint32_t cdd = S.cdd, cp = S.cp;
     int32_t prev = 0;
-    bool first = true;
     bool fail = false;
-    for (uint32_t i = 0; i < n_walk; i++) {
-        const uint32_t s = i & 3u;
-        if (s == 0u) {
-            q = qa;
-            qa = qb;
-            const uint32_t nx = (i >> 2) + 2u;
-            if (nx < nq) qb = __ldcg(wq + nx);
-        }
-        const uint32_t e = s == 0u ? q.x : (s == 1u ? q.y : (s == 2u ? q.z : q.w));
+    auto step = [&](uint32_t e, bool valid, bool anchor) {
+        e = valid ? e : 0u;  // a masked entry reads plane[0] and commits nothing
         const uint32_t v = e & 0xFFu;
         const uint32_t ra = (e >> 8) & 0xFFu, rb = (e >> 16) & 0xFFu, rc = e >> 24;
-        const bool para = ra != v;
-        const bool anchor = first && !para;  // the first walk vertex is the anchor
-        first = first && para;
-        // for root entries the references are the vertex itself and the
-        // prediction is discarded
+        const bool para = ra != v;  // roots are stored as (v, v, v, v)
         const int32_t ca = static_cast<int32_t>(plane[ra]);
         const int32_t cb = static_cast<int32_t>(plane[rb]);
         const int32_t cc = static_cast<int32_t>(plane[rc]);
@@ -810,13 +754,25 @@ __device__ __forceinline__ void vert_axis(const DecodeArgs& a, const GroupLane& 
         uint32_t p = para ? cp : cdd;
         int32_t r;
         const bool okr = residual<kShared>(w, rbase, p, para ? tp : td, end, r);
-        cp = para ? p : cp;
-        cdd = (!para && !anchor) ? p : cdd;
+        const bool commit = valid & !anchor;  // the anchor has no residual
+        cp = (commit & para) ? p : cp;
+        cdd = (commit & !para) ? p : cdd;
         const int32_t code = anchor ? anc : pred + r;
         // codes of a valid stream lie in [0, 2^g_bits)
-        fail = fail || !(okr || anchor) || static_cast<uint32_t>(code) > cmax;
-        plane[v] = static_cast<PlaneT<kWide>>(code);
-        prev = code;
+        fail = fail | (valid & ((!okr & !anchor) | (static_cast<uint32_t>(code) > cmax)));
+        if (valid) plane[v] = static_cast<PlaneT<kWide>>(code);
+        prev = valid ? code : prev;
+    };
+    // walk entries (v | a << 8 | b << 16 | c << 24), 16-byte aligned per meshlet
+    const uint4* wq = reinterpret_cast<const uint4*>(a.walk_scratch + L.wp_base);
+    uint4 qn = n_walk ? __ldcg(wq) : make_uint4(0u, 0u, 0u, 0u);
+    for (uint32_t i = 0; i < n_walk; i += 4u) {
+        const uint4 q = qn;
+        if (i + 4u < n_walk) qn = __ldcg(wq + (i >> 2) + 1u);
+        step(q.x, true, i == 0u);
+        step(q.y, i + 1u < n_walk, false);
+        step(q.z, i + 2u < n_walk, false);
+        step(q.w, i + 3u < n_walk, false);
     }
     S.cp = cp;
     S.bad = S.bad || fail;
@@ -855,53 +811,54 @@ __device__ void emit_axis(const DecodeArgs& a, const GroupLane& L, uint32_t rmas
     __syncwarp();
 }
 
-// One round: the active lanes decode their meshlets axis by axis, and after
-// each axis the warp writes that coordinate out of the shared code planes.
+// One round of warp d: its active lanes decode axis d of their meshlets,
+// then the warp writes that coordinate of every vertex.
 template <bool kShared, bool kWide>
-__device__ __forceinline__ void vert_round(const DecodeArgs& a, const GroupLane& L, bool act, uint32_t rmask,
-                                           const uint32_t* w, uint32_t rbase, uint8_t* planes, uint32_t code_off,
-                                           float* dqc, int lane) {
+__device__ __forceinline__ void vert_round(const DecodeArgs& a, const GroupLane& L, uint32_t d, bool act,
+                                           uint32_t rmask, const uint32_t* w, uint32_t rbase, uint8_t* planes,
+                                           uint32_t code_off, float* dqc, int lane) {
     VertLane S;
     S.bad = false;
     S.cp = 0u;
-    if (act) vert_setup<kShared>(L, w, rbase, S);
+    if (act) vert_setup<kShared>(L, d, w, rbase, S);
     PlaneT<kWide>* plane = reinterpret_cast<PlaneT<kWide>*>(planes + code_off);
-    for (uint32_t d = 0; d < 3u; d++) {
-        if (act && !S.bad) vert_axis<kShared, kWide>(a, L, d, w, rbase, plane, S);
-        __syncwarp();
-        emit_axis<kWide>(a, L, rmask, planes, code_off, d, dqc, lane);
-    }
+    if (act && !S.bad) vert_axis<kShared, kWide>(a, L, d, w, rbase, plane, S);
+    __syncwarp();
+    emit_axis<kWide>(a, L, rmask, planes, code_off, d, dqc, lane);
     if (act) {
-        // the last substream must end where the next meshlet starts (:507)
+        // pz, the last substream, must end where the next meshlet starts (:507)
         const MeshParams* P = L.P;
         const bool last_of_mesh = L.m - P->meshlet_begin + 1u == P->n_meshlets;
-        if (!S.bad && (last_of_mesh ? S.cp > L.d.end_bit : S.cp != L.d.end_bit)) S.bad = true;
+        if (d == 2u && !S.bad && (last_of_mesh ? S.cp > L.d.end_bit : S.cp != L.d.end_bit)) S.bad = true;
         if (S.bad) report(a.status, kErrCorrupt, L.m);
     }
 }
 
-template <int W, bool kWide>
-__global__ void __launch_bounds__(W * 32) vert_kernel(DecodeArgs a, uint32_t stage_bytes, uint32_t code_bytes,
-                                                      int persistent) {
+// A CTA decodes one group of 32 meshlets with three warps, warp d = axis d;
+// the group's residual bits are staged once and read by all three.
+template <bool kWide>
+__global__ void __launch_bounds__(96, 1) vert_kernel(DecodeArgs a, uint32_t stage_bytes, uint32_t code_bytes,
+                                                  int persistent) {
     extern __shared__ __align__(128) uint8_t smem[];
-    const int warp = threadIdx.x >> 5;
+    __shared__ uint32_t s_group;
+    const uint32_t d = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
-    if (*reinterpret_cast<volatile unsigned long long*>(&a.status->err) != 0ull) return;
+    const bool failed = *reinterpret_cast<volatile unsigned long long*>(&a.status->err) != 0ull;
+    if (__syncthreads_or(failed)) return;  // CTA-uniform: every barrier below is reached by all threads
     const uint32_t vstage = vert_stage_bytes(stage_bytes);
-    uint8_t* base = smem + warp * vert_warp_bytes(stage_bytes, code_bytes);
-    uint32_t* stage = reinterpret_cast<uint32_t*>(base);
-    uint8_t* planes = base + align16(vstage + 32u);
+    uint32_t* stage = reinterpret_cast<uint32_t*>(smem);
+    uint8_t* planes = smem + align16(vstage + 32u) + d * vert_axis_bytes(code_bytes);
     float* dqc = reinterpret_cast<float*>(planes + align16(code_bytes));
-    uint64_t* bar = reinterpret_cast<uint64_t*>(dqc + 8);
-    if (lane == 0) mbar_init(bar);
-    __syncwarp();
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + align16(vstage + 32u) + 3u * vert_axis_bytes(code_bytes));
+    if (threadIdx.x == 0) mbar_init(bar);
+    __syncthreads();
     uint32_t phase = 0u;
     const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
-    uint32_t g = blockIdx.x * W + warp;
+    uint32_t g = blockIdx.x;
     if (persistent) {
-        uint32_t t = 0u;
-        if (lane == 0) t = atomicAdd(&a.status->work_vert, 1u);
-        g = __shfl_sync(kFull, t, 0);
+        if (threadIdx.x == 0) s_group = atomicAdd(&a.status->work_vert, 1u);
+        __syncthreads();
+        g = s_group;
     }
     while (g < n_groups) {
         GroupLane L;
@@ -909,7 +866,7 @@ __global__ void __launch_bounds__(W * 32) vert_kernel(DecodeArgs a, uint32_t sta
         const uint32_t n_local = L.d.counts0 & 0xFFFFu;
         bool ok = L.valid;
         if (ok && !placement_ok(a, L)) {
-            report(a.status, kErrCorrupt, L.m);
+            if (d == 0u) report(a.status, kErrCorrupt, L.m);
             ok = false;
         }
         // this lane's residual bits: anchor .. end, 16-byte aligned
@@ -917,6 +874,7 @@ __global__ void __launch_bounds__(W * 32) vert_kernel(DecodeArgs a, uint32_t sta
         const unsigned long long end16 = (L.blob_off + ((L.d.end_bit + 7u) >> 3) + 15ull) & ~15ull;
         const uint32_t ssz = ok ? static_cast<uint32_t>(end16 - src16) : 0u;
         const uint32_t csz = align16(n_local * static_cast<uint32_t>(sizeof(PlaneT<kWide>)));
+        // the three warps see the same descriptors, so they form the same rounds
         uint32_t todo = __ballot_sync(kFull, ok);
         while (todo) {
             const int first = __ffs(todo) - 1;
@@ -945,28 +903,33 @@ __global__ void __launch_bounds__(W * 32) vert_kernel(DecodeArgs a, uint32_t sta
                 const int last = 31 - __clz(rmask);
                 const uint32_t total = __shfl_sync(kFull, cs, last);
                 const uint32_t dst_off = act ? cs - ssz : 0u;
-                __syncwarp();
-                if (lane == 0) mbar_expect(bar, total);
-                __syncwarp();
-                if (act && ssz) bulk_copy(reinterpret_cast<uint8_t*>(stage) + dst_off, a.arena + src16, ssz, bar);
-                if (!mbar_wait(bar, phase)) {
-                    if (lane == 0) report(a.status, kErrTimeout, L.m);
+                if (d == 0u) {
+                    if (lane == 0) mbar_expect(bar, total);
+                    __syncwarp();
+                    if (act && ssz)
+                        bulk_copy(reinterpret_cast<uint8_t*>(stage) + dst_off, a.arena + src16, ssz, bar);
+                }
+                const bool timed_out = !mbar_wait(bar, phase);
+                if (__syncthreads_or(timed_out)) {
+                    if (threadIdx.x == 0) report(a.status, kErrTimeout, L.m);
                     mbar_wait(bar, phase);  // let the copies land before the CTA exits
                     return;
                 }
                 phase ^= 1u;
                 const uint32_t rbase = static_cast<uint32_t>(L.blob_off * 8ull - src16 * 8ull + dst_off * 8ull);
-                vert_round<true, kWide>(a, L, act, rmask, stage, rbase, planes, code_off, dqc, lane);
+                vert_round<true, kWide>(a, L, d, act, rmask, stage, rbase, planes, code_off, dqc, lane);
             } else {
-                vert_round<false, kWide>(a, L, act, rmask, reinterpret_cast<const uint32_t*>(a.arena + L.blob_off),
-                                         0u, planes, code_off, dqc, lane);
+                vert_round<false, kWide>(a, L, d, act, rmask,
+                                         reinterpret_cast<const uint32_t*>(a.arena + L.blob_off), 0u, planes,
+                                         code_off, dqc, lane);
             }
-            __syncwarp();
+            __syncthreads();  // the next round overwrites the stage
         }
         if (!persistent) break;
-        uint32_t t = 0u;
-        if (lane == 0) t = atomicAdd(&a.status->work_vert, 1u);
-        g = __shfl_sync(kFull, t, 0);
+        __syncthreads();  // every thread has read s_group
+        if (threadIdx.x == 0) s_group = atomicAdd(&a.status->work_vert, 1u);
+        __syncthreads();
+        g = s_group;
     }
 }
 
@@ -1034,17 +997,17 @@ cudaError_t launch_conn(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t 
     return cudaGetLastError();
 }
 
-template <int W, bool kWide>
+template <bool kWide>
 cudaError_t launch_vert(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s) {
     static size_t configured[64] = {0};
     static OccCache occ;
-    const size_t smem = static_cast<size_t>(W) * vert_warp_bytes(cfg.stage_bytes, cfg.code_bytes);
-    cudaError_t e = opt_in_smem(vert_kernel<W, kWide>, smem, configured);
+    const size_t smem = vert_cta_bytes(cfg.stage_bytes, cfg.code_bytes);
+    cudaError_t e = opt_in_smem(vert_kernel<kWide>, smem, configured);
     if (e != cudaSuccess) return e;
     const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
-    const uint32_t grid = grid_for(vert_kernel<W, kWide>, W * 32, smem, cfg, n_groups, W, occ);
+    const uint32_t grid = grid_for(vert_kernel<kWide>, 96, smem, cfg, n_groups, 1, occ);
     if (grid == 0) return cudaSuccess;
-    vert_kernel<W, kWide><<<grid, W * 32, smem, s>>>(a, cfg.stage_bytes, cfg.code_bytes, cfg.persistent);
+    vert_kernel<kWide><<<grid, 96, smem, s>>>(a, cfg.stage_bytes, cfg.code_bytes, cfg.persistent);
     return cudaGetLastError();
 }
 
@@ -1053,7 +1016,7 @@ cudaError_t launch_pair(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t 
     cudaError_t e = launch_conn<W>(a, cfg, s);
     if (e != cudaSuccess) return e;
     if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[2]), s);
-    return a.wide_codes ? launch_vert<W, true>(a, cfg, s) : launch_vert<W, false>(a, cfg, s);
+    return a.wide_codes ? launch_vert<true>(a, cfg, s) : launch_vert<false>(a, cfg, s);
 }
 
 }  // namespace
@@ -1062,9 +1025,7 @@ size_t conn_smem_bytes(const LaunchCfg& cfg) {
     return static_cast<size_t>(cfg.warps_per_cta) * conn_warp_bytes(cfg.stage_bytes);
 }
 
-size_t vert_smem_bytes(const LaunchCfg& cfg) {
-    return static_cast<size_t>(cfg.warps_per_cta) * vert_warp_bytes(cfg.stage_bytes, cfg.code_bytes);
-}
+size_t vert_smem_bytes(const LaunchCfg& cfg) { return vert_cta_bytes(cfg.stage_bytes, cfg.code_bytes); }
 
 int device_sm_count() {
     static int cached[64] = {0};
