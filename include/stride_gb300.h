@@ -225,6 +225,10 @@ int stride_server_submit(stride_server* s, const uint8_t* data, size_t len, uint
 int stride_server_wait(stride_server* s, uint64_t req_id, int timeout_ms, stride_result* out);
 /* Frees the request's arena space. */
 int stride_server_release(stride_server* s, uint64_t req_id);
+/* hold != 0: keep admitting submissions to the queue but start no launch
+ * (e.g. to collect a frame's requests into as few launches as possible);
+ * hold == 0: resume.  Launches already running are not affected. */
+int stride_server_hold(stride_server* s, int hold);
 int stride_server_stats(stride_server* s, uint64_t* launches, uint64_t* completed,
                         uint64_t* arena_peak_bytes);
 void stride_server_destroy(stride_server* s);

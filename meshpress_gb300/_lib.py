@@ -112,6 +112,7 @@ SIGNATURES = [
     ("stride_server_submit", _I, [_P, _P, _SZ, ctypes.POINTER(_U64)]),
     ("stride_server_wait", _I, [_P, _U64, _I, ctypes.POINTER(ServerResult)]),
     ("stride_server_release", _I, [_P, _U64]),
+    ("stride_server_hold", _I, [_P, _I]),
     ("stride_server_stats", _I, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
     ("stride_server_destroy", None, [_P]),
 ]

@@ -2,6 +2,7 @@
 // parse, device buffers, enqueue and status.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -132,6 +133,31 @@ const char* status_message(int code) {
 
 using namespace stride;
 
+namespace stride {
+
+unsigned long long plan_luts(MeshParams* p, uint32_t n, uint32_t* meshes, uint32_t max_meshes, uint32_t* n_lut,
+                             uint32_t* lut_max) {
+    unsigned long long total = 0;
+    uint32_t k = 0, mx = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        p[i].has_lut = 0;
+        p[i].lut_off = 0;
+        const unsigned long long e = lut_entries(p[i]);
+        if (!e || k >= max_meshes || k >= 65535u) continue;  // grid.y limit of lut_kernel
+        p[i].has_lut = 1;
+        p[i].lut_off = total;
+        total += e;
+        if (meshes) meshes[k] = i;
+        k++;
+        mx = std::max<uint32_t>(mx, static_cast<uint32_t>(e));
+    }
+    *n_lut = k;
+    *lut_max = mx;
+    return total;
+}
+
+}  // namespace stride
+
 struct stride_handle {
     int device = 0;
     size_t len = 0, cap_bytes = 0;
@@ -148,6 +174,10 @@ struct stride_handle {
     uint32_t* d_idx = nullptr;
     float* d_pos = nullptr;
     size_t cap_v = 0, cap_t = 0;
+    float* d_lut = nullptr;             // dequantisation tables
+    unsigned long long lut_cap = 0;     // floats
+    uint32_t* d_lut_mesh = nullptr;     // the one-entry mesh list {0}
+    uint32_t n_lut = 0, lut_max = 0;
     cudaEvent_t done = nullptr;
     bool launched = false;
     LaunchCfg cfg;
@@ -163,6 +193,11 @@ static void free_buffers(stride_handle* h) {
     cudaFree(h->d_status);
     cudaFree(h->d_idx);
     cudaFree(h->d_pos);
+    cudaFree(h->d_lut);
+    cudaFree(h->d_lut_mesh);
+    h->d_lut = nullptr;
+    h->d_lut_mesh = nullptr;
+    h->lut_cap = 0;
     h->d_walk_scratch = nullptr;
     h->walk_cap = 0;
     h->d_blob = nullptr;
@@ -175,8 +210,25 @@ static void free_buffers(stride_handle* h) {
     h->d_pos = nullptr;
 }
 
-static int ensure_capacity(stride_handle* h, size_t len, uint32_t n_meshlets, uint64_t n_v) {
+// Buffers for a stream of this size; also plans the dequantisation tables
+// of `p` (has_lut, lut_off) and sizes their buffer.
+static int ensure_capacity(stride_handle* h, size_t len, MeshParams& p) {
+    const uint32_t n_meshlets = p.n_meshlets;
+    const uint64_t n_v = p.n_v;
     cudaError_t e;
+    const unsigned long long lut = plan_luts(&p, 1, nullptr, 1, &h->n_lut, &h->lut_max);
+    if (!h->d_lut_mesh) {
+        const uint32_t zero = 0u;
+        if ((e = cudaMalloc(&h->d_lut_mesh, sizeof(uint32_t))) != cudaSuccess ||
+            (e = cudaMemcpy(h->d_lut_mesh, &zero, sizeof(zero), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return cuda_fail(e, "cudaMalloc(table list)");
+    }
+    if (lut > h->lut_cap) {
+        cudaFree(h->d_lut);
+        h->d_lut = nullptr;
+        if ((e = cudaMalloc(&h->d_lut, 4ull * lut)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(tables)");
+        h->lut_cap = lut;
+    }
     const unsigned long long ww = walk_scratch_words(n_v, n_meshlets);
     if (ww > h->walk_cap) {
         cudaFree(h->d_walk_scratch);
@@ -272,10 +324,11 @@ int stride_open(const uint8_t* data, size_t len, stride_handle** out) {
     if (rc) return fail(rc, "%s", why);
     stride_handle* h = new stride_handle();
     cudaGetDevice(&h->device);
-    h->params = p;
     h->len = len;
     cudaError_t e;
-    if ((rc = ensure_capacity(h, len, p.n_meshlets, p.n_v)) != STRIDE_OK) {
+    rc = ensure_capacity(h, len, p);
+    h->params = p;
+    if (rc != STRIDE_OK) {
         free_buffers(h);
         delete h;
         return rc;
@@ -301,7 +354,7 @@ int stride_reload(stride_handle* h, const uint8_t* data, size_t len, void* strea
     char why[256] = {0};
     int rc = parse_header(data, len, &p, why, sizeof(why));
     if (rc) return fail(rc, "%s", why);
-    if ((rc = ensure_capacity(h, len, p.n_meshlets, p.n_v)) != STRIDE_OK) return rc;
+    if ((rc = ensure_capacity(h, len, p)) != STRIDE_OK) return rc;
     h->params = p;
     h->len = len;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
@@ -337,6 +390,10 @@ static DecodeArgs handle_args(stride_handle* h, uint32_t* d_idx, float* d_pos, i
     a.pos = d_pos;
     a.codes = d_codes;
     a.wide_codes = h->params.g_bits[0] > 16 || h->params.g_bits[1] > 16 || h->params.g_bits[2] > 16;
+    a.lut = h->d_lut;
+    a.lut_meshes = h->d_lut_mesh;
+    a.n_lut_meshes = h->n_lut;
+    a.lut_max = h->lut_max;
     return a;
 }
 

@@ -30,6 +30,9 @@ struct stride_batch {
     uint32_t* d_walk_scratch = nullptr;
     unsigned long long walk_cap = 0;
     Status* d_status = nullptr;
+    float* d_lut = nullptr;
+    uint32_t* d_lut_meshes = nullptr;
+    uint32_t n_lut = 0, lut_max = 0;
     bool wide = false;
     LaunchCfg cfg;
     cudaGraph_t graph = nullptr;
@@ -86,6 +89,8 @@ static void batch_free(stride_batch* b) {
     cudaFree(b->d_blk_prefix);
     cudaFree(b->d_walk_scratch);
     cudaFree(b->d_status);
+    cudaFree(b->d_lut);
+    cudaFree(b->d_lut_meshes);
 }
 
 static DecodeArgs batch_args(const stride_batch* b, uint32_t* d_idx, float* d_pos) {
@@ -105,6 +110,10 @@ static DecodeArgs batch_args(const stride_batch* b, uint32_t* d_idx, float* d_po
     a.pos = d_pos;
     a.codes = nullptr;
     a.wide_codes = b->wide;
+    a.lut = b->d_lut;
+    a.lut_meshes = b->d_lut_meshes;
+    a.n_lut_meshes = b->n_lut;
+    a.lut_max = b->lut_max;
     return a;
 }
 
@@ -144,6 +153,9 @@ int stride_batch_create(const uint8_t* const* blobs, const size_t* lens, uint32_
     if (b->wide) b->cfg.code_bytes = std::max<uint32_t>(b->cfg.code_bytes, kMaxLocal * 4u);
     b->arena_bytes = arena_bytes;
     b->walk_cap = walk_scratch_words(b->total_v, b->total_meshlets);
+    std::vector<uint32_t> lut_meshes(n_meshes);
+    const unsigned long long lut_floats =
+        plan_luts(b->params.data(), n_meshes, lut_meshes.data(), n_meshes, &b->n_lut, &b->lut_max);
     std::vector<uint8_t> arena(arena_bytes, 0);
     for (uint32_t i = 0; i < n_meshes; i++) std::memcpy(arena.data() + off[i], blobs[i], lens[i]);
     std::vector<uint32_t> mm(b->total_meshlets);
@@ -162,6 +174,10 @@ int stride_batch_create(const uint8_t* const* blobs, const size_t* lens, uint32_
         (e = cudaMalloc(&b->d_blk_prefix, sizeof(BlockPrefix) * std::max<uint32_t>(1u, nb))) != cudaSuccess ||
         (e = cudaMalloc(&b->d_walk_scratch, 4ull * b->walk_cap)) != cudaSuccess ||
         (e = cudaMalloc(&b->d_status, sizeof(Status))) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_lut, 4ull * std::max<unsigned long long>(1ull, lut_floats))) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_lut_meshes, 4ull * std::max<uint32_t>(1u, b->n_lut))) != cudaSuccess ||
+        (b->n_lut && (e = cudaMemcpy(b->d_lut_meshes, lut_meshes.data(), 4ull * b->n_lut,
+                                     cudaMemcpyHostToDevice)) != cudaSuccess) ||
         (e = cudaMemcpy(b->d_arena, arena.data(), arena_bytes, cudaMemcpyHostToDevice)) != cudaSuccess ||
         (e = cudaMemcpy(b->d_params, b->params.data(), sizeof(MeshParams) * n_meshes, cudaMemcpyHostToDevice)) !=
             cudaSuccess ||

@@ -51,9 +51,25 @@ struct MeshParams {
     int32_t pred_n[9];       // IRLP numerators, row = axis
     int32_t pred_k[3];
     int32_t pred_half[3];    // 2^(K-1), or 0 when K == 0
-    uint32_t pad;
+    uint32_t has_lut;        // positions come from a per-code table (see lut_entries)
+    unsigned long long lut_off;  // first float of the mesh's tables in DecodeArgs::lut
     stride_dequant_axis dq[3];
 };
+
+// Dequantisation tables: a mesh with at least as many duplicated vertices as
+// half its code space (all axes together) gets one float per code and axis,
+// evaluated once per decode by lut_kernel; axis d's table follows those of
+// the axes before it.  Only for codes of up to kLutMaxBits bits.
+constexpr uint32_t kLutMaxBits = 16;
+
+inline unsigned long long lut_entries(const MeshParams& p) {
+    unsigned long long e = 0;
+    for (int d = 0; d < 3; d++) {
+        if (p.g_bits[d] > kLutMaxBits) return 0;
+        e += 1ull << p.g_bits[d];
+    }
+    return e <= 2ull * p.n_v ? e : 0;
+}
 
 // Per-meshlet record: the scan kernel writes the first part, the
 // connectivity kernel the walk facts (64 bytes).
@@ -107,7 +123,17 @@ struct DecodeArgs {
     float* pos;
     int32_t* codes;                  // optional
     bool wide_codes;                 // some mesh has g_bits > 16
+    float* lut;                      // dequantisation tables (meshes with has_lut)
+    const uint32_t* lut_meshes;      // device: indices of those meshes
+    uint32_t n_lut_meshes;
+    uint32_t lut_max;                // largest table set (floats) of one mesh
 };
+
+// Host: assigns table offsets (has_lut, lut_off) to the meshes that get
+// tables; returns the floats needed, fills `meshes` (at most max_meshes
+// indices) and the largest per-mesh size.
+unsigned long long plan_luts(MeshParams* p, uint32_t n, uint32_t* meshes, uint32_t max_meshes, uint32_t* n_lut,
+                             uint32_t* lut_max);
 
 inline uint32_t scan_blocks(uint32_t total_meshlets) {
     return (total_meshlets + kScanThreads - 1) / kScanThreads;

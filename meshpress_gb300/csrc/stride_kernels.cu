@@ -121,6 +121,36 @@ __device__ __forceinline__ unsigned long long shfl64(unsigned long long v, int s
     return __shfl_sync(kFull, v, src);
 }
 
+// Sequential reader of one lane's bits through a three-word register
+// window: peeking costs one funnel shift, and the shared/global load that
+// refills the window is issued a word ahead of its use, off the chain that
+// carries the bit position.  Reads reach at most 95 bits past `pos`.
+template <bool kShared>
+struct BitWin {
+    const uint32_t* w;
+    uint32_t rbase, pos, w0, w1, w2;
+    __device__ __forceinline__ void seek(uint32_t p) {
+        pos = p;
+        const uint32_t i = (p + rbase) >> 5;
+        w0 = bswap32(ldw<kShared>(w, i));
+        w1 = bswap32(ldw<kShared>(w, i + 1u));
+        w2 = bswap32(ldw<kShared>(w, i + 2u));
+    }
+    __device__ __forceinline__ uint32_t peek() const { return __funnelshift_l(w1, w0, (pos + rbase) & 31u); }
+    // len <= 32: crosses at most one word boundary
+    __device__ __forceinline__ void advance(uint32_t len) {
+        const uint32_t np = pos + len;
+        const uint32_t i = (np + rbase) >> 5;
+        const bool cross = i != ((pos + rbase) >> 5);
+        pos = np;
+        if (cross) {
+            w0 = w1;
+            w1 = w2;
+            w2 = bswap32(ldw<kShared>(w, i + 2u));
+        }
+    }
+};
+
 // ---------------------------------------------------------------------------
 // Bulk-copy staging (TMA bulk, no tensor map) and its mbarrier.
 // ---------------------------------------------------------------------------
@@ -342,16 +372,80 @@ struct Fifo {
     }
 };
 
-// One triangle (three global vertex ids, 12 bytes) at triangle index t of a
-// 16-byte aligned index array: one 8-byte store on an 8-byte boundary and one
-// 4-byte store, chosen by the parity of t without a branch.
-__device__ __forceinline__ void store_tri(uint32_t* tri_out, uint32_t local, bool odd, uint32_t a, uint32_t b,
-                                          uint32_t c) {
-    uint32_t* p = tri_out + 3u * local;
-    uint2* p8 = reinterpret_cast<uint2*>(p + (odd ? 1u : 0u));
-    uint32_t* p4 = p + (odd ? 0u : 2u);
-    *p8 = odd ? make_uint2(b, c) : make_uint2(a, b);
-    *p4 = odd ? a : c;
+// Output rings.  Each lane collects its triangles (packed local ids) and its
+// walk entries in a 32-slot row of shared memory; every kFlushEvery token
+// iterations the warp writes whole 4-entry quads out with 16-byte stores
+// (a quad of triangles is 48 bytes starting at a triangle index divisible by
+// four), and at the end of the meshlet the unaligned head and tail go out as
+// single words.  A row is 36 words so that quads stay 16-byte aligned.
+constexpr uint32_t kRing = 32;
+constexpr uint32_t kRingRow = 36;
+constexpr uint32_t kFlushEvery = kRing - 4;  // a pending partial quad (<= 3) + new entries fit
+
+// Triangles [tf, tcnt) of one lane (local indices; the first triangle has
+// global index t_base, with ph = t_base & 3 and slot (ph + local) & 31).
+__device__ __forceinline__ void flush_tris(uint32_t* idx, unsigned long long t_base, const uint32_t* ring,
+                                           uint32_t& tf, uint32_t tcnt, uint32_t vloc, bool final) {
+    auto id = [vloc](uint32_t packed, uint32_t k) { return vloc + ((packed >> (8u * k)) & 0xFFu); };
+    const uint32_t ph = static_cast<uint32_t>(t_base) & 3u;
+    const uint32_t h = tf + ((4u - ((ph + tf) & 3u)) & 3u);  // first quad-aligned local index >= tf
+    const uint32_t he = min(h, tcnt);
+    const uint32_t r = (ph + tcnt) & 3u;
+    const uint32_t qe = tcnt >= r ? tcnt - r : 0u;            // end of the last whole quad (0: none)
+    uint32_t* out = idx + 3ull * t_base;
+    for (uint32_t l = tf; l < he; l++) {  // head: up to 3 triangles
+        const uint32_t p = ring[(ph + l) & 31u];
+        out[3u * l] = id(p, 0);
+        out[3u * l + 1u] = id(p, 1);
+        out[3u * l + 2u] = id(p, 2);
+    }
+    for (uint32_t l = h; l < qe; l += 4u) {
+        const uint4 q = *reinterpret_cast<const uint4*>(ring + ((ph + l) & 31u));
+        uint4* o = reinterpret_cast<uint4*>(out + 3u * l);
+        o[0] = make_uint4(id(q.x, 0), id(q.x, 1), id(q.x, 2), id(q.y, 0));
+        o[1] = make_uint4(id(q.y, 1), id(q.y, 2), id(q.z, 0), id(q.z, 1));
+        o[2] = make_uint4(id(q.z, 2), id(q.w, 0), id(q.w, 1), id(q.w, 2));
+    }
+    const uint32_t done = max(he, qe);
+    if (final) {
+        for (uint32_t l = done; l < tcnt; l++) {  // tail: up to 3 triangles
+            const uint32_t p = ring[(ph + l) & 31u];
+            out[3u * l] = id(p, 0);
+            out[3u * l + 1u] = id(p, 1);
+            out[3u * l + 2u] = id(p, 2);
+        }
+        tf = tcnt;
+    } else {
+        tf = done;
+    }
+}
+
+// Walk entries [wf, wcnt) of one lane; the lane's walk region starts 16-byte
+// aligned, so quads start at local indices divisible by four.
+__device__ __forceinline__ void flush_walk(uint32_t* out, const uint32_t* ring, uint32_t& wf, uint32_t wcnt,
+                                           bool final) {
+    const uint32_t qe = wcnt & ~3u;
+    for (uint32_t l = wf; l < qe; l += 4u)
+        *reinterpret_cast<uint4*>(out + l) = *reinterpret_cast<const uint4*>(ring + (l & 31u));
+    if (final) {
+        for (uint32_t l = max(wf, qe); l < wcnt; l++) out[l] = ring[l & 31u];
+        wf = wcnt;
+    } else {
+        wf = max(wf, qe);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 1b. dequantisation tables: one thread per (mesh, code), exact values
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) lut_kernel(DecodeArgs a) {
+    const MeshParams& P = a.meshes[a.lut_meshes[blockIdx.y]];
+    const uint32_t i = blockIdx.x * 256u + threadIdx.x;
+    const uint32_t e0 = 1u << P.g_bits[0], e1 = 1u << P.g_bits[1], e2 = 1u << P.g_bits[2];
+    if (i >= e0 + e1 + e2) return;
+    const uint32_t d = i < e0 ? 0u : (i < e0 + e1 ? 1u : 2u);
+    const uint32_t q = i - (d >= 1u ? e0 : 0u) - (d >= 2u ? e1 : 0u);
+    a.lut[P.lut_off + i] = stride_dequant(&P.dq[d], q);
 }
 
 // ---------------------------------------------------------------------------
@@ -359,14 +453,16 @@ __device__ __forceinline__ void store_tri(uint32_t* tri_out, uint32_t local, boo
 // ---------------------------------------------------------------------------
 __host__ __device__ constexpr uint32_t align16(uint32_t x) { return (x + 15u) & ~15u; }
 
+// connectivity warp: stage | first-occurrence bits (8 words per lane) |
+// triangle ring | walk ring | mbarrier
 __host__ __device__ inline uint32_t conn_warp_bytes(uint32_t stage_bytes) {
-    return align16(stage_bytes + 32u) + 8u * 32u * 4u + 16u;
+    return align16(stage_bytes + 32u) + 8u * 32u * 4u + 2u * 32u * kRingRow * 4u + 16u;
 }
 
 __host__ __device__ inline uint32_t vert_stage_bytes(uint32_t stage_bytes) { return stage_bytes / 2u; }
 
-// One axis warp's code plane and dequantisation constants (8 words).
-__host__ __device__ inline uint32_t vert_axis_bytes(uint32_t code_bytes) { return align16(code_bytes) + 32u; }
+// One axis warp's code plane.
+__host__ __device__ inline uint32_t vert_axis_bytes(uint32_t code_bytes) { return align16(code_bytes); }
 
 // Vertex CTA: residual stage | three axis regions | mbarrier.
 __host__ __device__ inline uint32_t vert_cta_bytes(uint32_t stage_bytes, uint32_t code_bytes) {
@@ -422,7 +518,7 @@ __device__ __forceinline__ bool placement_ok(const DecodeArgs& a, const GroupLan
 
 template <bool kShared>
 __device__ void conn_lane(const DecodeArgs& a, const GroupLane& L, bool act, const uint32_t* w, uint32_t rbase,
-                          uint32_t* seen, int lane) {
+                          uint32_t* seen, uint32_t* tring, uint32_t* wring, int lane) {
 #pragma unroll
     for (int i = 0; i < 8; i++) seen[i * 32 + lane] = 0u;
     __syncwarp();
@@ -430,12 +526,20 @@ __device__ void conn_lane(const DecodeArgs& a, const GroupLane& L, bool act, con
     const uint32_t n_tris = L.d.counts0 >> 16;
     const uint32_t ib = max(1u, 32u - __clz(n_local));
     const uint32_t end = L.d.end_bit;
-    uint32_t* tri_out = a.idx + 3ull * L.t_base;
     uint32_t* walk_out = a.walk_scratch + L.wp_base;
     // triangle indices are relative to the mesh's first vertex
     const uint32_t vloc = act ? static_cast<uint32_t>(L.v_base - L.P->v_offset) : 0u;
-    const uint32_t t0odd = static_cast<uint32_t>(L.t_base) & 1u;  // parity of the first triangle's index
-    uint32_t cpos = L.d.start_bit + 48u;
+    const uint32_t ph = static_cast<uint32_t>(L.t_base) & 3u;  // ring slot of triangle 0
+    uint32_t* tr = tring + lane * kRingRow;
+    uint32_t* wr = wring + lane * kRingRow;
+    uint32_t tf = 0u, wf = 0u;  // entries already written out
+    uint32_t flush_in = kFlushEvery;
+    BitWin<kShared> win;  // the token cursor (win.pos)
+    win.w = w;
+    win.rbase = rbase;
+    win.pos = win.w0 = win.w1 = win.w2 = 0u;
+    // only an active lane's bits are in the stage: an inactive lane reads nothing
+    if (act) win.seek(L.d.start_bit + 48u);
     uint32_t strips_left = L.d.n_strips;
     uint32_t tok_left = 0u, tok_idx = 0u, tris = 0u;
     uint32_t p0 = 0u, p1 = 0u, p2 = 0u;
@@ -450,7 +554,8 @@ __device__ void conn_lane(const DecodeArgs& a, const GroupLane& L, bool act, con
         if (running) {
             // a 32-bit window holds a strip header (16 bits) plus the next
             // token (at most 1 + 9 bits), or an edge code plus a token
-            const uint32_t x0 = peek32<kShared>(w, cpos + rbase);
+            const uint32_t x0 = win.peek();
+            uint32_t used = 0u;  // bits consumed by this iteration (at most 16 + 1 + 1 + 9)
             const bool hdr = tok_left == 0u;  // strip header (paradelta_v5_dup.py:519)
             const uint32_t len = x0 >> 16;
             const uint32_t sbody = len > 1u ? len - 1u : 0u;
@@ -458,16 +563,16 @@ __device__ void conn_lane(const DecodeArgs& a, const GroupLane& L, bool act, con
             tok_idx = hdr ? 0u : tok_idx;
             strips_left -= hdr ? 1u : 0u;
             tris += hdr ? 1u + sbody : 0u;
-            cpos += hdr ? 16u : 0u;
+            used += hdr ? 16u : 0u;
             uint32_t x = hdr ? (x0 << 16) : x0;
             const bool body = tok_idx >= 3u;
             const uint32_t ec = x >> 31;  // edge code of a strip-body token (:528)
             x = body ? (x << 1) : x;
-            cpos += body ? 1u : 0u;
+            used += body ? 1u : 0u;
             const bool raw = (x >> 31) != 0u;
             const uint32_t rid = (x << 1) >> (32u - ib);
             const uint32_t fi = (x << 1) >> 27;
-            cpos += raw ? 1u + ib : 6u;
+            used += raw ? 1u + ib : 6u;
             // decode_dup raises IndexError on both (FIFO index, local id)
             const bool invalid = (raw ? rid >= n_local : fi >= fifo.len) | (tris > n_tris);
             const uint32_t v = raw ? (rid & 0xFFu) : fifo.at((16u - fifo.len + fi) & 15u);
@@ -483,9 +588,9 @@ __device__ void conn_lane(const DecodeArgs& a, const GroupLane& L, bool act, con
             p0 = q0;
             p1 = q1;
             p2 = q2;
-            // triangle -> output, as global vertex ids
+            // triangle -> ring
             const bool emit = (body | (tok_idx == 2u)) & !invalid;
-            if (emit) store_tri(tri_out, tcnt, ((t0odd + tcnt) & 1u) != 0u, vloc + q0, vloc + q1, vloc + q2);
+            if (emit) tr[(ph + tcnt) & 31u] = q0 | (q1 << 8) | (q2 << 16);
             tcnt += emit ? 1u : 0u;
             // first occurrence -> next walk entry (:523-541).  Roots are 'none'
             // (stored as v,v,v,v); strip bodies 'para' with (a, b, c) = (p0, p1, cref).
@@ -495,20 +600,31 @@ __device__ void conn_lane(const DecodeArgs& a, const GroupLane& L, bool act, con
             const bool isnew = ((sw & bit) == 0u) & !invalid;
             if (isnew) *sp = sw | bit;
             const uint32_t e = body ? (v | (q0 << 8) | (q1 << 16) | (cref << 24)) : v * 0x01010101u;
-            if (isnew) walk_out[wcnt] = e;
+            if (isnew) wr[wcnt & 31u] = e;
             wcnt += isnew ? 1u : 0u;
             kind0 += (isnew & !body) ? 1u : 0u;
             tok_idx++;
             tok_left--;
-            bad = bad | invalid | (cpos > end);
+            win.advance(used);
+            bad = bad | invalid | (win.pos > end);
             running = !bad & ((tok_left | strips_left) != 0u);
         }
+        if (--flush_in == 0u) {  // warp-uniform
+            flush_in = kFlushEvery;
+            if (act) {
+                flush_tris(a.idx, L.t_base, tr, tf, tcnt, vloc, false);
+                flush_walk(walk_out, wr, wf, wcnt, false);
+            }
+        }
     }
+    __syncwarp();
     if (act) {
+        flush_tris(a.idx, L.t_base, tr, tf, tcnt, vloc, true);
+        flush_walk(walk_out, wr, wf, wcnt, true);
         if (bad || tris != n_tris) {
             report(a.status, kErrCorrupt, L.m);
         } else {
-            a.descs[L.m].anchor_bit = cpos;
+            a.descs[L.m].anchor_bit = win.pos;
             a.descs[L.m].walk = kind0 | (wcnt << 16);
         }
     }
@@ -523,7 +639,9 @@ __global__ void __launch_bounds__(W * 32) conn_kernel(DecodeArgs a, uint32_t sta
     uint8_t* base = smem + warp * conn_warp_bytes(stage_bytes);
     uint32_t* stage = reinterpret_cast<uint32_t*>(base);
     uint32_t* seen = reinterpret_cast<uint32_t*>(base + align16(stage_bytes + 32u));
-    uint64_t* bar = reinterpret_cast<uint64_t*>(seen + 8 * 32);
+    uint32_t* tring = seen + 8 * 32;
+    uint32_t* wring = tring + 32 * kRingRow;
+    uint64_t* bar = reinterpret_cast<uint64_t*>(wring + 32 * kRingRow);
     if (lane == 0) mbar_init(bar);
     __syncwarp();
     uint32_t phase = 0u;
@@ -569,10 +687,11 @@ __global__ void __launch_bounds__(W * 32) conn_kernel(DecodeArgs a, uint32_t sta
                     return;
                 }
                 phase ^= 1u;
-                conn_lane<true>(a, L, act, stage, static_cast<uint32_t>(L.blob_off * 8ull - s0 * 8ull), seen, lane);
+                conn_lane<true>(a, L, act, stage, static_cast<uint32_t>(L.blob_off * 8ull - s0 * 8ull), seen, tring, wring,
+                                lane);
             } else {
                 conn_lane<false>(a, L, act, reinterpret_cast<const uint32_t*>(a.arena + L.blob_off), 0u, seen,
-                                 lane);
+                                 tring, wring, lane);
             }
             __syncwarp();
         }
@@ -591,16 +710,10 @@ __global__ void __launch_bounds__(W * 32) conn_kernel(DecodeArgs a, uint32_t sta
 template <bool kWide>
 using PlaneT = typename std::conditional<kWide, int32_t, uint16_t>::type;
 
-__device__ __forceinline__ float dequant_value(const float* c, const MeshParams* P, uint32_t axis, uint32_t q) {
-    if (__float_as_uint(c[6])) return c[5];
-    stride_dequant_axis t;
-    t.a_hi = c[0];
-    t.a_lo = c[1];
-    t.b_hi = c[2];
-    t.b_lo = c[3];
-    t.err = c[4];
-    float y;
-    if (stride_dequant_fast(&t, q, &y)) return y;
+// Exact float64 evaluation for the codes whose float-float result is too
+// close to a float32 rounding boundary (well under 1 in 1000): out of line,
+// so the common path stays short and branch-free.
+__device__ __noinline__ float dequant_slow(const MeshParams* P, uint32_t axis, uint32_t q) {
     return stride_dequant_exact(&P->dq[axis], q);
 }
 
@@ -641,19 +754,27 @@ __device__ __forceinline__ bool skip_codes(const uint32_t* w, uint32_t rbase, ui
     const uint32_t k = tk & 0x3Fu;
     const bool eg = (tk & 0x80u) != 0u;
     bool ok = true;
+    BitWin<kShared> b;
+    b.w = w;
+    b.rbase = rbase;
+    b.seek(pos);
     for (uint32_t i = 0; i < n; i++) {
-        const uint32_t x = peek32<kShared>(w, pos + rbase);
+        const uint32_t x = b.peek();
         const uint32_t z = __clz(x);
         const uint32_t len = z + 1u + (eg ? z : 0u) + k;
-        uint32_t np = pos + len;
-        if (x == 0u) {
-            uint32_t u;
-            np = pos;
+        if (len <= 32u) {
+            b.advance(len);
+        } else {  // prefix or value beyond the window: general reader
+            uint32_t u, np = b.pos;
             ok = ok & (read_code<kShared>(w, rbase, np, tk, limit, u) == 0);
+            b.seek(min(np, limit));
         }
-        ok = ok & (np <= limit);
-        pos = min(np, limit);
+        if (b.pos > limit) {  // only a corrupt stream runs past its meshlet
+            ok = false;
+            b.seek(limit);
+        }
     }
+    pos = b.pos;
     return ok;
 }
 
@@ -779,11 +900,11 @@ __device__ __forceinline__ void vert_axis(const DecodeArgs& a, const GroupLane& 
 }
 
 // Axis d of every vertex of the round's meshlets -> positions (and codes),
-// the warp working through one meshlet at a time.
+// the warp working through one meshlet at a time.  The mesh's dequantisation
+// constants sit in registers for the whole meshlet.
 template <bool kWide>
 __device__ void emit_axis(const DecodeArgs& a, const GroupLane& L, uint32_t rmask, const uint8_t* planes,
-                          uint32_t code_off, uint32_t d, float* dqc, int lane) {
-    uint32_t cached = 0xFFFFFFFFu;
+                          uint32_t code_off, uint32_t d, int lane) {
     for (uint32_t mm = rmask; mm; mm &= mm - 1u) {
         const int j = __ffs(mm) - 1;
         const uint32_t nv = __shfl_sync(kFull, L.d.counts0, j) & 0xFFFFu;
@@ -791,17 +912,29 @@ __device__ void emit_axis(const DecodeArgs& a, const GroupLane& L, uint32_t rmas
         const uint32_t off = __shfl_sync(kFull, code_off, j);
         const uint32_t mj = __shfl_sync(kFull, L.mi, j);
         const MeshParams* Pj = a.meshes + mj;
-        if (mj != cached) {
-            __syncwarp();
-            if (lane < 8) dqc[lane] = reinterpret_cast<const float*>(&Pj->dq[d])[lane];
-            __syncwarp();
-            cached = mj;
-        }
+        stride_dequant_axis c;
+        c.a_hi = __ldg(&Pj->dq[d].a_hi);
+        c.a_lo = __ldg(&Pj->dq[d].a_lo);
+        c.b_hi = __ldg(&Pj->dq[d].b_hi);
+        c.b_lo = __ldg(&Pj->dq[d].b_lo);
+        c.err = __ldg(&Pj->dq[d].err);
+        const bool zero_bits = __ldg(&Pj->dq[d].zero_bits) != 0;
         const PlaneT<kWide>* pj = reinterpret_cast<const PlaneT<kWide>*>(planes + off);
         float* dst = a.pos + 3ull * vb + d;
-        for (uint32_t v = lane; v < nv; v += 32u) {
-            const uint32_t q = static_cast<uint32_t>(pj[v]);
-            dst[3u * v] = dequant_value(dqc, Pj, d, q);
+        if (__ldg(&Pj->has_lut)) {  // warp-uniform: the mesh has per-code tables
+            const uint32_t g0 = __ldg(&Pj->g_bits[0]), g1 = __ldg(&Pj->g_bits[1]), gd = __ldg(&Pj->g_bits[d]);
+            const float* lut = a.lut + __ldg(&Pj->lut_off) + (d >= 1u ? 1u << g0 : 0u) + (d >= 2u ? 1u << g1 : 0u);
+            const uint32_t qmax = (1u << gd) - 1u;  // codes of a corrupt stream may lie outside; it is rejected
+            for (uint32_t v = lane; v < nv; v += 32u)
+                dst[3u * v] = __ldg(lut + min(static_cast<uint32_t>(pj[v]), qmax));
+        } else {
+            for (uint32_t v = lane; v < nv; v += 32u) {
+                const uint32_t q = static_cast<uint32_t>(pj[v]);
+                float y;
+                const bool fast = stride_dequant_fast(&c, q, &y) != 0;
+                if (!fast || zero_bits) y = dequant_slow(Pj, d, q);
+                dst[3u * v] = y;
+            }
         }
         if (a.codes) {
             int32_t* cdst = a.codes + 3ull * vb + d;
@@ -816,7 +949,7 @@ __device__ void emit_axis(const DecodeArgs& a, const GroupLane& L, uint32_t rmas
 template <bool kShared, bool kWide>
 __device__ __forceinline__ void vert_round(const DecodeArgs& a, const GroupLane& L, uint32_t d, bool act,
                                            uint32_t rmask, const uint32_t* w, uint32_t rbase, uint8_t* planes,
-                                           uint32_t code_off, float* dqc, int lane) {
+                                           uint32_t code_off, int lane) {
     VertLane S;
     S.bad = false;
     S.cp = 0u;
@@ -824,7 +957,7 @@ __device__ __forceinline__ void vert_round(const DecodeArgs& a, const GroupLane&
     PlaneT<kWide>* plane = reinterpret_cast<PlaneT<kWide>*>(planes + code_off);
     if (act && !S.bad) vert_axis<kShared, kWide>(a, L, d, w, rbase, plane, S);
     __syncwarp();
-    emit_axis<kWide>(a, L, rmask, planes, code_off, d, dqc, lane);
+    emit_axis<kWide>(a, L, rmask, planes, code_off, d, lane);
     if (act) {
         // pz, the last substream, must end where the next meshlet starts (:507)
         const MeshParams* P = L.P;
@@ -848,7 +981,6 @@ __global__ void __launch_bounds__(96, 1) vert_kernel(DecodeArgs a, uint32_t stag
     const uint32_t vstage = vert_stage_bytes(stage_bytes);
     uint32_t* stage = reinterpret_cast<uint32_t*>(smem);
     uint8_t* planes = smem + align16(vstage + 32u) + d * vert_axis_bytes(code_bytes);
-    float* dqc = reinterpret_cast<float*>(planes + align16(code_bytes));
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem + align16(vstage + 32u) + 3u * vert_axis_bytes(code_bytes));
     if (threadIdx.x == 0) mbar_init(bar);
     __syncthreads();
@@ -917,11 +1049,11 @@ __global__ void __launch_bounds__(96, 1) vert_kernel(DecodeArgs a, uint32_t stag
                 }
                 phase ^= 1u;
                 const uint32_t rbase = static_cast<uint32_t>(L.blob_off * 8ull - src16 * 8ull + dst_off * 8ull);
-                vert_round<true, kWide>(a, L, d, act, rmask, stage, rbase, planes, code_off, dqc, lane);
+                vert_round<true, kWide>(a, L, d, act, rmask, stage, rbase, planes, code_off, lane);
             } else {
                 vert_round<false, kWide>(a, L, d, act, rmask,
                                          reinterpret_cast<const uint32_t*>(a.arena + L.blob_off), 0u, planes,
-                                         code_off, dqc, lane);
+                                         code_off, lane);
             }
             __syncthreads();  // the next round overwrites the stage
         }
@@ -1054,6 +1186,11 @@ int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void
     if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[0]), s);
     if (a.total_meshlets != 0) {
         scan_kernel<<<scan_blocks(a.total_meshlets), kScanThreads, 0, s>>>(a);
+        if (cudaGetLastError() != cudaSuccess) return STRIDE_ERR_CUDA;
+    }
+    if (a.n_lut_meshes != 0) {
+        const dim3 grid((a.lut_max + 255u) / 256u, a.n_lut_meshes);
+        lut_kernel<<<grid, 256, 0, s>>>(a);
         if (cudaGetLastError() != cudaSuccess) return STRIDE_ERR_CUDA;
     }
     if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[1]), s);

@@ -106,10 +106,11 @@ class Arena {
 
 // Device scratch of one launch over these totals (arena bytes).
 struct ScratchPlan {
-    uint64_t params, map, descs, sums, prefix, walk, status, total;
+    uint64_t params, map, lut_list, descs, sums, prefix, walk, lut, status, total;
 };
 
-ScratchPlan plan_scratch(uint32_t n_meshes, uint32_t meshlets, uint64_t n_v) {
+// lut_floats: dequantisation table floats of the launch's meshes
+ScratchPlan plan_scratch(uint32_t n_meshes, uint32_t meshlets, uint64_t n_v, uint64_t lut_floats) {
     ScratchPlan s;
     const uint32_t nb = std::max<uint32_t>(1u, scan_blocks(meshlets));
     uint64_t o = 0;
@@ -117,6 +118,8 @@ ScratchPlan plan_scratch(uint32_t n_meshes, uint32_t meshlets, uint64_t n_v) {
     o += up(sizeof(MeshParams) * n_meshes);
     s.map = o;
     o += up(4ull * std::max<uint32_t>(1u, meshlets));
+    s.lut_list = o;
+    o += up(4ull * n_meshes);
     s.descs = o;
     o += up(sizeof(MeshletDesc) * std::max<uint32_t>(1u, meshlets));
     s.sums = o;
@@ -125,6 +128,8 @@ ScratchPlan plan_scratch(uint32_t n_meshes, uint32_t meshlets, uint64_t n_v) {
     o += up(sizeof(BlockPrefix) * nb);
     s.walk = o;
     o += up(4ull * walk_scratch_words(n_v, meshlets));
+    s.lut = o;
+    o += up(4ull * lut_floats);
     s.status = o;
     o += up(sizeof(Status));
     s.total = o;
@@ -195,6 +200,7 @@ struct stride_server {
     std::vector<Pinned> pinned_pool;
     uint64_t next_id = 1, launches = 0, completed = 0, seq = 0;
     std::atomic<bool> stop{false};
+    bool hold = false;                    // queue without dispatching (stride_server_hold)
 
     std::mutex cb_mu;                     // completion list + wake-ups only
     std::condition_variable cb_cv;
@@ -255,7 +261,7 @@ void pinned_put(stride_server* s, Pinned& p) {
 
 // Arena bytes one request needs when it runs alone.
 uint64_t footprint(const MeshParams& p, size_t len) {
-    return up(blob_alloc_bytes(len)) + out_bytes(p.n_v, p.n_t) + plan_scratch(1, p.n_meshlets, p.n_v).total;
+    return up(blob_alloc_bytes(len)) + out_bytes(p.n_v, p.n_t) + plan_scratch(1, p.n_meshlets, p.n_v, lut_entries(p)).total;
 }
 
 void finish_request(stride_server* s, Request* r, int status) {
@@ -332,7 +338,7 @@ bool dispatch(stride_server* s, int slot_i) {
     const uint32_t max_batch = s->opts.max_batch ? s->opts.max_batch : 256u;
     // take requests in arrival order while payload, outputs and scratch fit
     std::vector<Request*> take;
-    uint64_t tv = 0, tt = 0;
+    uint64_t tv = 0, tt = 0, tl = 0;
     uint32_t tm = 0;
     for (Request* r : s->queue) {
         if (take.size() >= max_batch) break;
@@ -342,7 +348,7 @@ bool dispatch(stride_server* s, int slot_i) {
         // outputs + scratch for the launch with this request in it
         const uint64_t need = out_bytes(tv + r->p.n_v, tt + r->p.n_t) +
                               plan_scratch(static_cast<uint32_t>(take.size() + 1), tm + r->p.n_meshlets,
-                                           tv + r->p.n_v).total;
+                                           tv + r->p.n_v, tl + lut_entries(r->p)).total;
         uint64_t probe = 0;
         if (!s->arena.alloc(need, &probe)) {
             s->arena.release(off, blob_alloc_bytes(r->data.size()));
@@ -355,9 +361,10 @@ bool dispatch(stride_server* s, int slot_i) {
         tv += r->p.n_v;
         tt += r->p.n_t;
         tm += r->p.n_meshlets;
+        tl += lut_entries(r->p);
     }
     if (take.empty()) return false;
-    const ScratchPlan sp = plan_scratch(static_cast<uint32_t>(take.size()), tm, tv);
+    const ScratchPlan sp = plan_scratch(static_cast<uint32_t>(take.size()), tm, tv, tl);
     l->out_size = out_bytes(tv, tt);
     l->scratch_size = sp.total;
     // the probe above reserved nothing, so allocate for real (cannot fail:
@@ -399,8 +406,13 @@ bool dispatch(stride_server* s, int slot_i) {
         t += p.n_t;
         m += p.n_meshlets;
     }
-    // stage: mesh table | meshlet->mesh map | payloads
-    size_t stage_bytes = up(sizeof(MeshParams) * take.size()) + up(4ull * std::max<uint32_t>(1u, tm));
+    uint32_t n_lut = 0, lut_max = 0;
+    std::vector<uint32_t> lut_list(take.size());
+    plan_luts(params.data(), static_cast<uint32_t>(take.size()), lut_list.data(),
+              static_cast<uint32_t>(take.size()), &n_lut, &lut_max);
+    // stage: mesh table | meshlet->mesh map | table mesh list | payloads
+    const size_t list_off = up(sizeof(MeshParams) * take.size()) + up(4ull * std::max<uint32_t>(1u, tm));
+    size_t stage_bytes = list_off + up(4ull * take.size());
     for (Request* r : take) stage_bytes += up(r->data.size());
     if (slot.stage.bytes < stage_bytes) {
         pinned_put(s, slot.stage);  // idle: the slot's previous launch has retired
@@ -418,7 +430,8 @@ bool dispatch(stride_server* s, int slot_i) {
     for (size_t i = 0; i < take.size(); i++)
         std::fill(hmap + params[i].meshlet_begin, hmap + params[i].meshlet_begin + params[i].n_meshlets,
                   static_cast<uint32_t>(i));
-    uint8_t* hp = reinterpret_cast<uint8_t*>(hmap) + up(4ull * std::max<uint32_t>(1u, tm));
+    std::memcpy(hs + list_off, lut_list.data(), 4ull * n_lut);
+    uint8_t* hp = hs + list_off + up(4ull * take.size());
     cudaStream_t st = slot.stream;
     uint8_t* base = s->d_arena;
     uint8_t* sc = base + l->scratch_off;
@@ -426,6 +439,8 @@ bool dispatch(stride_server* s, int slot_i) {
     e = cudaMemcpyAsync(sc + sp.params, hs, sizeof(MeshParams) * take.size(), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess && tm)
         e = cudaMemcpyAsync(sc + sp.map, hmap, 4ull * tm, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess && n_lut)
+        e = cudaMemcpyAsync(sc + sp.lut_list, hs + list_off, 4ull * n_lut, cudaMemcpyHostToDevice, st);
     for (Request* r : take) {
         if (e != cudaSuccess) break;
         std::memcpy(hp, r->data.data(), r->data.size());
@@ -450,6 +465,10 @@ bool dispatch(stride_server* s, int slot_i) {
         a.idx = reinterpret_cast<uint32_t*>(base + l->out_off);
         a.pos = reinterpret_cast<float*>(base + l->out_off + up(12ull * tt));
         a.codes = nullptr;
+        a.lut = reinterpret_cast<float*>(sc + sp.lut);
+        a.lut_meshes = reinterpret_cast<const uint32_t*>(sc + sp.lut_list);
+        a.n_lut_meshes = n_lut;
+        a.lut_max = lut_max;
         a.wide_codes = false;
         for (const MeshParams& p : params)
             a.wide_codes = a.wide_codes || p.g_bits[0] > 16 || p.g_bits[1] > 16 || p.g_bits[2] > 16;
@@ -520,7 +539,7 @@ void scheduler_main(stride_server* s) {
             continue;
         }
         // fill every idle stream while the queue admits something
-        for (size_t i = 0; i < s->slots.size() && !s->queue.empty(); i++) {
+        for (size_t i = 0; i < s->slots.size() && !s->queue.empty() && !s->hold; i++) {
             if (s->slots[i].busy) continue;
             if (!dispatch(s, static_cast<int>(i))) break;
         }
@@ -637,6 +656,16 @@ int stride_server_release(stride_server* s, uint64_t req_id) {
             r->launch.reset();
         }
         s->reqs.erase(it);
+    }
+    notify_scheduler(s);
+    return STRIDE_OK;
+}
+
+int stride_server_hold(stride_server* s, int hold) {
+    if (!s) return fail(STRIDE_ERR_ARG, "null server");
+    {
+        std::lock_guard<std::mutex> g(s->mu);
+        s->hold = hold != 0;
     }
     notify_scheduler(s);
     return STRIDE_OK;

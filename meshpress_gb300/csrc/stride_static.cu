@@ -58,7 +58,7 @@ int static_scratch(uint8_t** out) {
 size_t up256(size_t x) { return (x + 255) & ~static_cast<size_t>(255); }
 
 struct StaticLayout {
-    size_t blob, params, descs, sums, prefix, walk, status, total;
+    size_t blob, params, lut_list, descs, sums, prefix, walk, lut, status, total;
 };
 
 StaticLayout plan(size_t len, const MeshParams& p) {
@@ -68,6 +68,8 @@ StaticLayout plan(size_t len, const MeshParams& p) {
     o += up256(blob_alloc_bytes(len));
     L.params = o;
     o += up256(sizeof(MeshParams));
+    L.lut_list = o;
+    o += up256(sizeof(uint32_t));
     L.descs = o;
     o += up256(sizeof(MeshletDesc) * p.n_meshlets);
     L.sums = o;
@@ -76,6 +78,8 @@ StaticLayout plan(size_t len, const MeshParams& p) {
     o += up256(sizeof(BlockPrefix) * scan_blocks(p.n_meshlets));
     L.walk = o;
     o += up256(4ull * walk_scratch_words(p.n_v, p.n_meshlets));
+    L.lut = o;
+    o += up256(4ull * lut_entries(p));
     L.status = o;
     o += up256(sizeof(Status));
     L.total = o;
@@ -92,6 +96,8 @@ extern "C" int stride_decode_static(const uint8_t* data, size_t len, void* strea
     char why[256] = {0};
     int rc = parse_header(data, len, &p, why, sizeof(why));
     if (rc) return fail(rc, "%s", why);
+    uint32_t n_lut = 0, lut_max = 0;
+    plan_luts(&p, 1, nullptr, 1, &n_lut, &lut_max);
     const StaticLayout L = plan(len, p);
     if (L.total > kStaticScratchBytes)
         return fail(STRIDE_ERR_NOMEM,
@@ -109,7 +115,8 @@ extern "C" int stride_decode_static(const uint8_t* data, size_t len, void* strea
     // so `data` and `p` may go away afterwards
     if ((e = cudaMemcpyAsync(base + L.blob, data, len, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
         (e = cudaMemsetAsync(base + L.blob + len, 0, kBlobPad, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(base + L.params, &p, sizeof(p), cudaMemcpyHostToDevice, s)) != cudaSuccess)
+        (e = cudaMemcpyAsync(base + L.params, &p, sizeof(p), cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(base + L.lut_list, 0, sizeof(uint32_t), s)) != cudaSuccess)
         return cuda_fail(e, "stride_decode_static upload");
     DecodeArgs a;
     a.arena = base + L.blob;
@@ -127,6 +134,10 @@ extern "C" int stride_decode_static(const uint8_t* data, size_t len, void* strea
     a.pos = d_pos;
     a.codes = nullptr;
     a.wide_codes = p.g_bits[0] > 16 || p.g_bits[1] > 16 || p.g_bits[2] > 16;
+    a.lut = reinterpret_cast<float*>(base + L.lut);
+    a.lut_meshes = reinterpret_cast<const uint32_t*>(base + L.lut_list);
+    a.n_lut_meshes = n_lut;
+    a.lut_max = lut_max;
     LaunchCfg cfg;
     if (a.wide_codes) cfg.code_bytes = kMaxLocal * 4u > cfg.code_bytes ? kMaxLocal * 4u : cfg.code_bytes;
     rc = enqueue_decode(a, cfg, stream);

@@ -102,6 +102,10 @@ class DecodeServer:
         """Free the request's results (views from ``wait`` become invalid)."""
         _lib.check(self._lib.stride_server_release(self._h, int(req_id)), "release")
 
+    def hold(self, on: bool = True):
+        """Queue submissions without launching them until ``hold(False)``."""
+        _lib.check(self._lib.stride_server_hold(self._h, int(bool(on))), "hold")
+
     def stats(self) -> dict:
         a, b, c = ctypes.c_uint64(), ctypes.c_uint64(), ctypes.c_uint64()
         _lib.check(self._lib.stride_server_stats(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))

@@ -58,8 +58,10 @@ def test_alone_equals_mix(torch_cuda, pool):
             r = srv.wait(rid)
             _same(torch, r, t, v)
             srv.release(rid)
-    # mix: three threads submit the pool twice over, interleaved
+    # mix: three threads submit the pool twice over, interleaved; the first
+    # half is queued behind a hold so that launches certainly share requests
     with DecodeServer(512 << 20, n_streams=3, max_batch=6) as srv:
+        srv.hold(True)
         ids = {}
         lock = threading.Lock()
 
@@ -69,12 +71,15 @@ def test_alone_equals_mix(torch_cuda, pool):
                 with lock:
                     ids[rid] = j % len(pool)
                 time.sleep(0.0005 * (j % 4))
+                if k == 0 and j >= len(pool):
+                    srv.hold(False)
 
         th = [threading.Thread(target=feed, args=(k,)) for k in range(3)]
         for x in th:
             x.start()
         for x in th:
             x.join()
+        srv.hold(False)
         for rid, j in sorted(ids.items()):
             r = srv.wait(rid, timeout_ms=60000)
             _same(torch, r, pool[j][1], pool[j][2])
