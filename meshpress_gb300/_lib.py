@@ -45,7 +45,7 @@ class StrideInfo(ctypes.Structure):
     _fields_ = [("n_meshlets", ctypes.c_uint32), ("g_bits", ctypes.c_uint32 * 3),
                 ("n_v", ctypes.c_uint64), ("n_t", ctypes.c_uint64), ("nbytes", ctypes.c_uint64),
                 ("center", ctypes.c_float * 3), ("scale", ctypes.c_float),
-                ("pred_n", ctypes.c_int32 * 9), ("pred_k", ctypes.c_int32 * 3)]
+                ("pred_n", ctypes.c_int32 * 9), ("pred_k", ctypes.c_int32 * 3), ("kernels", ctypes.c_uint32)]
 
 
 class LaunchCfg(ctypes.Structure):

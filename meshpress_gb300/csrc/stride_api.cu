@@ -303,6 +303,7 @@ static void fill_info(const MeshParams& p, size_t len, stride_info_t* info) {
     info->n_v = p.n_v;
     info->n_t = p.n_t;
     info->nbytes = len;
+    info->kernels = p.n_meshlets ? (lut_entries(p) ? 4u : 3u) : (lut_entries(p) ? 1u : 0u);
 }
 
 int stride_inspect(const uint8_t* data, size_t len, stride_info_t* info) {

@@ -71,3 +71,16 @@ def test_decoder_fails_loudly_without_library(monkeypatch):
     monkeypatch.setattr(_lib, "_lib", None)
     with pytest.raises(RuntimeError):
         _lib.load()
+
+
+def test_kernel_count_reports_dequantisation_tables(built_libs):
+    """Meshes with at least half as many duplicated vertices as codes (all
+    axes) decode with per-code tables: one more kernel launch."""
+    big = _golden.load("grid129_b12")["data"]     # 12-bit codes, ~20 K vertices: tables
+    small = _golden.load("grid9_b12")["data"]     # 128 triangles: direct evaluation
+    wide = _golden.load("grid17_canon_b16")["data"]
+    assert _lib.inspect(big).kernels == 4
+    assert _lib.inspect(small).kernels == 3
+    info = _lib.inspect(wide)
+    entries = sum(1 << g for g in info.g_bits)
+    assert info.kernels == (4 if entries <= 2 * info.n_v else 3)
