@@ -65,11 +65,16 @@ typedef struct {
 
 /* Launch shape of the decode kernel (the autotuner's search space). */
 typedef struct {
-    int32_t warps_per_cta;   /* warps (32 meshlets each) per CTA: 1, 2 or 4   */
-    int32_t persistent;      /* 1 = persistent work-stealing grid            */
-    int32_t ctas_per_sm;     /* persistent grid = ctas_per_sm * SMs (0 = 4)   */
-    uint32_t stage_bytes;    /* per-warp shared-memory payload staging       */
-    uint32_t code_bytes;     /* per-warp shared-memory integer-code storage  */
+    int32_t warps_per_cta;   /* 1, 2 or 4: connectivity kernel CTAs hold one
+                                (1, 2) or two (4) parser/assembler warp pairs
+                                of 32 meshlets each; the vertex kernel's CTA is
+                                always three warps (one per axis)            */
+    int32_t persistent;      /* 1 = persistent work-stealing vertex grid     */
+    int32_t ctas_per_sm;     /* persistent grid = ctas_per_sm * SMs
+                                (0 = as many as fit)                         */
+    uint32_t stage_bytes;    /* shared-memory staging of a group's bytes
+                                (the vertex kernel stages half of this)      */
+    uint32_t code_bytes;     /* shared-memory code plane of one axis warp    */
 } stride_launch_cfg;
 
 /* Thread-local description of the last error in this thread. */

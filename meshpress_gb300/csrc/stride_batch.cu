@@ -330,7 +330,7 @@ int stride_batch_autotune(stride_batch* b, void* stream, uint32_t* d_idx, float*
     const uint32_t stage_opts[] = {8u * 1024u, 12u * 1024u, 16u * 1024u, 24u * 1024u};
     // code plane per warp: 2 bytes per vertex (4 above 16-bit codes), 32
     // meshlets of up to 256 vertices fill 16 KiB
-    const uint32_t code_opts[] = {6u * 1024u, 8u * 1024u, 12u * 1024u, 16u * 1024u};
+    const uint32_t code_opts[] = {6u * 1024u, 8u * 1024u, 10u * 1024u, 12u * 1024u, 16u * 1024u};
     for (int w : {1, 2, 4})
         for (uint32_t st : stage_opts)
             for (uint32_t cb : code_opts)

@@ -100,7 +100,7 @@ struct Status {
 };
 
 struct LaunchCfg {
-    int warps_per_cta = 2;
+    int warps_per_cta = 4;
     int persistent = 1;
     int ctas_per_sm = 0;
     uint32_t stage_bytes = 16 * 1024;  // per-warp payload staging (vertex kernel: half)

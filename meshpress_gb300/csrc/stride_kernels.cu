@@ -152,6 +152,19 @@ struct BitWin {
 };
 
 // ---------------------------------------------------------------------------
+// Named barriers between specific warps of a CTA (producer arrives,
+// consumer waits); `threads` counts both sides.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void named_arrive(uint32_t id, uint32_t threads) {
+    __threadfence_block();  // shared-memory writes before the arrive are visible to the waiting warps
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+
+__device__ __forceinline__ void named_sync(uint32_t id, uint32_t threads) {
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+
+// ---------------------------------------------------------------------------
 // Bulk-copy staging (TMA bulk, no tensor map) and its mbarrier.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t smem_addr(const void* p) {
@@ -453,10 +466,13 @@ __global__ void __launch_bounds__(256) lut_kernel(DecodeArgs a) {
 // ---------------------------------------------------------------------------
 __host__ __device__ constexpr uint32_t align16(uint32_t x) { return (x + 15u) & ~15u; }
 
-// connectivity warp: stage | first-occurrence bits (8 words per lane) |
-// triangle ring | walk ring | mbarrier
-__host__ __device__ inline uint32_t conn_warp_bytes(uint32_t stage_bytes) {
-    return align16(stage_bytes + 32u) + 8u * 32u * 4u + 2u * 32u * kRingRow * 4u + 16u;
+// connectivity warp pair: stage | token records (two chunks) | chunk counts
+// (4 words) | first-occurrence bits (8 words per lane) | triangle ring |
+// walk ring | mbarrier
+constexpr uint32_t kChunkWords = 16u;  // iterations per chunk (kChunk)
+__host__ __device__ inline uint32_t conn_pair_bytes(uint32_t stage_bytes) {
+    return align16(stage_bytes + 32u) + 2u * kChunkWords * 32u * 4u + 16u + 8u * 32u * 4u +
+           2u * 32u * kRingRow * 4u + 16u;
 }
 
 __host__ __device__ inline uint32_t vert_stage_bytes(uint32_t stage_bytes) { return stage_bytes / 2u; }
@@ -464,7 +480,7 @@ __host__ __device__ inline uint32_t vert_stage_bytes(uint32_t stage_bytes) { ret
 // One axis warp's code plane.
 __host__ __device__ inline uint32_t vert_axis_bytes(uint32_t code_bytes) { return align16(code_bytes); }
 
-// Vertex CTA: residual stage | three axis regions | mbarrier.
+// Vertex CTA: residual stage | three axis planes | mbarrier.
 __host__ __device__ inline uint32_t vert_cta_bytes(uint32_t stage_bytes, uint32_t code_bytes) {
     return align16(vert_stage_bytes(stage_bytes) + 32u) + 3u * vert_axis_bytes(code_bytes) + 16u;
 }
@@ -516,16 +532,115 @@ __device__ __forceinline__ bool placement_ok(const DecodeArgs& a, const GroupLan
     return ok && L.wp_base + ((n_local + 3u) & ~3u) <= a.walk_cap;
 }
 
+// Connectivity as a producer/consumer pair of warps per group of 32
+// meshlets.  The parser warp runs the serial part of every lane's token
+// chain -- bit cursor, strip headers, token widths, the 16-entry FIFO -- and
+// writes one 32-bit record per lane and iteration into a two-chunk ring in
+// shared memory; the assembler warp replays the records: strip state,
+// triangles, first occurrences (walk), output rings.  The two chains run on
+// different warps, so each is about half as long as the fused one.
+//
+// Record: bits 0..7 vertex, bit 8 valid, bit 9 edge code, bits 10..11 token
+// position in its strip (0..2 the three roots, 3 a strip-body token).
+constexpr uint32_t kChunk = kChunkWords;  // iterations per ring chunk
+constexpr uint32_t kChunkDone = 1u << 31;  // count word: the parser has finished
+constexpr uint32_t kChunkAbort = 1u << 30; // count word: the group was abandoned
+
+// Named barrier ids of pair p: full[0], full[1], empty[0], empty[1].
+__device__ __forceinline__ uint32_t bar_full(uint32_t pair, uint32_t c) { return 1u + 4u * pair + c; }
+__device__ __forceinline__ uint32_t bar_empty(uint32_t pair, uint32_t c) { return 3u + 4u * pair + c; }
+
+// Parser warp, one round.  `abort`: the stage never arrived; publish an
+// empty, abandoned round so that the assembler leaves too.
 template <bool kShared>
-__device__ void conn_lane(const DecodeArgs& a, const GroupLane& L, bool act, const uint32_t* w, uint32_t rbase,
-                          uint32_t* seen, uint32_t* tring, uint32_t* wring, int lane) {
-#pragma unroll
-    for (int i = 0; i < 8; i++) seen[i * 32 + lane] = 0u;
-    __syncwarp();
+__device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, const uint32_t* w, uint32_t rbase,
+                           uint32_t* recs, uint32_t* counts, uint32_t pair, bool abort, int lane) {
     const uint32_t n_local = L.d.counts0 & 0xFFFFu;
     const uint32_t n_tris = L.d.counts0 >> 16;
     const uint32_t ib = max(1u, 32u - __clz(n_local));
     const uint32_t end = L.d.end_bit;
+    BitWin<kShared> win;  // the token cursor (win.pos)
+    win.w = w;
+    win.rbase = rbase;
+    win.pos = win.w0 = win.w1 = win.w2 = 0u;
+    // only an active lane's bits are in the stage: an inactive lane reads nothing
+    if (act && !abort) win.seek(L.d.start_bit + 48u);
+    uint32_t strips_left = L.d.n_strips;
+    uint32_t tok_left = 0u, tok_idx = 0u, tris = 0u;
+    Fifo fifo;
+    bool bad = false;
+    bool running = act && !abort && strips_left > 0u;
+    uint32_t k = 0u;  // chunk
+    for (;;) {
+        const uint32_t c = k & 1u;
+        if (k >= 2u) named_sync(bar_empty(pair, c), 64);  // the assembler is done with chunk k - 2
+        uint32_t* rc = recs + c * kChunk * 32u + lane;
+        uint32_t n = 0u;
+        while (n < kChunk && __any_sync(kFull, running)) {
+            uint32_t rec = 0u;
+            if (running) {
+                // a 32-bit window holds a strip header (16 bits) plus the next
+                // token (at most 1 + 9 bits), or an edge code plus a token
+                const uint32_t x0 = win.peek();
+                uint32_t used = 0u;
+                const bool hdr = tok_left == 0u;  // strip header (paradelta_v5_dup.py:519)
+                const uint32_t len = x0 >> 16;
+                const uint32_t sbody = len > 1u ? len - 1u : 0u;
+                tok_left = hdr ? 3u + sbody : tok_left;
+                tok_idx = hdr ? 0u : tok_idx;
+                strips_left -= hdr ? 1u : 0u;
+                tris += hdr ? 1u + sbody : 0u;
+                used += hdr ? 16u : 0u;
+                uint32_t x = hdr ? (x0 << 16) : x0;
+                const bool body = tok_idx >= 3u;
+                const uint32_t ec = x >> 31;  // edge code of a strip-body token (:528)
+                x = body ? (x << 1) : x;
+                used += body ? 1u : 0u;
+                const bool raw = (x >> 31) != 0u;
+                const uint32_t rid = (x << 1) >> (32u - ib);
+                const uint32_t fi = (x << 1) >> 27;
+                used += raw ? 1u + ib : 6u;
+                // decode_dup raises IndexError on both (FIFO index, local id)
+                const bool invalid = (raw ? rid >= n_local : fi >= fifo.len) | (tris > n_tris);
+                const uint32_t v = raw ? (rid & 0xFFu) : fifo.at((16u - fifo.len + fi) & 15u);
+                const uint32_t at = fifo.find(v);
+                const uint32_t rm = at < 16u ? at : (fifo.len >= 15u ? 0u : 15u - fifo.len);
+                fifo.remove_append(rm, v);
+                fifo.len += ((at == 16u) & (fifo.len < 16u)) ? 1u : 0u;
+                rec = invalid ? 0u : (v | 0x100u | ((body ? ec : 0u) << 9) | (min(tok_idx, 3u) << 10));
+                tok_idx++;
+                tok_left--;
+                win.advance(used);
+                bad = bad | invalid | (win.pos > end);
+                running = !bad & ((tok_left | strips_left) != 0u);
+            }
+            rc[n * 32u] = rec;
+            n++;
+        }
+        const bool done = !__any_sync(kFull, running);
+        if (lane == 0) counts[c] = n | (done ? kChunkDone : 0u) | (abort ? kChunkAbort : 0u);
+        named_arrive(bar_full(pair, c), 64);
+        k++;
+        if (done) break;
+    }
+    // take the assembler's remaining chunk releases: the ring and the
+    // barriers are clean for the next round
+    for (uint32_t j = k >= 2u ? k - 2u : 0u; j < k; j++) named_sync(bar_empty(pair, j & 1u), 64);
+    if (act && !abort) {
+        if (bad || tris != n_tris) {
+            report(a.status, kErrCorrupt, L.m);
+        } else {
+            a.descs[L.m].anchor_bit = win.pos;
+        }
+    }
+}
+
+// Assembler warp, one round; returns true when the parser abandoned it.
+__device__ bool conn_assemble(const DecodeArgs& a, const GroupLane& L, bool act, uint32_t* seen, uint32_t* tring,
+                              uint32_t* wring, const uint32_t* recs, const uint32_t* counts, uint32_t pair,
+                              int lane) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) seen[i * 32 + lane] = 0u;
     uint32_t* walk_out = a.walk_scratch + L.wp_base;
     // triangle indices are relative to the mesh's first vertex
     const uint32_t vloc = act ? static_cast<uint32_t>(L.v_base - L.P->v_offset) : 0u;
@@ -534,145 +649,111 @@ __device__ void conn_lane(const DecodeArgs& a, const GroupLane& L, bool act, con
     uint32_t* wr = wring + lane * kRingRow;
     uint32_t tf = 0u, wf = 0u;  // entries already written out
     uint32_t flush_in = kFlushEvery;
-    BitWin<kShared> win;  // the token cursor (win.pos)
-    win.w = w;
-    win.rbase = rbase;
-    win.pos = win.w0 = win.w1 = win.w2 = 0u;
-    // only an active lane's bits are in the stage: an inactive lane reads nothing
-    if (act) win.seek(L.d.start_bit + 48u);
-    uint32_t strips_left = L.d.n_strips;
-    uint32_t tok_left = 0u, tok_idx = 0u, tris = 0u;
-    uint32_t p0 = 0u, p1 = 0u, p2 = 0u;
+    uint32_t P = 0u;  // strip state p0 | p1 << 8 | p2 << 16
     uint32_t tcnt = 0u, wcnt = 0u, kind0 = 0u;
-    Fifo fifo;
-    bool bad = false;
-    bool running = act && strips_left > 0u;
-    // One token per iteration, every lane on the same straight-line path:
-    // the strip header, edge code, vertex kind and walk bookkeeping are all
-    // selects and predicated stores, so lanes never split on them.
-    while (__any_sync(kFull, running)) {
-        if (running) {
-            // a 32-bit window holds a strip header (16 bits) plus the next
-            // token (at most 1 + 9 bits), or an edge code plus a token
-            const uint32_t x0 = win.peek();
-            uint32_t used = 0u;  // bits consumed by this iteration (at most 16 + 1 + 1 + 9)
-            const bool hdr = tok_left == 0u;  // strip header (paradelta_v5_dup.py:519)
-            const uint32_t len = x0 >> 16;
-            const uint32_t sbody = len > 1u ? len - 1u : 0u;
-            tok_left = hdr ? 3u + sbody : tok_left;
-            tok_idx = hdr ? 0u : tok_idx;
-            strips_left -= hdr ? 1u : 0u;
-            tris += hdr ? 1u + sbody : 0u;
-            used += hdr ? 16u : 0u;
-            uint32_t x = hdr ? (x0 << 16) : x0;
-            const bool body = tok_idx >= 3u;
-            const uint32_t ec = x >> 31;  // edge code of a strip-body token (:528)
-            x = body ? (x << 1) : x;
-            used += body ? 1u : 0u;
-            const bool raw = (x >> 31) != 0u;
-            const uint32_t rid = (x << 1) >> (32u - ib);
-            const uint32_t fi = (x << 1) >> 27;
-            used += raw ? 1u + ib : 6u;
-            // decode_dup raises IndexError on both (FIFO index, local id)
-            const bool invalid = (raw ? rid >= n_local : fi >= fifo.len) | (tris > n_tris);
-            const uint32_t v = raw ? (rid & 0xFFu) : fifo.at((16u - fifo.len + fi) & 15u);
-            const uint32_t at = fifo.find(v);
-            const uint32_t rm = at < 16u ? at : (fifo.len >= 15u ? 0u : 15u - fifo.len);
-            fifo.remove_append(rm, v);
-            fifo.len += ((at == 16u) & (fifo.len < 16u)) ? 1u : 0u;
-            // edge code 0 -> (p1, p2 | p0), 1 -> (p0, p2 | p1)  (:530-535)
-            const uint32_t cref = ec ? p1 : p0;
-            const uint32_t q0 = body ? (ec ? p0 : p1) : (tok_idx == 0u ? v : p0);
-            const uint32_t q1 = body ? p2 : (tok_idx == 1u ? v : p1);
-            const uint32_t q2 = (body | (tok_idx == 2u)) ? v : p2;
-            p0 = q0;
-            p1 = q1;
-            p2 = q2;
-            // triangle -> ring
-            const bool emit = (body | (tok_idx == 2u)) & !invalid;
-            if (emit) tr[(ph + tcnt) & 31u] = q0 | (q1 << 8) | (q2 << 16);
-            tcnt += emit ? 1u : 0u;
-            // first occurrence -> next walk entry (:523-541).  Roots are 'none'
-            // (stored as v,v,v,v); strip bodies 'para' with (a, b, c) = (p0, p1, cref).
-            uint32_t* sp = seen + (v >> 5) * 32u + lane;
-            const uint32_t sw = *sp;
-            const uint32_t bit = 1u << (v & 31u);
-            const bool isnew = ((sw & bit) == 0u) & !invalid;
-            if (isnew) *sp = sw | bit;
-            const uint32_t e = body ? (v | (q0 << 8) | (q1 << 16) | (cref << 24)) : v * 0x01010101u;
-            if (isnew) wr[wcnt & 31u] = e;
-            wcnt += isnew ? 1u : 0u;
-            kind0 += (isnew & !body) ? 1u : 0u;
-            tok_idx++;
-            tok_left--;
-            win.advance(used);
-            bad = bad | invalid | (win.pos > end);
-            running = !bad & ((tok_left | strips_left) != 0u);
-        }
-        if (--flush_in == 0u) {  // warp-uniform
-            flush_in = kFlushEvery;
-            if (act) {
-                flush_tris(a.idx, L.t_base, tr, tf, tcnt, vloc, false);
-                flush_walk(walk_out, wr, wf, wcnt, false);
+    bool abort = false;
+    for (uint32_t k = 0u;; k++) {
+        const uint32_t c = k & 1u;
+        named_sync(bar_full(pair, c), 64);
+        const uint32_t cw = counts[c];
+        const uint32_t n = cw & (kChunk | (kChunk - 1u));
+        const uint32_t* rc = recs + c * kChunk * 32u + lane;
+        for (uint32_t i = 0; i < n; i++) {
+            const uint32_t rec = rc[i * 32u];
+            if (rec & 0x100u) {
+                const uint32_t v = rec & 0xFFu;
+                const uint32_t ec = (rec >> 9) & 1u;
+                const uint32_t ti = (rec >> 10) & 3u;
+                const bool body = ti == 3u;
+                // edge code 0 -> (p1, p2 | p0), 1 -> (p0, p2 | p1) (:530-535);
+                // a root token puts v at its position
+                const uint32_t sel = body ? (ec ? 0x7420u : 0x7421u) : (0x7210u + ((4u - ti) << (4u * ti)));
+                const uint32_t cref = ec ? ((P >> 8) & 0xFFu) : (P & 0xFFu);
+                const uint32_t Pn = __byte_perm(P, v, sel);
+                const bool emit = body | (ti == 2u);
+                if (emit) tr[(ph + tcnt) & 31u] = Pn;
+                tcnt += emit ? 1u : 0u;
+                // first occurrence -> next walk entry (:523-541).  Roots are 'none'
+                // (stored as v,v,v,v); strip bodies 'para' with (a, b, c) = (p0, p1, cref).
+                uint32_t* sp = seen + (v >> 5) * 32u + lane;
+                const uint32_t sw = *sp;
+                const uint32_t bit = 1u << (v & 31u);
+                const bool isnew = (sw & bit) == 0u;
+                if (isnew) *sp = sw | bit;
+                const uint32_t e = body ? (v | ((Pn & 0xFFFFu) << 8) | (cref << 24)) : v * 0x01010101u;
+                if (isnew) wr[wcnt & 31u] = e;
+                wcnt += isnew ? 1u : 0u;
+                kind0 += (isnew & !body) ? 1u : 0u;
+                P = Pn;
+            }
+            if (--flush_in == 0u) {  // warp-uniform
+                flush_in = kFlushEvery;
+                if (act) {
+                    flush_tris(a.idx, L.t_base, tr, tf, tcnt, vloc, false);
+                    flush_walk(walk_out, wr, wf, wcnt, false);
+                }
             }
         }
+        named_arrive(bar_empty(pair, c), 64);
+        abort = (cw & kChunkAbort) != 0u;
+        if (cw & kChunkDone) break;
     }
-    __syncwarp();
-    if (act) {
+    if (act && !abort) {
         flush_tris(a.idx, L.t_base, tr, tf, tcnt, vloc, true);
         flush_walk(walk_out, wr, wf, wcnt, true);
-        if (bad || tris != n_tris) {
-            report(a.status, kErrCorrupt, L.m);
-        } else {
-            a.descs[L.m].anchor_bit = win.pos;
-            a.descs[L.m].walk = kind0 | (wcnt << 16);
-        }
+        a.descs[L.m].walk = kind0 | (wcnt << 16);
     }
+    return abort;
 }
 
-template <int W>
-__global__ void __launch_bounds__(W * 32) conn_kernel(DecodeArgs a, uint32_t stage_bytes, int persistent) {
+// Pair p of a CTA (warps 2p and 2p + 1: parser, assembler) decodes group
+// blockIdx.x * G + p.  Past the kernel-entry barrier the pairs never wait
+// for one another, and the two warps of a pair run the same rounds (their
+// descriptors are the same) and the same chunk hand-over.
+template <int G>
+__global__ void __launch_bounds__(G * 64) conn_kernel(DecodeArgs a, uint32_t stage_bytes) {
     extern __shared__ __align__(128) uint8_t smem[];
-    const int warp = threadIdx.x >> 5;
+    const uint32_t pair = threadIdx.x >> 6;
+    const bool parser = ((threadIdx.x >> 5) & 1u) == 0u;
     const int lane = threadIdx.x & 31;
-    if (*reinterpret_cast<volatile unsigned long long*>(&a.status->err) != 0ull) return;
-    uint8_t* base = smem + warp * conn_warp_bytes(stage_bytes);
+    const bool failed = *reinterpret_cast<volatile unsigned long long*>(&a.status->err) != 0ull;
+    if (__syncthreads_or(failed)) return;
+    uint8_t* base = smem + pair * conn_pair_bytes(stage_bytes);
     uint32_t* stage = reinterpret_cast<uint32_t*>(base);
-    uint32_t* seen = reinterpret_cast<uint32_t*>(base + align16(stage_bytes + 32u));
+    uint32_t* recs = reinterpret_cast<uint32_t*>(base + align16(stage_bytes + 32u));
+    uint32_t* counts = recs + 2u * kChunk * 32u;
+    uint32_t* seen = counts + 4;
     uint32_t* tring = seen + 8 * 32;
     uint32_t* wring = tring + 32 * kRingRow;
     uint64_t* bar = reinterpret_cast<uint64_t*>(wring + 32 * kRingRow);
-    if (lane == 0) mbar_init(bar);
-    __syncwarp();
-    uint32_t phase = 0u;
+    if (parser && lane == 0) mbar_init(bar);
+    __syncthreads();
     const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
-    uint32_t g = blockIdx.x * W + warp;
-    if (persistent) {
-        uint32_t t = 0u;
-        if (lane == 0) t = atomicAdd(&a.status->work_conn, 1u);
-        g = __shfl_sync(kFull, t, 0);
+    const uint32_t g = blockIdx.x * G + pair;
+    if (g >= n_groups) return;  // both warps of the pair
+    GroupLane L;
+    load_group_lane(a, g, lane, L);
+    bool ok = L.valid;
+    if (ok && !placement_ok(a, L)) {
+        if (parser) report(a.status, kErrCorrupt, L.m);
+        ok = false;
     }
-    while (g < n_groups) {
-        GroupLane L;
-        load_group_lane(a, g, lane, L);
-        bool ok = L.valid;
-        if (ok && !placement_ok(a, L)) {
-            report(a.status, kErrCorrupt, L.m);
-            ok = false;
-        }
-        const unsigned long long start_b = L.blob_off + (L.d.start_bit >> 3);
-        const unsigned long long end16 = (L.blob_off + ((L.d.end_bit + 7u) >> 3) + 15ull) & ~15ull;
-        uint32_t todo = __ballot_sync(kFull, ok);
-        while (todo) {
-            const int first = __ffs(todo) - 1;
-            const bool in = (todo >> lane) & 1u;
-            const unsigned long long s0 = shfl64(start_b, first) & ~15ull;
-            const bool fit = in && (end16 - s0) <= stage_bytes;
-            uint32_t rmask = __ballot_sync(kFull, fit);
-            const bool staged = rmask != 0u;
-            if (!staged) rmask = 1u << first;  // larger than the stage: read from global memory
-            todo &= ~rmask;
-            const bool act = (rmask >> lane) & 1u;
+    const unsigned long long start_b = L.blob_off + (L.d.start_bit >> 3);
+    const unsigned long long end16 = (L.blob_off + ((L.d.end_bit + 7u) >> 3) + 15ull) & ~15ull;
+    uint32_t phase = 0u;
+    uint32_t todo = __ballot_sync(kFull, ok);
+    while (todo) {
+        const int first = __ffs(todo) - 1;
+        const bool in = (todo >> lane) & 1u;
+        const unsigned long long s0 = shfl64(start_b, first) & ~15ull;
+        const bool fit = in && (end16 - s0) <= stage_bytes;
+        uint32_t rmask = __ballot_sync(kFull, fit);
+        const bool staged = rmask != 0u;
+        if (!staged) rmask = 1u << first;  // larger than the stage: read from global memory
+        todo &= ~rmask;
+        const bool act = (rmask >> lane) & 1u;
+        if (parser) {
+            bool abort = false;
             if (staged) {
                 const int last = 31 - __clz(rmask);
                 const uint32_t bytes = static_cast<uint32_t>(shfl64(end16, last) - s0);
@@ -681,24 +762,23 @@ __global__ void __launch_bounds__(W * 32) conn_kernel(DecodeArgs a, uint32_t sta
                     mbar_expect(bar, bytes);
                     bulk_copy(stage, a.arena + s0, bytes, bar);
                 }
-                if (!mbar_wait(bar, phase)) {
+                abort = __any_sync(kFull, !mbar_wait(bar, phase));
+                if (abort) {
                     if (lane == 0) report(a.status, kErrTimeout, L.m);
                     mbar_wait(bar, phase);  // let the copy land before the CTA exits
-                    return;
                 }
                 phase ^= 1u;
-                conn_lane<true>(a, L, act, stage, static_cast<uint32_t>(L.blob_off * 8ull - s0 * 8ull), seen, tring, wring,
-                                lane);
+                conn_parse<true>(a, L, act, stage, static_cast<uint32_t>(L.blob_off * 8ull - s0 * 8ull), recs, counts,
+                                 pair, abort, lane);
             } else {
-                conn_lane<false>(a, L, act, reinterpret_cast<const uint32_t*>(a.arena + L.blob_off), 0u, seen,
-                                 tring, wring, lane);
+                conn_parse<false>(a, L, act, reinterpret_cast<const uint32_t*>(a.arena + L.blob_off), 0u, recs,
+                                  counts, pair, false, lane);
             }
-            __syncwarp();
+            if (abort) return;  // the assembler has seen the abandoned round and leaves too
+        } else {
+            if (conn_assemble(a, L, act, seen, tring, wring, recs, counts, pair, lane)) return;
         }
-        if (!persistent) break;
-        uint32_t t = 0u;
-        if (lane == 0) t = atomicAdd(&a.status->work_conn, 1u);
-        g = __shfl_sync(kFull, t, 0);
+        __syncwarp();
     }
 }
 
@@ -787,18 +867,11 @@ struct VertLane {
     bool bad;
 };
 
-// Anchor, the six (tag, k) pairs, and where axis d's two substreams start
-// (paradelta_v5_dup.py:544-579): the delta substreams dx dy dz come first,
-// then px py pz, so axis d skips the three delta substreams and the d
-// parallelogram substreams before its own (substream lengths are not
-// stored, only their code counts).
+// Anchor code of axis d and the six (tag, k) pairs (paradelta_v5_dup.py:
+// 544-557); returns the bit after them (the start of dx).
 template <bool kShared>
-__device__ __forceinline__ void vert_setup(const GroupLane& L, uint32_t d, const uint32_t* w, uint32_t rbase,
-                                           VertLane& S) {
-    const uint32_t n_kind0 = L.d.walk & 0xFFFFu;
-    const uint32_t n_walk = L.d.walk >> 16;
-    const uint32_t n_delta = n_kind0 ? n_kind0 - 1u : 0u;  // the anchor has no delta
-    const uint32_t n_para = n_walk - n_kind0;
+__device__ __forceinline__ uint32_t vert_header(const GroupLane& L, uint32_t d, const uint32_t* w, uint32_t rbase,
+                                                VertLane& S, uint32_t (&tk)[6]) {
     const uint32_t end = L.d.end_bit;
     const MeshParams* P = L.P;
     uint32_t pos = L.d.anchor_bit;
@@ -811,7 +884,6 @@ __device__ __forceinline__ void vert_setup(const GroupLane& L, uint32_t d, const
         S.anc = e == d ? v : S.anc;
         pos += gb;
     }
-    uint32_t tk[6];
 #pragma unroll
     for (int i = 0; i < 6; i++) {
         const uint32_t t = peek32<kShared>(w, pos + rbase) >> 16;
@@ -822,19 +894,8 @@ __device__ __forceinline__ void vert_setup(const GroupLane& L, uint32_t d, const
     }
     S.td = d == 0u ? tk[0] : (d == 1u ? tk[1] : tk[2]);
     S.tp = d == 0u ? tk[3] : (d == 1u ? tk[4] : tk[5]);
-    bad = bad || pos > end;
-    pos = min(pos, end);
-    bool ok = !bad;
-    S.cdd = pos;
-#pragma unroll
-    for (uint32_t e = 0; e < 3u; e++) {
-        S.cdd = e == d ? pos : S.cdd;
-        if (ok) ok = skip_codes<kShared>(w, rbase, pos, tk[e], n_delta, end);
-    }
-    for (uint32_t e = 0; e < d; e++)
-        if (ok) ok = skip_codes<kShared>(w, rbase, pos, e == 0u ? tk[3] : tk[4], n_para, end);
-    S.cp = pos;
-    S.bad = !ok;
+    S.bad = bad || pos > end;
+    return min(pos, end);
 }
 
 // Integer codes of axis d in walk order (IRLP, paradelta_v5_dup.py:91-104
@@ -900,31 +961,45 @@ __device__ __forceinline__ void vert_axis(const DecodeArgs& a, const GroupLane& 
 }
 
 // Axis d of every vertex of the round's meshlets -> positions (and codes),
-// the warp working through one meshlet at a time.  The mesh's dequantisation
-// constants sit in registers for the whole meshlet.
+// the warp working through one meshlet at a time.  The mesh's constants
+// (table base, or float-float dequantisation coefficients) stay in registers
+// while consecutive meshlets belong to the same mesh.
 template <bool kWide>
 __device__ void emit_axis(const DecodeArgs& a, const GroupLane& L, uint32_t rmask, const uint8_t* planes,
                           uint32_t code_off, uint32_t d, int lane) {
+    uint32_t cached = 0xFFFFFFFFu;
+    const MeshParams* Pj = a.meshes;
+    stride_dequant_axis c;
+    c.a_hi = c.a_lo = c.b_hi = c.b_lo = c.err = 0.f;
+    bool zero_bits = false, has_lut = false;
+    const float* lut = nullptr;
+    uint32_t qmax = 0u;
     for (uint32_t mm = rmask; mm; mm &= mm - 1u) {
         const int j = __ffs(mm) - 1;
         const uint32_t nv = __shfl_sync(kFull, L.d.counts0, j) & 0xFFFFu;
         const unsigned long long vb = shfl64(L.v_base, j);
         const uint32_t off = __shfl_sync(kFull, code_off, j);
         const uint32_t mj = __shfl_sync(kFull, L.mi, j);
-        const MeshParams* Pj = a.meshes + mj;
-        stride_dequant_axis c;
-        c.a_hi = __ldg(&Pj->dq[d].a_hi);
-        c.a_lo = __ldg(&Pj->dq[d].a_lo);
-        c.b_hi = __ldg(&Pj->dq[d].b_hi);
-        c.b_lo = __ldg(&Pj->dq[d].b_lo);
-        c.err = __ldg(&Pj->dq[d].err);
-        const bool zero_bits = __ldg(&Pj->dq[d].zero_bits) != 0;
+        if (mj != cached) {  // warp-uniform
+            cached = mj;
+            Pj = a.meshes + mj;
+            has_lut = __ldg(&Pj->has_lut) != 0;
+            if (has_lut) {
+                const uint32_t g0 = __ldg(&Pj->g_bits[0]), g1 = __ldg(&Pj->g_bits[1]);
+                lut = a.lut + __ldg(&Pj->lut_off) + (d >= 1u ? 1u << g0 : 0u) + (d >= 2u ? 1u << g1 : 0u);
+                qmax = (1u << __ldg(&Pj->g_bits[d])) - 1u;  // a corrupt stream's codes may lie outside
+            } else {
+                c.a_hi = __ldg(&Pj->dq[d].a_hi);
+                c.a_lo = __ldg(&Pj->dq[d].a_lo);
+                c.b_hi = __ldg(&Pj->dq[d].b_hi);
+                c.b_lo = __ldg(&Pj->dq[d].b_lo);
+                c.err = __ldg(&Pj->dq[d].err);
+                zero_bits = __ldg(&Pj->dq[d].zero_bits) != 0;
+            }
+        }
         const PlaneT<kWide>* pj = reinterpret_cast<const PlaneT<kWide>*>(planes + off);
         float* dst = a.pos + 3ull * vb + d;
-        if (__ldg(&Pj->has_lut)) {  // warp-uniform: the mesh has per-code tables
-            const uint32_t g0 = __ldg(&Pj->g_bits[0]), g1 = __ldg(&Pj->g_bits[1]), gd = __ldg(&Pj->g_bits[d]);
-            const float* lut = a.lut + __ldg(&Pj->lut_off) + (d >= 1u ? 1u << g0 : 0u) + (d >= 2u ? 1u << g1 : 0u);
-            const uint32_t qmax = (1u << gd) - 1u;  // codes of a corrupt stream may lie outside; it is rejected
+        if (has_lut) {
             for (uint32_t v = lane; v < nv; v += 32u)
                 dst[3u * v] = __ldg(lut + min(static_cast<uint32_t>(pj[v]), qmax));
         } else {
@@ -944,16 +1019,41 @@ __device__ void emit_axis(const DecodeArgs& a, const GroupLane& L, uint32_t rmas
     __syncwarp();
 }
 
-// One round of warp d: its active lanes decode axis d of their meshlets,
-// then the warp writes that coordinate of every vertex.
+// One round of warp d: its active lanes find where their axis' two
+// substreams start -- the delta substreams dx dy dz come first, then px py
+// pz, so axis d skips the three delta substreams and the d parallelogram
+// substreams before its own (substream lengths are not stored, only their
+// code counts) -- decode axis d of their meshlets, then the warp writes that
+// coordinate of every vertex.  The three warps skip independently: waiting
+// for one another's skips measured slower than repeating them.
 template <bool kShared, bool kWide>
 __device__ __forceinline__ void vert_round(const DecodeArgs& a, const GroupLane& L, uint32_t d, bool act,
                                            uint32_t rmask, const uint32_t* w, uint32_t rbase, uint8_t* planes,
                                            uint32_t code_off, int lane) {
     VertLane S;
     S.bad = false;
-    S.cp = 0u;
-    if (act) vert_setup<kShared>(L, d, w, rbase, S);
+    S.cp = S.cdd = 0u;
+    S.anc = 0;
+    S.td = S.tp = 0u;
+    if (act) {
+        uint32_t tk[6];
+        uint32_t pos = vert_header<kShared>(L, d, w, rbase, S, tk);
+        const uint32_t n_kind0 = L.d.walk & 0xFFFFu;
+        const uint32_t n_delta = n_kind0 ? n_kind0 - 1u : 0u;  // the anchor has no delta
+        const uint32_t n_para = (L.d.walk >> 16) - n_kind0;
+        const uint32_t end = L.d.end_bit;
+        bool ok = !S.bad;
+        S.cdd = pos;
+#pragma unroll
+        for (uint32_t e = 0; e < 3u; e++) {
+            S.cdd = e == d ? pos : S.cdd;
+            if (ok) ok = skip_codes<kShared>(w, rbase, pos, tk[e], n_delta, end);
+        }
+        for (uint32_t e = 0; e < d; e++)
+            if (ok) ok = skip_codes<kShared>(w, rbase, pos, e == 0u ? tk[3] : tk[4], n_para, end);
+        S.cp = pos;
+        S.bad = !ok;
+    }
     PlaneT<kWide>* plane = reinterpret_cast<PlaneT<kWide>*>(planes + code_off);
     if (act && !S.bad) vert_axis<kShared, kWide>(a, L, d, w, rbase, plane, S);
     __syncwarp();
@@ -1115,17 +1215,19 @@ uint32_t grid_for(K kernel, int threads, size_t smem, const LaunchCfg& cfg, uint
     return grid;
 }
 
-template <int W>
+// Connectivity pairs per CTA for a launch shape (warps_per_cta 4 -> 2 pairs).
+__host__ __device__ constexpr int conn_pairs(int warps_per_cta) { return warps_per_cta >= 4 ? 2 : 1; }
+
+template <int G>
 cudaError_t launch_conn(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s) {
     static size_t configured[64] = {0};
-    static OccCache occ;
-    const size_t smem = static_cast<size_t>(W) * conn_warp_bytes(cfg.stage_bytes);
-    cudaError_t e = opt_in_smem(conn_kernel<W>, smem, configured);
+    const size_t smem = static_cast<size_t>(G) * conn_pair_bytes(cfg.stage_bytes);
+    cudaError_t e = opt_in_smem(conn_kernel<G>, smem, configured);
     if (e != cudaSuccess) return e;
     const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
-    const uint32_t grid = grid_for(conn_kernel<W>, W * 32, smem, cfg, n_groups, W, occ);
+    const uint32_t grid = (n_groups + G - 1) / G;
     if (grid == 0) return cudaSuccess;
-    conn_kernel<W><<<grid, W * 32, smem, s>>>(a, cfg.stage_bytes, cfg.persistent);
+    conn_kernel<G><<<grid, G * 64, smem, s>>>(a, cfg.stage_bytes);
     return cudaGetLastError();
 }
 
@@ -1145,7 +1247,7 @@ cudaError_t launch_vert(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t 
 
 template <int W>
 cudaError_t launch_pair(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s, void* const* ev) {
-    cudaError_t e = launch_conn<W>(a, cfg, s);
+    cudaError_t e = launch_conn<conn_pairs(W)>(a, cfg, s);
     if (e != cudaSuccess) return e;
     if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[2]), s);
     return a.wide_codes ? launch_vert<true>(a, cfg, s) : launch_vert<false>(a, cfg, s);
@@ -1154,7 +1256,7 @@ cudaError_t launch_pair(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t 
 }  // namespace
 
 size_t conn_smem_bytes(const LaunchCfg& cfg) {
-    return static_cast<size_t>(cfg.warps_per_cta) * conn_warp_bytes(cfg.stage_bytes);
+    return static_cast<size_t>(conn_pairs(cfg.warps_per_cta)) * conn_pair_bytes(cfg.stage_bytes);
 }
 
 size_t vert_smem_bytes(const LaunchCfg& cfg) { return vert_cta_bytes(cfg.stage_bytes, cfg.code_bytes); }
