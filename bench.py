@@ -487,7 +487,7 @@ def run_batch(args):
         from concurrent.futures import ThreadPoolExecutor
         import oracle
         oracle.build()
-        t_all = b.d_tris.cpu().numpy().view(np.uint32)
+        t_all = b.d_tris.view(torch.int32).cpu().numpy().view(np.uint32)
         v_all = b.d_verts.cpu().numpy()
 
         def same(i):
@@ -644,8 +644,9 @@ def run_serve(args):
         alone.append((t.view(torch.int32).clone(), v.view(torch.int32).clone()))
         if rank == 0:
             opos, oidx = oracle.decode_mt(x, 0)
-            pool_exact = pool_exact and np.array_equal(t.cpu().numpy().view(np.uint32).astype(np.int64), oidx) \
-                and np.array_equal(v.cpu().numpy().view(np.uint32), opos.view(np.uint32))
+            ti = t.view(torch.int32).cpu().numpy().view(np.uint32).astype(np.int64)
+            pool_exact = pool_exact and np.array_equal(ti, oidx) and \
+                np.array_equal(v.cpu().numpy().view(np.uint32), opos.view(np.uint32))
         d.close()
     rates = [float(r) for r in args.rates.split(",")]
     rng = np.random.default_rng(11)
