@@ -660,7 +660,7 @@ def run_serve(args):
         picks = rng.integers(0, len(blobs), n_req)
         srv = DecodeServer(args.serve_budget_gb << 30, n_streams=3, max_batch=256)
         ids = [None] * n_req
-        lat, ok = [], [0, 0]
+        lat, ok, failed = [], [0, 0], {}
         first_submit = [None]
         last_done = [0.0]
 
@@ -681,9 +681,12 @@ def run_serve(args):
             while ids[i] is None:
                 time.sleep(0.0002)
             r = srv.wait(ids[i])
-            good = r.ok and torch.equal(r.tris.view(torch.int32), alone[picks[i]][0]) and \
-                torch.equal(r.verts.view(torch.int32), alone[picks[i]][1])
-            ok[0 if good else 1] += 1
+            if not r.ok:
+                failed[r.status] = failed.get(r.status, 0) + 1
+            else:
+                good = torch.equal(r.tris.view(torch.int32), alone[picks[i]][0]) and \
+                    torch.equal(r.verts.view(torch.int32), alone[picks[i]][1])
+                ok[0 if good else 1] += 1
             lat.append(r.latency_ms)
             if first_submit[0] is None:
                 first_submit[0] = r.t_submit_us
@@ -713,6 +716,7 @@ def run_serve(args):
                 "mean_requests_per_launch": round(n_req / max(1, st["launches"]), 2),
                 "arena_peak_gb": round(st["arena_peak_bytes"] / 2 ** 30, 3),
                 "exact_responses": ok[0], "mismatched_responses": ok[1],
+                "failed_responses": {str(k): v for k, v in failed.items()},
                 "pool_bit_exact_vs_oracle": bool(pool_exact), "wall_s": round(wall, 3),
             }
             print(json.dumps(line), flush=True)

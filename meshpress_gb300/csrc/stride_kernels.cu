@@ -46,12 +46,17 @@ constexpr unsigned kFull = 0xFFFFFFFFu;
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ uint32_t bswap32(uint32_t x) { return __byte_perm(x, 0u, 0x0123u); }
 
+// Global data is read through L2 only (ld.global.cg here, and every plain
+// global load of this file is compiled with -dlcm=cg): the serving engine
+// rewrites arena ranges (streams, mesh tables, dequantisation tables) for a
+// new launch while launches on other streams may still run on the same SMs,
+// so nothing may be served from an SM's L1 or read-only cache.
 template <bool kShared>
 __device__ __forceinline__ uint32_t ldw(const uint32_t* w, uint32_t i) {
     if constexpr (kShared) {
         return w[i];
     } else {
-        return __ldg(w + i);
+        return __ldcg(w + i);
     }
 }
 
@@ -280,7 +285,7 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a) {
     MeshletDesc d;
     memset(&d, 0, sizeof(d));
     if (m < a.total_meshlets) {
-        const uint32_t mi = a.meshlet_mesh ? __ldg(a.meshlet_mesh + m) : 0u;
+        const uint32_t mi = a.meshlet_mesh ? __ldcg(a.meshlet_mesh + m) : 0u;
         const MeshParams& P = a.meshes[mi];
         const int e = scan_meshlet(a.arena, P, m - P.meshlet_begin, d);
         if (e) {
@@ -513,7 +518,7 @@ __device__ __forceinline__ void load_group_lane(const DecodeArgs& a, uint32_t g,
         memset(&L.d, 0, sizeof(L.d));
         L.v_base = L.t_base = L.wp_base = 0ull;
     }
-    L.mi = (L.valid && a.meshlet_mesh) ? __ldg(a.meshlet_mesh + L.m) : 0u;
+    L.mi = (L.valid && a.meshlet_mesh) ? __ldcg(a.meshlet_mesh + L.m) : 0u;
     L.P = a.meshes + L.mi;
     L.blob_off = L.valid ? L.P->blob_off : 0ull;
 }
@@ -983,25 +988,25 @@ __device__ void emit_axis(const DecodeArgs& a, const GroupLane& L, uint32_t rmas
         if (mj != cached) {  // warp-uniform
             cached = mj;
             Pj = a.meshes + mj;
-            has_lut = __ldg(&Pj->has_lut) != 0;
+            has_lut = __ldcg(&Pj->has_lut) != 0;
             if (has_lut) {
-                const uint32_t g0 = __ldg(&Pj->g_bits[0]), g1 = __ldg(&Pj->g_bits[1]);
-                lut = a.lut + __ldg(&Pj->lut_off) + (d >= 1u ? 1u << g0 : 0u) + (d >= 2u ? 1u << g1 : 0u);
-                qmax = (1u << __ldg(&Pj->g_bits[d])) - 1u;  // a corrupt stream's codes may lie outside
+                const uint32_t g0 = __ldcg(&Pj->g_bits[0]), g1 = __ldcg(&Pj->g_bits[1]);
+                lut = a.lut + __ldcg(&Pj->lut_off) + (d >= 1u ? 1u << g0 : 0u) + (d >= 2u ? 1u << g1 : 0u);
+                qmax = (1u << __ldcg(&Pj->g_bits[d])) - 1u;  // a corrupt stream's codes may lie outside
             } else {
-                c.a_hi = __ldg(&Pj->dq[d].a_hi);
-                c.a_lo = __ldg(&Pj->dq[d].a_lo);
-                c.b_hi = __ldg(&Pj->dq[d].b_hi);
-                c.b_lo = __ldg(&Pj->dq[d].b_lo);
-                c.err = __ldg(&Pj->dq[d].err);
-                zero_bits = __ldg(&Pj->dq[d].zero_bits) != 0;
+                c.a_hi = __ldcg(&Pj->dq[d].a_hi);
+                c.a_lo = __ldcg(&Pj->dq[d].a_lo);
+                c.b_hi = __ldcg(&Pj->dq[d].b_hi);
+                c.b_lo = __ldcg(&Pj->dq[d].b_lo);
+                c.err = __ldcg(&Pj->dq[d].err);
+                zero_bits = __ldcg(&Pj->dq[d].zero_bits) != 0;
             }
         }
         const PlaneT<kWide>* pj = reinterpret_cast<const PlaneT<kWide>*>(planes + off);
         float* dst = a.pos + 3ull * vb + d;
         if (has_lut) {
             for (uint32_t v = lane; v < nv; v += 32u)
-                dst[3u * v] = __ldg(lut + min(static_cast<uint32_t>(pj[v]), qmax));
+                dst[3u * v] = __ldcg(lut + min(static_cast<uint32_t>(pj[v]), qmax));
         } else {
             for (uint32_t v = lane; v < nv; v += 32u) {
                 const uint32_t q = static_cast<uint32_t>(pj[v]);

@@ -290,9 +290,12 @@ void retire(stride_server* s, Launch* l) {
     Slot& slot = s->slots[l->slot];
     std::shared_ptr<Launch> keep = slot.busy;  // == l
     slot.busy.reset();
-    const cudaError_t ce = cudaStreamQuery(slot.stream);  // surfaces launch faults
+    // surfaces launch faults; "not ready" is the completion host function
+    // itself, which may not yet count as finished when this runs
+    const cudaError_t ce = cudaStreamQuery(slot.stream);
     uint32_t bad = 0;
-    int code = ce == cudaSuccess ? status_to_code(*slot.h_status, &bad) : STRIDE_ERR_CUDA;
+    int code = (ce == cudaSuccess || ce == cudaErrorNotReady) ? status_to_code(*slot.h_status, &bad)
+                                                              : STRIDE_ERR_CUDA;
     free_launch_buffers(s, l);
     if (code == STRIDE_OK) {
         for (Request* r : l->reqs) {
@@ -369,14 +372,17 @@ bool dispatch(stride_server* s, int slot_i) {
     l->scratch_size = sp.total;
     // the probe above reserved nothing, so allocate for real (cannot fail:
     // the same bytes were free a moment ago and nothing ran in between)
-    if (!s->arena.alloc(l->out_size, &l->out_off) || !s->arena.alloc(l->scratch_size, &l->scratch_off)) {
+    l->has_out = s->arena.alloc(l->out_size, &l->out_off);
+    l->has_scratch = l->has_out && s->arena.alloc(l->scratch_size, &l->scratch_off);
+    if (!l->has_scratch) {
+        if (l->has_out) s->arena.release(l->out_off, l->out_size);
+        l->has_out = false;
         for (Request* r : take) {
             s->arena.release(r->blob_off, blob_alloc_bytes(r->data.size()));
             r->has_blob = false;
         }
         return false;
     }
-    l->has_out = l->has_scratch = true;
     for (size_t i = 0; i < take.size(); i++) s->queue.pop_front();
     l->reqs = take;
     l->total_v = tv;
