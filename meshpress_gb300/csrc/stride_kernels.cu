@@ -952,10 +952,13 @@ __device__ __forceinline__ void vert_axis(const DecodeArgs& a, const GroupLane& 
     };
     // walk entries (v | a << 8 | b << 16 | c << 24), 16-byte aligned per meshlet
     const uint4* wq = reinterpret_cast<const uint4*>(a.walk_scratch + L.wp_base);
+    // two quads in flight: the walk is read from L2
     uint4 qn = n_walk ? __ldcg(wq) : make_uint4(0u, 0u, 0u, 0u);
+    uint4 qm = n_walk > 4u ? __ldcg(wq + 1) : qn;
     for (uint32_t i = 0; i < n_walk; i += 4u) {
         const uint4 q = qn;
-        if (i + 4u < n_walk) qn = __ldcg(wq + (i >> 2) + 1u);
+        qn = qm;
+        if (i + 8u < n_walk) qm = __ldcg(wq + (i >> 2) + 2u);
         step(q.x, true, i == 0u);
         step(q.y, i + 1u < n_walk, false);
         step(q.z, i + 2u < n_walk, false);
@@ -1004,9 +1007,20 @@ __device__ void emit_axis(const DecodeArgs& a, const GroupLane& L, uint32_t rmas
         }
         const PlaneT<kWide>* pj = reinterpret_cast<const PlaneT<kWide>*>(planes + off);
         float* dst = a.pos + 3ull * vb + d;
-        if (has_lut) {
-            for (uint32_t v = lane; v < nv; v += 32u)
-                dst[3u * v] = __ldcg(lut + min(static_cast<uint32_t>(pj[v]), qmax));
+        if (has_lut) {  // four table reads in flight per lane
+            for (uint32_t v0 = 0; v0 < nv; v0 += 128u) {
+                float y[4];
+#pragma unroll
+                for (uint32_t k = 0; k < 4u; k++) {
+                    const uint32_t v = v0 + lane + 32u * k;
+                    y[k] = v < nv ? __ldcg(lut + min(static_cast<uint32_t>(pj[v]), qmax)) : 0.f;
+                }
+#pragma unroll
+                for (uint32_t k = 0; k < 4u; k++) {
+                    const uint32_t v = v0 + lane + 32u * k;
+                    if (v < nv) dst[3u * v] = y[k];
+                }
+            }
         } else {
             for (uint32_t v = lane; v < nv; v += 32u) {
                 const uint32_t q = static_cast<uint32_t>(pj[v]);
