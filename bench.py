@@ -473,8 +473,8 @@ def run_batch(args):
     blobs, cfg = batch_streams(args.batch_meshes, args.bits)
     n_t_all = cfg["triangles"]
     lib = _lib.load()
-    # scan + connectivity + vertex kernels, plus the table kernel when any mesh has tables
-    per_step_kernels = 3 + int(any(_lib.inspect(x).kernels == 4 for x in blobs))
+    # scan (with the dequantisation tables) + connectivity + vertex kernels
+    per_step_kernels = 3
     b = BatchDecoder(blobs)
     launch = None
     if args.tune:

@@ -59,8 +59,9 @@ typedef struct {
     float scale;
     int32_t pred_n[9];
     int32_t pred_k[3];
-    uint32_t kernels;    /* kernel launches one decode makes (3, or 4 with per-code
-                            dequantisation tables)                           */
+    uint32_t kernels;    /* kernel launches one decode makes: 3 (scan, which also
+                            fills any per-code dequantisation tables;
+                            connectivity; vertex), 0 for an empty stream     */
 } stride_info_t;
 
 /* Launch shape of the decode kernel (the autotuner's search space). */

@@ -143,7 +143,7 @@ unsigned long long plan_luts(MeshParams* p, uint32_t n, uint32_t* meshes, uint32
         p[i].has_lut = 0;
         p[i].lut_off = 0;
         const unsigned long long e = lut_entries(p[i]);
-        if (!e || k >= max_meshes || k >= 65535u) continue;  // grid.y limit of lut_kernel
+        if (!e || k >= max_meshes || k >= 65535u) continue;  // bounds the table blocks of the scan launch
         p[i].has_lut = 1;
         p[i].lut_off = total;
         total += e;
@@ -303,7 +303,7 @@ static void fill_info(const MeshParams& p, size_t len, stride_info_t* info) {
     info->n_v = p.n_v;
     info->n_t = p.n_t;
     info->nbytes = len;
-    info->kernels = p.n_meshlets ? (lut_entries(p) ? 4u : 3u) : (lut_entries(p) ? 1u : 0u);
+    info->kernels = p.n_meshlets ? 3u : 0u;  // scan (+ tables), connectivity, vertex
 }
 
 int stride_inspect(const uint8_t* data, size_t len, stride_info_t* info) {

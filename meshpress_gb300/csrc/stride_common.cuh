@@ -58,7 +58,7 @@ struct MeshParams {
 
 // Dequantisation tables: a mesh with at least as many duplicated vertices as
 // half its code space (all axes together) gets one float per code and axis,
-// evaluated once per decode by lut_kernel; axis d's table follows those of
+// evaluated once per decode by extra blocks of the scan launch; axis d's table follows those of
 // the axes before it.  Only for codes of up to kLutMaxBits bits.
 constexpr uint32_t kLutMaxBits = 16;
 

@@ -276,7 +276,25 @@ __device__ __forceinline__ unsigned long long block_scan(unsigned long long x, u
     return excl;
 }
 
-__global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a) {
+// Dequantisation tables: block b of mesh lut_meshes[b / bx] evaluates codes
+// (b % bx) * 256 + threadIdx.x of its three axes, exactly.
+__device__ __forceinline__ void lut_block(const DecodeArgs& a, uint32_t b, uint32_t bx) {
+    const MeshParams& P = a.meshes[a.lut_meshes[b / bx]];
+    const uint32_t i = (b % bx) * 256u + threadIdx.x;
+    const uint32_t e0 = 1u << P.g_bits[0], e1 = 1u << P.g_bits[1], e2 = 1u << P.g_bits[2];
+    if (i >= e0 + e1 + e2) return;
+    const uint32_t d = i < e0 ? 0u : (i < e0 + e1 ? 1u : 2u);
+    const uint32_t q = i - (d >= 1u ? e0 : 0u) - (d >= 2u ? e1 : 0u);
+    a.lut[P.lut_off + i] = stride_dequant(&P.dq[d], q);
+}
+
+// Blocks [0, nb) scan the meshlets; the blocks after them (lut_bx per mesh
+// with tables) fill the dequantisation tables in the same launch.
+__global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a, uint32_t nb, uint32_t lut_bx) {
+    if (blockIdx.x >= nb) {  // block-uniform
+        lut_block(a, blockIdx.x - nb, lut_bx);
+        return;
+    }
     __shared__ unsigned long long wsum[kScanThreads / 32];
     __shared__ int is_last;
     const uint32_t tid = threadIdx.x;
@@ -316,19 +334,19 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a) {
     // The last block to finish turns the block sums into block prefixes.
     __threadfence();
     __syncthreads();
-    if (tid == 0) is_last = atomicAdd(&a.status->ticket, 1u) == gridDim.x - 1u;
+    if (tid == 0) is_last = atomicAdd(&a.status->ticket, 1u) == nb - 1u;
     __syncthreads();
     if (!is_last) return;
     __threadfence();
     unsigned long long cv = 0ull, ct = 0ull, cw = 0ull;
-    for (uint32_t base = 0; base < gridDim.x; base += kScanThreads) {
+    for (uint32_t base = 0; base < nb; base += kScanThreads) {
         const uint32_t i = base + tid;
-        const uint4 s = i < gridDim.x ? __ldcg(a.blk_sums + i) : make_uint4(0u, 0u, 0u, 0u);
+        const uint4 s = i < nb ? __ldcg(a.blk_sums + i) : make_uint4(0u, 0u, 0u, 0u);
         // per-chunk sums stay below 2^32 (256 blocks x 65536), so pack pairs
         unsigned long long ta, tb;
         const unsigned long long ea = block_scan((static_cast<unsigned long long>(s.y) << 32) | s.x, wsum, ta);
         const unsigned long long eb = block_scan(s.z, wsum, tb);
-        if (i < gridDim.x) {
+        if (i < nb) {
             BlockPrefix p;
             p.v = cv + (ea & 0xFFFFFFFFull);
             p.t = ct + (ea >> 32);
@@ -451,19 +469,6 @@ __device__ __forceinline__ void flush_walk(uint32_t* out, const uint32_t* ring, 
     } else {
         wf = max(wf, qe);
     }
-}
-
-// ---------------------------------------------------------------------------
-// 1b. dequantisation tables: one thread per (mesh, code), exact values
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) lut_kernel(DecodeArgs a) {
-    const MeshParams& P = a.meshes[a.lut_meshes[blockIdx.y]];
-    const uint32_t i = blockIdx.x * 256u + threadIdx.x;
-    const uint32_t e0 = 1u << P.g_bits[0], e1 = 1u << P.g_bits[1], e2 = 1u << P.g_bits[2];
-    if (i >= e0 + e1 + e2) return;
-    const uint32_t d = i < e0 ? 0u : (i < e0 + e1 ? 1u : 2u);
-    const uint32_t q = i - (d >= 1u ? e0 : 0u) - (d >= 2u ? e1 : 0u);
-    a.lut[P.lut_off + i] = stride_dequant(&P.dq[d], q);
 }
 
 // ---------------------------------------------------------------------------
@@ -833,6 +838,8 @@ __device__ __forceinline__ bool residual(const uint32_t* w, uint32_t rbase, uint
 }
 
 // Skip n codewords (substream boundaries are not stored in the stream).
+// Up to four codewords that lie wholly inside the 32-bit window are taken
+// per step; a codeword longer than the window goes to the general reader.
 template <bool kShared>
 __device__ __forceinline__ bool skip_codes(const uint32_t* w, uint32_t rbase, uint32_t& pos, uint32_t tk,
                                            uint32_t n, uint32_t limit) {
@@ -843,16 +850,26 @@ __device__ __forceinline__ bool skip_codes(const uint32_t* w, uint32_t rbase, ui
     b.w = w;
     b.rbase = rbase;
     b.seek(pos);
-    for (uint32_t i = 0; i < n; i++) {
+    while (n > 0u) {
         const uint32_t x = b.peek();
-        const uint32_t z = __clz(x);
-        const uint32_t len = z + 1u + (eg ? z : 0u) + k;
-        if (len <= 32u) {
-            b.advance(len);
+        uint32_t used = 0u, cnt = 0u;
+#pragma unroll
+        for (int s = 0; s < 4; s++) {
+            const uint32_t xx = __funnelshift_lc(0u, x, used);  // the window past the codewords taken
+            const uint32_t z = __clz(xx);                       // 32 when nothing is left
+            const uint32_t len = z + 1u + (eg ? z : 0u) + k;
+            const bool fits = (used + len <= 32u) & (cnt < n);
+            used += fits ? len : 0u;
+            cnt += fits ? 1u : 0u;
+        }
+        if (cnt) {
+            b.advance(used);
+            n -= cnt;
         } else {  // prefix or value beyond the window: general reader
             uint32_t u, np = b.pos;
             ok = ok & (read_code<kShared>(w, rbase, np, tk, limit, u) == 0);
             b.seek(min(np, limit));
+            n--;
         }
         if (b.pos > limit) {  // only a corrupt stream runs past its meshlet
             ok = false;
@@ -1305,14 +1322,15 @@ int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void
     if (check_config(cfg, a.wide_codes)) return STRIDE_ERR_ARG;
     if (cudaMemsetAsync(a.status, 0, sizeof(Status), s) != cudaSuccess) return STRIDE_ERR_CUDA;
     if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[0]), s);
-    if (a.total_meshlets != 0) {
-        scan_kernel<<<scan_blocks(a.total_meshlets), kScanThreads, 0, s>>>(a);
-        if (cudaGetLastError() != cudaSuccess) return STRIDE_ERR_CUDA;
-    }
-    if (a.n_lut_meshes != 0) {
-        const dim3 grid((a.lut_max + 255u) / 256u, a.n_lut_meshes);
-        lut_kernel<<<grid, 256, 0, s>>>(a);
-        if (cudaGetLastError() != cudaSuccess) return STRIDE_ERR_CUDA;
+    {
+        const uint32_t nb = scan_blocks(a.total_meshlets);
+        const uint32_t lut_bx = (a.lut_max + 255u) / 256u;
+        const unsigned long long grid = nb + static_cast<unsigned long long>(a.n_lut_meshes) * lut_bx;
+        if (grid > 0x7FFFFFFFull) return STRIDE_ERR_UNSUPPORTED;
+        if (grid) {
+            scan_kernel<<<static_cast<uint32_t>(grid), kScanThreads, 0, s>>>(a, nb, lut_bx);
+            if (cudaGetLastError() != cudaSuccess) return STRIDE_ERR_CUDA;
+        }
     }
     if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[1]), s);
     if (a.total_meshlets != 0) {
