@@ -84,7 +84,8 @@ struct __align__(16) MeshletDesc {
     uint32_t pad0;
     uint32_t anchor_bit;   // end of connectivity = anchor codes
     uint32_t walk;         // n_kind0 | n_walk << 16
-    uint32_t pad[6];
+    uint32_t slot_meshlet; // meshlet decoded at slot i (= this record's index)
+    uint32_t pad[5];
 };
 
 struct BlockPrefix {

@@ -157,16 +157,40 @@ struct BitWin {
 };
 
 // ---------------------------------------------------------------------------
-// Named barriers between specific warps of a CTA (producer arrives,
-// consumer waits); `threads` counts both sides.
+// Named barriers between the two warps of a connectivity pair (producer
+// arrives, consumer waits; 64 threads).  Pair p uses ids 1 + 4p .. 4 + 4p:
+// slot 0, 1 = record chunk 0, 1 full; slot 2, 3 = chunk 0, 1 empty.  The
+// ids are immediates: an id in a register makes the CTA reserve all 16 of
+// the SM's per-CTA barriers, which caps a two-pair CTA at four per SM.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void named_arrive(uint32_t id, uint32_t threads) {
-    __threadfence_block();  // shared-memory writes before the arrive are visible to the waiting warps
-    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(threads) : "memory");
+template <int kId>
+__device__ __forceinline__ void bar_sync_imm() {
+    asm volatile("bar.sync %0, 64;" ::"n"(kId) : "memory");
+}
+template <int kId>
+__device__ __forceinline__ void bar_arrive_imm() {
+    asm volatile("bar.arrive %0, 64;" ::"n"(kId) : "memory");
 }
 
-__device__ __forceinline__ void named_sync(uint32_t id, uint32_t threads) {
-    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+template <int kBase, bool kArrive>
+__device__ __forceinline__ void pair_bar_at(uint32_t slot) {
+    switch (slot) {
+        case 0: kArrive ? bar_arrive_imm<kBase>() : bar_sync_imm<kBase>(); break;
+        case 1: kArrive ? bar_arrive_imm<kBase + 1>() : bar_sync_imm<kBase + 1>(); break;
+        case 2: kArrive ? bar_arrive_imm<kBase + 2>() : bar_sync_imm<kBase + 2>(); break;
+        default: kArrive ? bar_arrive_imm<kBase + 3>() : bar_sync_imm<kBase + 3>(); break;
+    }
+}
+
+// warp-uniform pair and slot; G pairs per CTA (1 or 2)
+template <int G, bool kArrive>
+__device__ __forceinline__ void pair_bar(uint32_t pair, uint32_t slot) {
+    if (kArrive) __threadfence_block();  // shared-memory writes before the arrive reach the waiting warp
+    if (G == 1 || pair == 0u) {
+        pair_bar_at<1, kArrive>(slot);
+    } else {
+        pair_bar_at<5, kArrive>(slot);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -217,6 +241,68 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
     }
     return true;
 }
+
+// ---------------------------------------------------------------------------
+// Per-lane byte rings of the connectivity parser.  Each lane streams its own
+// meshlet through a 64-word ring in shared memory, 32 words (128 bytes) per
+// chunk, fetched with 16-byte cp.async copies (L2 only) a chunk ahead of the
+// bit cursor.  Word j of the lane's data (counted from its 16-byte aligned
+// first byte) sits at ring[(j + rot) & 63]; the per-lane rotation (a
+// multiple of four words) spreads lanes that read the same relative word
+// over different banks.
+// ---------------------------------------------------------------------------
+constexpr uint32_t kLaneRingWords = 64u;
+constexpr uint32_t kLaneChunkWords = 32u;
+
+__device__ __forceinline__ void cp_async16(uint32_t* dst, const uint8_t* src, uint32_t src_bytes) {
+    unsigned long long gsrc;
+    asm volatile("cvta.to.global.u64 %0, %1;" : "=l"(gsrc) : "l"(src));
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(dst)), "l"(gsrc), "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// Chunk c of a lane's data: bytes [128c, 128c + 128) from `src` (16-byte
+// aligned); 16-byte units at or past `avail` are zero-filled without a read.
+__device__ __forceinline__ void ring_fetch(uint32_t* ring, const uint8_t* src, uint32_t avail, uint32_t rot,
+                                           uint32_t c) {
+#pragma unroll
+    for (uint32_t u = 0; u < kLaneChunkWords / 4u; u++) {
+        const uint32_t off = c * (4u * kLaneChunkWords) + 16u * u;
+        const bool in = off < avail;
+        cp_async16(ring + ((c * kLaneChunkWords + 4u * u + rot) & (kLaneRingWords - 1u)), in ? src + off : src,
+                   in ? 16u : 0u);
+    }
+}
+
+// The BitWin cursor over a lane ring.
+struct RingWin {
+    const uint32_t* ring;
+    uint32_t rbase, pos, w0, w1, w2;
+    __device__ __forceinline__ uint32_t at(uint32_t i) const { return bswap32(ring[i & (kLaneRingWords - 1u)]); }
+    __device__ __forceinline__ void seek(uint32_t p) {
+        pos = p;
+        const uint32_t i = (p + rbase) >> 5;
+        w0 = at(i);
+        w1 = at(i + 1u);
+        w2 = at(i + 2u);
+    }
+    __device__ __forceinline__ uint32_t peek() const { return __funnelshift_l(w1, w0, (pos + rbase) & 31u); }
+    __device__ __forceinline__ void advance(uint32_t len) {
+        const uint32_t np = pos + len;
+        const uint32_t i = (np + rbase) >> 5;
+        const bool cross = i != ((pos + rbase) >> 5);
+        pos = np;
+        if (cross) {
+            w0 = w1;
+            w1 = w2;
+            w2 = at(i + 2u);
+        }
+    }
+    // rotated index of the next word the window will load
+    __device__ __forceinline__ uint32_t next_word() const { return ((pos + rbase) >> 5) + 3u; }
+};
 
 // ---------------------------------------------------------------------------
 // 1. scan kernel
@@ -290,12 +376,21 @@ __device__ __forceinline__ void lut_block(const DecodeArgs& a, uint32_t b, uint3
 
 // Blocks [0, nb) scan the meshlets; the blocks after them (lut_bx per mesh
 // with tables) fill the dequantisation tables in the same launch.
+//
+// Slots: the decode kernels take meshlets in groups of 32 slots, one lane
+// each, and a warp runs as many token iterations as its longest meshlet.
+// Each block therefore orders its 256 meshlets by token count (triangles
+// plus two per strip; ties by index) and slot i of the block holds the
+// meshlet of rank i, so a group's lanes have about the same work.  Outputs
+// are placed per meshlet, so the order changes no result.
 __global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a, uint32_t nb, uint32_t lut_bx) {
     if (blockIdx.x >= nb) {  // block-uniform
         lut_block(a, blockIdx.x - nb, lut_bx);
         return;
     }
     __shared__ unsigned long long wsum[kScanThreads / 32];
+    __shared__ __align__(16) uint32_t skey[kScanThreads];
+    __shared__ uint32_t sslot[kScanThreads];
     __shared__ int is_last;
     const uint32_t tid = threadIdx.x;
     const uint32_t m = blockIdx.x * kScanThreads + tid;
@@ -317,6 +412,23 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a, uint32
     unsigned long long t1, t2;
     const unsigned long long e1 = block_scan((static_cast<unsigned long long>(nt) << 32) | nl, wsum, t1);
     const unsigned long long e2 = block_scan((nl + 3u) & ~3u, wsum, t2);
+    // rank by (tokens, index); meshlets past the end rank last
+    {
+        const uint32_t tokens = nt + 2u * d.n_strips;  // <= 256 + 2 * 256
+        const uint32_t key = (m < a.total_meshlets ? tokens : 0xFFFFFFu) << 8 | tid;
+        skey[tid] = key;
+        __syncthreads();
+        uint32_t rank = 0u;
+        const uint4* k4 = reinterpret_cast<const uint4*>(skey);
+#pragma unroll 8
+        for (uint32_t j = 0; j < kScanThreads / 4u; j++) {
+            const uint4 q = k4[j];
+            rank += (q.x < key) + (q.y < key) + (q.z < key) + (q.w < key);
+        }
+        sslot[rank] = tid;
+        __syncthreads();
+        d.slot_meshlet = blockIdx.x * kScanThreads + sslot[tid];
+    }
     if (m < a.total_meshlets) {
         d.v_pref = static_cast<uint32_t>(e1);
         d.t_pref = static_cast<uint32_t>(e1 >> 32);
@@ -476,13 +588,12 @@ __device__ __forceinline__ void flush_walk(uint32_t* out, const uint32_t* ring, 
 // ---------------------------------------------------------------------------
 __host__ __device__ constexpr uint32_t align16(uint32_t x) { return (x + 15u) & ~15u; }
 
-// connectivity warp pair: stage | token records (two chunks) | chunk counts
-// (4 words) | first-occurrence bits (8 words per lane) | triangle ring |
-// walk ring | mbarrier
+// connectivity warp pair: lane byte rings | token records (two chunks) |
+// chunk counts (4 words) | first-occurrence bits (8 words per lane) |
+// triangle ring | walk ring.  22,544 bytes: five two-pair CTAs fit an SM.
 constexpr uint32_t kChunkWords = 16u;  // iterations per chunk (kChunk)
-__host__ __device__ inline uint32_t conn_pair_bytes(uint32_t stage_bytes) {
-    return align16(stage_bytes + 32u) + 2u * kChunkWords * 32u * 4u + 16u + 8u * 32u * 4u +
-           2u * 32u * kRingRow * 4u + 16u;
+__host__ __device__ constexpr uint32_t conn_pair_bytes() {
+    return 32u * kLaneRingWords * 4u + 2u * kChunkWords * 32u * 4u + 16u + 8u * 32u * 4u + 2u * 32u * kRingRow * 4u;
 }
 
 __host__ __device__ inline uint32_t vert_stage_bytes(uint32_t stage_bytes) { return stage_bytes / 2u; }
@@ -506,8 +617,9 @@ struct GroupLane {
 };
 
 __device__ __forceinline__ void load_group_lane(const DecodeArgs& a, uint32_t g, int lane, GroupLane& L) {
-    L.m = g * 32u + lane;
-    L.valid = L.m < a.total_meshlets;
+    const uint32_t slot = g * 32u + lane;
+    L.valid = slot < a.total_meshlets;
+    L.m = L.valid ? __ldcg(&a.descs[slot].slot_meshlet) : slot;
     if (L.valid) {
         const uint4* src = reinterpret_cast<const uint4*>(a.descs + L.m);
         uint4* dst = reinterpret_cast<uint4*>(&L.d);
@@ -554,36 +666,48 @@ __device__ __forceinline__ bool placement_ok(const DecodeArgs& a, const GroupLan
 // position in its strip (0..2 the three roots, 3 a strip-body token).
 constexpr uint32_t kChunk = kChunkWords;  // iterations per ring chunk
 constexpr uint32_t kChunkDone = 1u << 31;  // count word: the parser has finished
-constexpr uint32_t kChunkAbort = 1u << 30; // count word: the group was abandoned
 
-// Named barrier ids of pair p: full[0], full[1], empty[0], empty[1].
-__device__ __forceinline__ uint32_t bar_full(uint32_t pair, uint32_t c) { return 1u + 4u * pair + c; }
-__device__ __forceinline__ uint32_t bar_empty(uint32_t pair, uint32_t c) { return 3u + 4u * pair + c; }
+// Pair barrier slots: chunk c full, chunk c empty.
+__device__ __forceinline__ uint32_t bar_full(uint32_t c) { return c; }
+__device__ __forceinline__ uint32_t bar_empty(uint32_t c) { return 2u + c; }
 
-// Parser warp, one round.  `abort`: the stage never arrived; publish an
-// empty, abandoned round so that the assembler leaves too.
-template <bool kShared>
-__device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, const uint32_t* w, uint32_t rbase,
-                           uint32_t* recs, uint32_t* counts, uint32_t pair, bool abort, int lane) {
+// Parser warp.  Each active lane streams its meshlet's bytes through its
+// ring: chunks 0 and 1 before the first token, then after every record
+// chunk (at most kChunk tokens of at most 26 bits, i.e. 13 words) one more
+// chunk whenever fewer than 33 words lie ahead of the window.  The copies of
+// one refill are waited for at the next, so each has a full record chunk
+// of time to land; a refill overwrites the chunk two behind, which the
+// window has passed (its last words are in registers).
+template <int G>
+__device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, uint32_t* ring, uint32_t* recs,
+                           uint32_t* counts, uint32_t pair, int lane) {
     const uint32_t n_local = L.d.counts0 & 0xFFFFu;
     const uint32_t n_tris = L.d.counts0 >> 16;
     const uint32_t ib = max(1u, 32u - __clz(n_local));
     const uint32_t end = L.d.end_bit;
-    BitWin<kShared> win;  // the token cursor (win.pos)
-    win.w = w;
-    win.rbase = rbase;
+    const unsigned long long s0 = (L.blob_off + (L.d.start_bit >> 3)) & ~15ull;
+    const unsigned long long e16 = (L.blob_off + ((end + 7u) >> 3) + 15ull) & ~15ull;
+    const uint32_t avail = act ? static_cast<uint32_t>(e16 - s0) : 0u;  // inactive lanes read nothing
+    const uint8_t* src = a.arena + (act ? s0 : 0ull);
+    const uint32_t rot = (static_cast<uint32_t>(lane) * 4u) & 31u;
+    ring_fetch(ring, src, avail, rot, 0u);
+    ring_fetch(ring, src, avail, rot, 1u);
+    cp_async_wait_all();
+    uint32_t req = 2u;  // chunks requested
+    RingWin win;  // the token cursor (win.pos)
+    win.ring = ring;
+    win.rbase = static_cast<uint32_t>(L.blob_off * 8ull - s0 * 8ull) + 32u * rot;
     win.pos = win.w0 = win.w1 = win.w2 = 0u;
-    // only an active lane's bits are in the stage: an inactive lane reads nothing
-    if (act && !abort) win.seek(L.d.start_bit + 48u);
+    if (act) win.seek(L.d.start_bit + 48u);
     uint32_t strips_left = L.d.n_strips;
     uint32_t tok_left = 0u, tok_idx = 0u, tris = 0u;
     Fifo fifo;
     bool bad = false;
-    bool running = act && !abort && strips_left > 0u;
+    bool running = act && strips_left > 0u;
     uint32_t k = 0u;  // chunk
     for (;;) {
         const uint32_t c = k & 1u;
-        if (k >= 2u) named_sync(bar_empty(pair, c), 64);  // the assembler is done with chunk k - 2
+        if (k >= 2u) pair_bar<G, false>(pair, bar_empty(c));  // the assembler is done with chunk k - 2
         uint32_t* rc = recs + c * kChunk * 32u + lane;
         uint32_t n = 0u;
         while (n < kChunk && __any_sync(kFull, running)) {
@@ -628,15 +752,23 @@ __device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, co
             n++;
         }
         const bool done = !__any_sync(kFull, running);
-        if (lane == 0) counts[c] = n | (done ? kChunkDone : 0u) | (abort ? kChunkAbort : 0u);
-        named_arrive(bar_full(pair, c), 64);
+        if (lane == 0) counts[c] = n | (done ? kChunkDone : 0u);
+        pair_bar<G, true>(pair, bar_full(c));
         k++;
         if (done) break;
+        // refill (the previous refill has had a record chunk to land)
+        cp_async_wait_all();
+        if (running && kLaneChunkWords * req < win.next_word() - rot + 33u) {
+            ring_fetch(ring, src, avail, rot, req);
+            req++;
+        }
+        cp_async_commit();
     }
+    cp_async_wait_all();  // no copy may land after the CTA's shared memory is gone
     // take the assembler's remaining chunk releases: the ring and the
-    // barriers are clean for the next round
-    for (uint32_t j = k >= 2u ? k - 2u : 0u; j < k; j++) named_sync(bar_empty(pair, j & 1u), 64);
-    if (act && !abort) {
+    // barriers are clean
+    for (uint32_t j = k >= 2u ? k - 2u : 0u; j < k; j++) pair_bar<G, false>(pair, bar_empty(j & 1u));
+    if (act) {
         if (bad || tris != n_tris) {
             report(a.status, kErrCorrupt, L.m);
         } else {
@@ -645,8 +777,9 @@ __device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, co
     }
 }
 
-// Assembler warp, one round; returns true when the parser abandoned it.
-__device__ bool conn_assemble(const DecodeArgs& a, const GroupLane& L, bool act, uint32_t* seen, uint32_t* tring,
+// Assembler warp.
+template <int G>
+__device__ void conn_assemble(const DecodeArgs& a, const GroupLane& L, bool act, uint32_t* seen, uint32_t* tring,
                               uint32_t* wring, const uint32_t* recs, const uint32_t* counts, uint32_t pair,
                               int lane) {
 #pragma unroll
@@ -661,10 +794,9 @@ __device__ bool conn_assemble(const DecodeArgs& a, const GroupLane& L, bool act,
     uint32_t flush_in = kFlushEvery;
     uint32_t P = 0u;  // strip state p0 | p1 << 8 | p2 << 16
     uint32_t tcnt = 0u, wcnt = 0u, kind0 = 0u;
-    bool abort = false;
     for (uint32_t k = 0u;; k++) {
         const uint32_t c = k & 1u;
-        named_sync(bar_full(pair, c), 64);
+        pair_bar<G, false>(pair, bar_full(c));
         const uint32_t cw = counts[c];
         const uint32_t n = cw & (kChunk | (kChunk - 1u));
         const uint32_t* rc = recs + c * kChunk * 32u + lane;
@@ -704,40 +836,35 @@ __device__ bool conn_assemble(const DecodeArgs& a, const GroupLane& L, bool act,
                 }
             }
         }
-        named_arrive(bar_empty(pair, c), 64);
-        abort = (cw & kChunkAbort) != 0u;
+        pair_bar<G, true>(pair, bar_empty(c));
         if (cw & kChunkDone) break;
     }
-    if (act && !abort) {
+    if (act) {
         flush_tris(a.idx, L.t_base, tr, tf, tcnt, vloc, true);
         flush_walk(walk_out, wr, wf, wcnt, true);
         a.descs[L.m].walk = kind0 | (wcnt << 16);
     }
-    return abort;
 }
 
 // Pair p of a CTA (warps 2p and 2p + 1: parser, assembler) decodes group
-// blockIdx.x * G + p.  Past the kernel-entry barrier the pairs never wait
-// for one another, and the two warps of a pair run the same rounds (their
-// descriptors are the same) and the same chunk hand-over.
+// blockIdx.x * G + p in one round: every lane streams its own meshlet, so
+// no meshlet is too large.  Past the kernel-entry barrier the pairs never
+// wait for one another.
 template <int G>
-__global__ void __launch_bounds__(G * 64) conn_kernel(DecodeArgs a, uint32_t stage_bytes) {
+__global__ void __launch_bounds__(G * 64) conn_kernel(DecodeArgs a) {
     extern __shared__ __align__(128) uint8_t smem[];
     const uint32_t pair = threadIdx.x >> 6;
     const bool parser = ((threadIdx.x >> 5) & 1u) == 0u;
     const int lane = threadIdx.x & 31;
     const bool failed = *reinterpret_cast<volatile unsigned long long*>(&a.status->err) != 0ull;
     if (__syncthreads_or(failed)) return;
-    uint8_t* base = smem + pair * conn_pair_bytes(stage_bytes);
-    uint32_t* stage = reinterpret_cast<uint32_t*>(base);
-    uint32_t* recs = reinterpret_cast<uint32_t*>(base + align16(stage_bytes + 32u));
+    uint8_t* base = smem + pair * conn_pair_bytes();
+    uint32_t* rings = reinterpret_cast<uint32_t*>(base);
+    uint32_t* recs = rings + 32u * kLaneRingWords;
     uint32_t* counts = recs + 2u * kChunk * 32u;
     uint32_t* seen = counts + 4;
     uint32_t* tring = seen + 8 * 32;
     uint32_t* wring = tring + 32 * kRingRow;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(wring + 32 * kRingRow);
-    if (parser && lane == 0) mbar_init(bar);
-    __syncthreads();
     const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
     const uint32_t g = blockIdx.x * G + pair;
     if (g >= n_groups) return;  // both warps of the pair
@@ -748,47 +875,11 @@ __global__ void __launch_bounds__(G * 64) conn_kernel(DecodeArgs a, uint32_t sta
         if (parser) report(a.status, kErrCorrupt, L.m);
         ok = false;
     }
-    const unsigned long long start_b = L.blob_off + (L.d.start_bit >> 3);
-    const unsigned long long end16 = (L.blob_off + ((L.d.end_bit + 7u) >> 3) + 15ull) & ~15ull;
-    uint32_t phase = 0u;
-    uint32_t todo = __ballot_sync(kFull, ok);
-    while (todo) {
-        const int first = __ffs(todo) - 1;
-        const bool in = (todo >> lane) & 1u;
-        const unsigned long long s0 = shfl64(start_b, first) & ~15ull;
-        const bool fit = in && (end16 - s0) <= stage_bytes;
-        uint32_t rmask = __ballot_sync(kFull, fit);
-        const bool staged = rmask != 0u;
-        if (!staged) rmask = 1u << first;  // larger than the stage: read from global memory
-        todo &= ~rmask;
-        const bool act = (rmask >> lane) & 1u;
-        if (parser) {
-            bool abort = false;
-            if (staged) {
-                const int last = 31 - __clz(rmask);
-                const uint32_t bytes = static_cast<uint32_t>(shfl64(end16, last) - s0);
-                __syncwarp();
-                if (lane == 0) {
-                    mbar_expect(bar, bytes);
-                    bulk_copy(stage, a.arena + s0, bytes, bar);
-                }
-                abort = __any_sync(kFull, !mbar_wait(bar, phase));
-                if (abort) {
-                    if (lane == 0) report(a.status, kErrTimeout, L.m);
-                    mbar_wait(bar, phase);  // let the copy land before the CTA exits
-                }
-                phase ^= 1u;
-                conn_parse<true>(a, L, act, stage, static_cast<uint32_t>(L.blob_off * 8ull - s0 * 8ull), recs, counts,
-                                 pair, abort, lane);
-            } else {
-                conn_parse<false>(a, L, act, reinterpret_cast<const uint32_t*>(a.arena + L.blob_off), 0u, recs,
-                                  counts, pair, false, lane);
-            }
-            if (abort) return;  // the assembler has seen the abandoned round and leaves too
-        } else {
-            if (conn_assemble(a, L, act, seen, tring, wring, recs, counts, pair, lane)) return;
-        }
-        __syncwarp();
+    if (!__any_sync(kFull, ok)) return;  // both warps see the same lanes
+    if (parser) {
+        conn_parse<G>(a, L, ok, rings + lane * kLaneRingWords, recs, counts, pair, lane);
+    } else {
+        conn_assemble<G>(a, L, ok, seen, tring, wring, recs, counts, pair, lane);
     }
 }
 
@@ -1213,6 +1304,11 @@ cudaError_t opt_in_smem(K kernel, size_t smem, size_t* configured) {
         cudaError_t e =
             cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
         if (e != cudaSuccess) return e;
+        // the whole unified L1 as shared memory: both kernels read global
+        // data through L2 only, and the default split leaves room for one
+        // CTA fewer per SM than the shared-memory size allows
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+        if (e != cudaSuccess) return e;
         configured[dev] = smem;
     }
     return cudaSuccess;
@@ -1256,14 +1352,15 @@ __host__ __device__ constexpr int conn_pairs(int warps_per_cta) { return warps_p
 
 template <int G>
 cudaError_t launch_conn(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s) {
+    (void)cfg;
     static size_t configured[64] = {0};
-    const size_t smem = static_cast<size_t>(G) * conn_pair_bytes(cfg.stage_bytes);
+    const size_t smem = static_cast<size_t>(G) * conn_pair_bytes();
     cudaError_t e = opt_in_smem(conn_kernel<G>, smem, configured);
     if (e != cudaSuccess) return e;
     const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
     const uint32_t grid = (n_groups + G - 1) / G;
     if (grid == 0) return cudaSuccess;
-    conn_kernel<G><<<grid, G * 64, smem, s>>>(a, cfg.stage_bytes);
+    conn_kernel<G><<<grid, G * 64, smem, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -1292,7 +1389,7 @@ cudaError_t launch_pair(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t 
 }  // namespace
 
 size_t conn_smem_bytes(const LaunchCfg& cfg) {
-    return static_cast<size_t>(conn_pairs(cfg.warps_per_cta)) * conn_pair_bytes(cfg.stage_bytes);
+    return static_cast<size_t>(conn_pairs(cfg.warps_per_cta)) * conn_pair_bytes();
 }
 
 size_t vert_smem_bytes(const LaunchCfg& cfg) { return vert_cta_bytes(cfg.stage_bytes, cfg.code_bytes); }
