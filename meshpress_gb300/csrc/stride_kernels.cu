@@ -1077,7 +1077,9 @@ __device__ __forceinline__ void vert_axis(const DecodeArgs& a, const GroupLane& 
 }
 
 // Axis d of every vertex of the round's meshlets -> positions (and codes),
-// the warp working through one meshlet at a time.  The mesh's constants
+// the warp working through one meshlet at a time (n_local <= kMaxLocal, so
+// a meshlet's table reads all go out before its first store: one L2 round
+// trip per meshlet).  The mesh's constants
 // (table base, or float-float dequantisation coefficients) stay in registers
 // while consecutive meshlets belong to the same mesh.
 template <bool kWide>
@@ -1115,19 +1117,17 @@ __device__ void emit_axis(const DecodeArgs& a, const GroupLane& L, uint32_t rmas
         }
         const PlaneT<kWide>* pj = reinterpret_cast<const PlaneT<kWide>*>(planes + off);
         float* dst = a.pos + 3ull * vb + d;
-        if (has_lut) {  // four table reads in flight per lane
-            for (uint32_t v0 = 0; v0 < nv; v0 += 128u) {
-                float y[4];
+        if (has_lut) {  // every table read of the meshlet (<= 256 vertices) in flight at once
+            float y[kMaxLocal / 32];
 #pragma unroll
-                for (uint32_t k = 0; k < 4u; k++) {
-                    const uint32_t v = v0 + lane + 32u * k;
-                    y[k] = v < nv ? __ldcg(lut + min(static_cast<uint32_t>(pj[v]), qmax)) : 0.f;
-                }
+            for (uint32_t k = 0; k < kMaxLocal / 32u; k++) {
+                const uint32_t v = lane + 32u * k;
+                y[k] = v < nv ? __ldcg(lut + min(static_cast<uint32_t>(pj[v]), qmax)) : 0.f;
+            }
 #pragma unroll
-                for (uint32_t k = 0; k < 4u; k++) {
-                    const uint32_t v = v0 + lane + 32u * k;
-                    if (v < nv) dst[3u * v] = y[k];
-                }
+            for (uint32_t k = 0; k < kMaxLocal / 32u; k++) {
+                const uint32_t v = lane + 32u * k;
+                if (v < nv) dst[3u * v] = y[k];
             }
         } else {
             for (uint32_t v = lane; v < nv; v += 32u) {
