@@ -493,14 +493,18 @@ struct Fifo {
         const uint32_t b = (x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu;
         return ~(b | x) & m;
     }
-    // byte position of v among the valid entries, or 16
+    // byte position of v among the valid entries, or 16.  The valid entries
+    // are distinct, so at most one byte matches: its word i comes from which
+    // t is set, its byte j from the single bit 8j + 7 (2^(8j) * 0x00010203
+    // has j in its top byte) -- no bit-scan instruction on the chain.
     __device__ __forceinline__ uint32_t find(uint32_t v) const {
         const uint32_t vv = __byte_perm(v, 0u, 0u);
         const uint32_t t0 = match(f0, vv, m0), t1 = match(f1, vv, m1);
         const uint32_t t2 = match(f2, vv, m2), t3 = match(f3, vv, m3);
-        const uint32_t u = (t0 >> 7) | (t1 >> 6) | (t2 >> 5) | (t3 >> 4);  // bit 8j+i: word i, byte j
-        const uint32_t b = __ffs(u) - 1u;
-        return u ? 4u * (b & 7u) + (b >> 3) : 16u;
+        const uint32_t t = t0 | t1 | t2 | t3;
+        const uint32_t j = ((t >> 7) * 0x00010203u) >> 24;
+        const uint32_t i = ((t1 | t3) != 0u ? 1u : 0u) | ((t2 | t3) != 0u ? 2u : 0u);
+        return t ? 4u * i + j : 16u;
     }
     // remove the byte at p, shift the newer bytes down, append v as newest
     __device__ __forceinline__ void remove_append(uint32_t p, uint32_t v) {
@@ -616,6 +620,30 @@ struct GroupLane {
     unsigned long long blob_off;
 };
 
+// Order in which the decode kernels take groups.  The scan sorts each
+// 256-meshlet window ascending by token count, so a window's groups (eight)
+// grow costlier with their index; taking every window's last group first and
+// every window's first group last approximates costliest-first: the cheap
+// groups land on the CTAs dispatched last (the extra CTA some SMs get) and at
+// the end of the vertex kernel's work queue.  Entry f -> group; a bijection
+// of [0, n_groups).
+__device__ __forceinline__ uint32_t group_at(uint32_t f, uint32_t n_groups) {
+    constexpr uint32_t kPer = kScanThreads / 32u;  // groups per window
+    const uint32_t nw = (n_groups + kPer - 1u) / kPer;
+    const uint32_t q = n_groups - kPer * (nw - 1u);  // groups in the last window, 1..kPer
+    const uint32_t head = (kPer - q) * (nw - 1u);     // entries of the levels the last window lacks
+    uint32_t l, w;
+    if (f < head) {
+        l = kPer - 1u - f / (nw - 1u);
+        w = f % (nw - 1u);
+    } else {
+        const uint32_t r = f - head;
+        l = q - 1u - r / nw;
+        w = r % nw;
+    }
+    return kPer * w + l;
+}
+
 __device__ __forceinline__ void load_group_lane(const DecodeArgs& a, uint32_t g, int lane, GroupLane& L) {
     const uint32_t slot = g * 32u + lane;
     L.valid = slot < a.total_meshlets;
@@ -704,13 +732,19 @@ __device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
     Fifo fifo;
     bool bad = false;
     bool running = act && strips_left > 0u;
+    // A strip of length len takes len + 2 tokens and adds len triangles (one
+    // for len 0), and a lane stops once its triangles would pass n_tris, so
+    // n_tris + 2 n_strips iterations finish (or fail) every lane: the warp
+    // runs the largest of those counts instead of voting every iteration.
+    const uint32_t iters = __reduce_max_sync(kFull, act ? n_tris + 2u * L.d.n_strips : 0u);
+    uint32_t it = 0u;
     uint32_t k = 0u;  // chunk
     for (;;) {
         const uint32_t c = k & 1u;
         if (k >= 2u) pair_bar<G, false>(pair, bar_empty(c));  // the assembler is done with chunk k - 2
         uint32_t* rc = recs + c * kChunk * 32u + lane;
-        uint32_t n = 0u;
-        while (n < kChunk && __any_sync(kFull, running)) {
+        const uint32_t n = min(kChunk, iters - it);
+        for (uint32_t i = 0; i < n; i++) {
             uint32_t rec = 0u;
             if (running) {
                 // a 32-bit window holds a strip header (16 bits) plus the next
@@ -736,6 +770,8 @@ __device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
                 used += raw ? 1u + ib : 6u;
                 // decode_dup raises IndexError on both (FIFO index, local id)
                 const bool invalid = (raw ? rid >= n_local : fi >= fifo.len) | (tris > n_tris);
+                // (find also for FIFO tokens, whose position is known: selecting
+                // between the two compiles to a divergent branch, which costs more)
                 const uint32_t v = raw ? (rid & 0xFFu) : fifo.at((16u - fifo.len + fi) & 15u);
                 const uint32_t at = fifo.find(v);
                 const uint32_t rm = at < 16u ? at : (fifo.len >= 15u ? 0u : 15u - fifo.len);
@@ -748,10 +784,10 @@ __device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
                 bad = bad | invalid | (win.pos > end);
                 running = !bad & ((tok_left | strips_left) != 0u);
             }
-            rc[n * 32u] = rec;
-            n++;
+            rc[i * 32u] = rec;
         }
-        const bool done = !__any_sync(kFull, running);
+        it += n;
+        const bool done = it >= iters;
         if (lane == 0) counts[c] = n | (done ? kChunkDone : 0u);
         pair_bar<G, true>(pair, bar_full(c));
         k++;
@@ -765,6 +801,7 @@ __device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
         cp_async_commit();
     }
     cp_async_wait_all();  // no copy may land after the CTA's shared memory is gone
+    bad = bad | running;      // cannot happen: the count bounds every lane
     // take the assembler's remaining chunk releases: the ring and the
     // barriers are clean
     for (uint32_t j = k >= 2u ? k - 2u : 0u; j < k; j++) pair_bar<G, false>(pair, bar_empty(j & 1u));
@@ -866,8 +903,9 @@ __global__ void __launch_bounds__(G * 64) conn_kernel(DecodeArgs a) {
     uint32_t* tring = seen + 8 * 32;
     uint32_t* wring = tring + 32 * kRingRow;
     const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
-    const uint32_t g = blockIdx.x * G + pair;
-    if (g >= n_groups) return;  // both warps of the pair
+    const uint32_t f = blockIdx.x * G + pair;
+    if (f >= n_groups) return;  // both warps of the pair
+    const uint32_t g = group_at(f, n_groups);
     GroupLane L;
     load_group_lane(a, g, lane, L);
     bool ok = L.valid;
@@ -1213,13 +1251,14 @@ __global__ void __launch_bounds__(96, 1) vert_kernel(DecodeArgs a, uint32_t stag
     __syncthreads();
     uint32_t phase = 0u;
     const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
-    uint32_t g = blockIdx.x;
+    uint32_t f = blockIdx.x;  // position in the group order
     if (persistent) {
         if (threadIdx.x == 0) s_group = atomicAdd(&a.status->work_vert, 1u);
         __syncthreads();
-        g = s_group;
+        f = s_group;
     }
-    while (g < n_groups) {
+    while (f < n_groups) {
+        const uint32_t g = group_at(f, n_groups);
         GroupLane L;
         load_group_lane(a, g, lane, L);
         const uint32_t n_local = L.d.counts0 & 0xFFFFu;
@@ -1288,7 +1327,7 @@ __global__ void __launch_bounds__(96, 1) vert_kernel(DecodeArgs a, uint32_t stag
         __syncthreads();  // every thread has read s_group
         if (threadIdx.x == 0) s_group = atomicAdd(&a.status->work_vert, 1u);
         __syncthreads();
-        g = s_group;
+        f = s_group;
     }
 }
 
