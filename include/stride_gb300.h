@@ -73,9 +73,12 @@ typedef struct {
     int32_t persistent;      /* 1 = persistent work-stealing vertex grid     */
     int32_t ctas_per_sm;     /* persistent grid = ctas_per_sm * SMs
                                 (0 = as many as fit)                         */
-    uint32_t stage_bytes;    /* shared-memory staging of a group's bytes
-                                (the vertex kernel stages half of this)      */
-    uint32_t code_bytes;     /* shared-memory code plane of one axis warp    */
+    uint32_t stage_bytes;    /* the vertex kernel stages a round's residual
+                                bits in half of this (the connectivity
+                                kernel streams each meshlet through fixed
+                                256-byte per-lane rings)                     */
+    uint32_t code_bytes;     /* shared-memory code plane of one axis warp
+                                (>= 516, or 1028 above 16-bit codes)        */
 } stride_launch_cfg;
 
 /* Thread-local description of the last error in this thread. */

@@ -1063,9 +1063,9 @@ __device__ __forceinline__ void vert_axis(const DecodeArgs& a, const GroupLane& 
     const uint32_t end = L.d.end_bit;
     const MeshParams* P = L.P;
     if (n_walk < n_local) {  // vertices the walk never reaches keep code 0
-        uint4* z = reinterpret_cast<uint4*>(plane);
-        const uint32_t nz = (n_local * static_cast<uint32_t>(sizeof(PlaneT<kWide>)) + 15u) >> 4;
-        for (uint32_t i = 0; i < nz; i++) z[i] = make_uint4(0u, 0u, 0u, 0u);
+        uint32_t* z = reinterpret_cast<uint32_t*>(plane);
+        const uint32_t nz = (n_local * static_cast<uint32_t>(sizeof(PlaneT<kWide>)) + 3u) >> 2;
+        for (uint32_t i = 0; i < nz; i++) z[i] = 0u;
     }
     const int32_t n0 = P->pred_n[3 * d], n1 = P->pred_n[3 * d + 1], n2 = P->pred_n[3 * d + 2];
     const int32_t K = P->pred_k[d], half = P->pred_half[d];
@@ -1271,13 +1271,21 @@ __global__ void __launch_bounds__(96, 1) vert_kernel(DecodeArgs a, uint32_t stag
         const unsigned long long src16 = (L.blob_off + (L.d.anchor_bit >> 3)) & ~15ull;
         const unsigned long long end16 = (L.blob_off + ((L.d.end_bit + 7u) >> 3) + 15ull) & ~15ull;
         const uint32_t ssz = ok ? static_cast<uint32_t>(end16 - src16) : 0u;
-        const uint32_t csz = align16(n_local * static_cast<uint32_t>(sizeof(PlaneT<kWide>)));
+        // its stage region: an odd number of 16-byte units, for the reason
+        // the code planes have odd word counts (lanes read at about the same
+        // offsets at the same time)
+        const uint32_t sreg = ssz + ((ssz & 16u) ? 0u : 16u);
+        // A lane's code plane is an odd number of words: the walk visits local
+        // ids in about the same order in every meshlet, so the lanes read and
+        // write at about the same offsets at the same time, and odd strides
+        // put those offsets in different banks (16-byte strides used 8).
+        const uint32_t csz = 4u * (((n_local * static_cast<uint32_t>(sizeof(PlaneT<kWide>)) + 3u) >> 2) | 1u);
         // the three warps see the same descriptors, so they form the same rounds
         uint32_t todo = __ballot_sync(kFull, ok);
         while (todo) {
             const int first = __ffs(todo) - 1;
             const bool in = (todo >> lane) & 1u;
-            uint32_t cc = in ? csz : 0u, cs = in ? ssz : 0u;
+            uint32_t cc = in ? csz : 0u, cs = in ? sreg : 0u;
 #pragma unroll
             for (int o = 1; o < 32; o <<= 1) {
                 const uint32_t t1 = __shfl_up_sync(kFull, cc, o);
@@ -1298,9 +1306,9 @@ __global__ void __launch_bounds__(96, 1) vert_kernel(DecodeArgs a, uint32_t stag
             const bool act = (rmask >> lane) & 1u;
             const uint32_t code_off = act ? cc - csz : 0u;
             if (staged) {
-                const int last = 31 - __clz(rmask);
-                const uint32_t total = __shfl_sync(kFull, cs, last);
-                const uint32_t dst_off = act ? cs - ssz : 0u;
+                // bytes the copies deliver (the regions' padding is not copied)
+                const uint32_t total = __reduce_add_sync(kFull, act ? ssz : 0u);
+                const uint32_t dst_off = act ? cs - sreg : 0u;
                 if (d == 0u) {
                     if (lane == 0) mbar_expect(bar, total);
                     __syncwarp();
@@ -1448,7 +1456,8 @@ int device_sm_count() {
 
 int check_config(const LaunchCfg& cfg, bool wide) {
     if (cfg.warps_per_cta != 1 && cfg.warps_per_cta != 2 && cfg.warps_per_cta != 4) return STRIDE_ERR_ARG;
-    if (cfg.code_bytes < kMaxLocal * (wide ? 4u : 2u) || cfg.stage_bytes < 256u) return STRIDE_ERR_ARG;
+    // one meshlet of kMaxLocal vertices, its plane padded to an odd word count
+    if (cfg.code_bytes < kMaxLocal * (wide ? 4u : 2u) + 4u || cfg.stage_bytes < 256u) return STRIDE_ERR_ARG;
     if (conn_smem_bytes(cfg) > 227u * 1024u || vert_smem_bytes(cfg) > 227u * 1024u) return STRIDE_ERR_ARG;
     return STRIDE_OK;
 }

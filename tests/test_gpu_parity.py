@@ -118,7 +118,7 @@ def _cfg(w, pers, stage, code, per_sm=0):
 @pytest.mark.parametrize("cfg", [
     (1, 0, 20 * 1024, 16 * 1024), (2, 0, 16 * 1024, 8 * 1024), (4, 1, 12 * 1024, 6 * 1024),
     (1, 1, 256, 2048),           # tiny stage: meshlets fall back to global reads
-    (2, 0, 64 * 1024, 512),      # code plane of one 256-vertex meshlet: one meshlet per round
+    (2, 0, 64 * 1024, 516),      # code plane of one 256-vertex meshlet (odd word count): one per round
 ], ids=["w1", "w2", "w4p", "global_reads", "one_per_round"])
 def test_launch_shapes_give_identical_output(torch_cuda, cfg):
     V, T = synth.icosphere(5, seed=11)
@@ -127,7 +127,7 @@ def test_launch_shapes_give_identical_output(torch_cuda, cfg):
     assert_same_as_oracle(e.data, pos, idx, codes)
 
 
-@pytest.mark.parametrize("cfg", [(2, 1, 16 * 1024, 1024), (1, 0, 256, 32 * 1024)], ids=["one_per_round", "global_reads"])
+@pytest.mark.parametrize("cfg", [(2, 1, 16 * 1024, 1028), (1, 0, 256, 32 * 1024)], ids=["one_per_round", "global_reads"])
 def test_wide_codes_launch_shapes(torch_cuda, cfg):
     """20-bit codes (32-bit code plane) under the smallest plane and stage."""
     V, T = synth.heightfield_grid(129, seed=6)
