@@ -51,12 +51,16 @@ __device__ __forceinline__ uint32_t bswap32(uint32_t x) { return __byte_perm(x, 
 // rewrites arena ranges (streams, mesh tables, dequantisation tables) for a
 // new launch while launches on other streams may still run on the same SMs,
 // so nothing may be served from an SM's L1 or read-only cache.
+//
+// ldw returns word i in bit order (the stream's first bit as the MSB).  The
+// vertex kernel's stage is put in bit order once when it lands, so reads
+// from it need no byte swap; global words are swapped as they are read.
 template <bool kShared>
 __device__ __forceinline__ uint32_t ldw(const uint32_t* w, uint32_t i) {
     if constexpr (kShared) {
         return w[i];
     } else {
-        return __ldcg(w + i);
+        return bswap32(__ldcg(w + i));
     }
 }
 
@@ -64,8 +68,8 @@ __device__ __forceinline__ uint32_t ldw(const uint32_t* w, uint32_t i) {
 template <bool kShared>
 __device__ __forceinline__ uint32_t peek32(const uint32_t* w, uint32_t rel) {
     const uint32_t i = rel >> 5;
-    const uint32_t hi = bswap32(ldw<kShared>(w, i));
-    const uint32_t lo = bswap32(ldw<kShared>(w, i + 1));
+    const uint32_t hi = ldw<kShared>(w, i);
+    const uint32_t lo = ldw<kShared>(w, i + 1);
     return __funnelshift_l(lo, hi, rel & 31u);
 }
 
@@ -137,9 +141,9 @@ struct BitWin {
     __device__ __forceinline__ void seek(uint32_t p) {
         pos = p;
         const uint32_t i = (p + rbase) >> 5;
-        w0 = bswap32(ldw<kShared>(w, i));
-        w1 = bswap32(ldw<kShared>(w, i + 1u));
-        w2 = bswap32(ldw<kShared>(w, i + 2u));
+        w0 = ldw<kShared>(w, i);
+        w1 = ldw<kShared>(w, i + 1u);
+        w2 = ldw<kShared>(w, i + 2u);
     }
     __device__ __forceinline__ uint32_t peek() const { return __funnelshift_l(w1, w0, (pos + rbase) & 31u); }
     // len <= 32: crosses at most one word boundary
@@ -151,7 +155,7 @@ struct BitWin {
         if (cross) {
             w0 = w1;
             w1 = w2;
-            w2 = bswap32(ldw<kShared>(w, i + 2u));
+            w2 = ldw<kShared>(w, i + 2u);
         }
     }
 };
@@ -1322,6 +1326,11 @@ __global__ void __launch_bounds__(96, 1) vert_kernel(DecodeArgs a, uint32_t stag
                     return;
                 }
                 phase ^= 1u;
+                {  // the round's stage in bit order, once for the three warps
+                    const uint32_t words = __shfl_sync(kFull, cs, 31 - __clz(rmask)) >> 2;
+                    for (uint32_t i = threadIdx.x; i < words; i += 96u) stage[i] = bswap32(stage[i]);
+                    __syncthreads();
+                }
                 const uint32_t rbase = static_cast<uint32_t>(L.blob_off * 8ull - src16 * 8ull + dst_off * 8ull);
                 vert_round<true, kWide>(a, L, d, act, rmask, stage, rbase, planes, code_off, lane);
             } else {
