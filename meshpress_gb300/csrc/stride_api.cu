@@ -181,7 +181,28 @@ struct stride_handle {
     cudaEvent_t done = nullptr;
     bool launched = false;
     LaunchCfg cfg;
+    // stride_decode_host: copy streams and the events they wait on
+    cudaStream_t copy[2] = {nullptr, nullptr};
+    cudaEvent_t conn_done = nullptr, vert_done = nullptr, copied[2] = {nullptr, nullptr};
 };
+
+static void free_copy_streams(stride_handle* h) {
+    for (auto& c : h->copy)
+        if (c) cudaStreamDestroy(c), c = nullptr;
+    for (cudaEvent_t* e : {&h->conn_done, &h->vert_done, &h->copied[0], &h->copied[1]})
+        if (*e) cudaEventDestroy(*e), *e = nullptr;
+}
+
+static cudaError_t make_copy_streams(stride_handle* h) {
+    if (h->copy[0]) return cudaSuccess;
+    cudaError_t e = cudaSuccess;
+    for (auto& c : h->copy)
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking);
+    for (cudaEvent_t* ev : {&h->conn_done, &h->vert_done, &h->copied[0], &h->copied[1]})
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) free_copy_streams(h);
+    return e;
+}
 
 static void free_buffers(stride_handle* h) {
     cudaFree(h->d_blob);
@@ -467,13 +488,33 @@ int stride_decode_host(stride_handle* h, void* stream, uint32_t* h_idx, float* h
         if ((e = cudaMalloc(&h->d_idx, 12 * h->params.n_t)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(idx)");
         h->cap_t = h->params.n_t;
     }
-    int rc = stride_decode(h, stream, h->d_idx, h->d_pos, nullptr);
-    if (rc) return rc;
+    if ((e = make_copy_streams(h)) != cudaSuccess) return cuda_fail(e, "copy streams");
+    // The triangle indices are final when the connectivity kernel ends, so
+    // their copy to the host runs beside the vertex kernel; each output goes
+    // out in two halves on the handle's two copy streams (two copy engines).
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    if ((e = cudaMemcpyAsync(h_idx, h->d_idx, 12 * h->params.n_t, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(h_pos, h->d_pos, 12 * h->params.n_v, cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-        (e = cudaEventRecord(h->done, s)) != cudaSuccess)
-        return cuda_fail(e, "stride_decode_host copy");
+    void* ev[4] = {nullptr, nullptr, h->conn_done, h->vert_done};
+    int rc = enqueue_decode(handle_args(h, h->d_idx, h->d_pos, nullptr), h->cfg, stream, ev);
+    if (rc) return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    h->launched = true;
+    const size_t ib = 12 * h->params.n_t, pb = 12 * h->params.n_v;
+    const size_t ih = (ib / 2) & ~size_t(15), ph = (pb / 2) & ~size_t(15);
+    const size_t ioff[2] = {0, ih}, ilen[2] = {ih, ib - ih};
+    const size_t poff[2] = {0, ph}, plen[2] = {ph, pb - ph};
+    for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+        cudaStream_t c = h->copy[k];
+        if ((e = cudaStreamWaitEvent(c, h->conn_done, 0)) == cudaSuccess && ilen[k])
+            e = cudaMemcpyAsync(reinterpret_cast<uint8_t*>(h_idx) + ioff[k],
+                                reinterpret_cast<const uint8_t*>(h->d_idx) + ioff[k], ilen[k], cudaMemcpyDeviceToHost, c);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c, h->vert_done, 0);
+        if (e == cudaSuccess && plen[k])
+            e = cudaMemcpyAsync(reinterpret_cast<uint8_t*>(h_pos) + poff[k],
+                                reinterpret_cast<const uint8_t*>(h->d_pos) + poff[k], plen[k], cudaMemcpyDeviceToHost, c);
+        if (e == cudaSuccess) e = cudaEventRecord(h->copied[k], c);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, h->copied[k], 0);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(h->done, s);
+    if (e != cudaSuccess) return cuda_fail(e, "stride_decode_host copy");
     return stride_status(h, 1, nullptr);
 }
 
@@ -495,6 +536,7 @@ void stride_close(stride_handle* h) {
     if (!h) return;
     if (h->launched) cudaEventSynchronize(h->done);
     if (h->done) cudaEventDestroy(h->done);
+    free_copy_streams(h);
     free_buffers(h);
     delete h;
 }

@@ -149,8 +149,9 @@ inline unsigned long long walk_scratch_words(unsigned long long n_v, unsigned lo
 int parse_header(const uint8_t* data, size_t len, MeshParams* p, char* why, size_t why_len);
 
 // Enqueue scan + connectivity + vertex kernels for `a` on `stream`.  When
-// `ev` is non-null, four events are recorded: before the scan kernel,
-// after it, after the connectivity kernel and after the vertex kernel.
+// `ev` is non-null, its non-null entries of four are recorded: before the
+// scan kernel, after it, after the connectivity kernel and after the vertex
+// kernel.
 int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void* const* ev = nullptr);
 
 // STRIDE_OK when `cfg` is a launchable shape.

@@ -1434,11 +1434,16 @@ cudaError_t launch_vert(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t 
     return cudaGetLastError();
 }
 
+// ev[k] is recorded when ev and ev[k] are non-null
+void record(void* const* ev, int k, cudaStream_t s) {
+    if (ev && ev[k]) cudaEventRecord(static_cast<cudaEvent_t>(ev[k]), s);
+}
+
 template <int W>
 cudaError_t launch_pair(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s, void* const* ev) {
     cudaError_t e = launch_conn<conn_pairs(W)>(a, cfg, s);
     if (e != cudaSuccess) return e;
-    if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[2]), s);
+    record(ev, 2, s);
     return a.wide_codes ? launch_vert<true>(a, cfg, s) : launch_vert<false>(a, cfg, s);
 }
 
@@ -1475,7 +1480,7 @@ int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (check_config(cfg, a.wide_codes)) return STRIDE_ERR_ARG;
     if (cudaMemsetAsync(a.status, 0, sizeof(Status), s) != cudaSuccess) return STRIDE_ERR_CUDA;
-    if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[0]), s);
+    record(ev, 0, s);
     {
         const uint32_t nb = scan_blocks(a.total_meshlets);
         const uint32_t lut_bx = (a.lut_max + 255u) / 256u;
@@ -1486,7 +1491,7 @@ int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void
             if (cudaGetLastError() != cudaSuccess) return STRIDE_ERR_CUDA;
         }
     }
-    if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[1]), s);
+    record(ev, 1, s);
     if (a.total_meshlets != 0) {
         cudaError_t e;
         switch (cfg.warps_per_cta) {
@@ -1496,9 +1501,9 @@ int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void
         }
         if (e != cudaSuccess) return STRIDE_ERR_CUDA;
     } else if (ev) {
-        cudaEventRecord(static_cast<cudaEvent_t>(ev[2]), s);
+        record(ev, 2, s);
     }
-    if (ev) cudaEventRecord(static_cast<cudaEvent_t>(ev[3]), s);
+    record(ev, 3, s);
     return STRIDE_OK;
 }
 
