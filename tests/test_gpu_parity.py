@@ -76,6 +76,26 @@ def test_decode_to_host_and_device_agree(torch_cuda):
         assert np.array_equal(p2.view(np.uint32), pos.view(np.uint32)) and np.array_equal(i2, idx)
 
 
+def test_decode_to_host_pinned_overlap(torch_cuda):
+    """Pinned host outputs: the index copy runs beside the vertex kernel on
+    the handle's copy streams; results equal the device decode bit for bit."""
+    torch = torch_cuda
+    from meshpress_gb300 import ParaDeltaV5GpuDecoder
+    V, T = synth.noise_heightfield(513, seed=4)
+    data = encoder.encode(V, T, precision_error=B12, precision_mode="bbox_frac").data
+    dec = ParaDeltaV5GpuDecoder(data)
+    tris, verts = dec.decode_to_device()
+    h_pos = torch.empty((dec.n_v_total, 3), dtype=torch.float32, pin_memory=True)
+    h_idx = torch.empty((dec.n_t_total, 3), dtype=torch.int32, pin_memory=True)
+    for _ in range(3):
+        h_pos.fill_(float("nan"))
+        h_idx.fill_(-1)
+        pos, idx = dec.decode_to_host(out=(h_pos.numpy(), h_idx.numpy().view(np.uint32)))
+        assert np.array_equal(pos.view(np.uint32), verts.cpu().numpy().view(np.uint32))
+        assert np.array_equal(idx, tris.view(torch.int32).cpu().numpy().view(np.uint32))
+    dec.close()
+
+
 ENC_CASES = {
     "grid129_b12": (lambda: synth.heightfield_grid(129, seed=1), dict(precision_error=B12, precision_mode="bbox_frac")),
     "grid257_b10": (lambda: synth.noise_heightfield(257, seed=5), dict(precision_error=synth.bbox_bits_error(10),
