@@ -327,10 +327,12 @@ int stride_batch_autotune(stride_batch* b, void* stream, uint32_t* d_idx, float*
     if (iters < 1) iters = 3;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     std::vector<LaunchCfg> cands;
-    const uint32_t stage_opts[] = {8u * 1024u, 12u * 1024u, 16u * 1024u, 24u * 1024u};
+    // the vertex kernel stages half of stage_bytes
+    const uint32_t stage_opts[] = {8u * 1024u, 10u * 1024u, 12u * 1024u, 16u * 1024u, 24u * 1024u};
     // code plane per warp: 2 bytes per vertex (4 above 16-bit codes), 32
-    // meshlets of up to 256 vertices fill 16 KiB
-    const uint32_t code_opts[] = {6u * 1024u, 8u * 1024u, 10u * 1024u, 12u * 1024u, 16u * 1024u};
+    // meshlets of up to 256 vertices fill 16 KiB; 10.5 KiB planes with a
+    // 5 KiB stage are the largest that fit six vertex CTAs on an SM
+    const uint32_t code_opts[] = {6u * 1024u, 8u * 1024u, 10u * 1024u, 10752u, 11u * 1024u, 12u * 1024u, 16u * 1024u};
     for (int w : {1, 2, 4})
         for (uint32_t st : stage_opts)
             for (uint32_t cb : code_opts)

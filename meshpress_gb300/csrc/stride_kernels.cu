@@ -1239,7 +1239,7 @@ __device__ __forceinline__ void vert_round(const DecodeArgs& a, const GroupLane&
 // A CTA decodes one group of 32 meshlets with three warps, warp d = axis d;
 // the group's residual bits are staged once and read by all three.
 template <bool kWide>
-__global__ void __launch_bounds__(96, 1) vert_kernel(DecodeArgs a, uint32_t stage_bytes, uint32_t code_bytes,
+__global__ void __maxnreg__(112) vert_kernel(DecodeArgs a, uint32_t stage_bytes, uint32_t code_bytes,
                                                   int persistent) {
     extern __shared__ __align__(128) uint8_t smem[];
     __shared__ uint32_t s_group;
