@@ -1060,8 +1060,9 @@ __device__ __forceinline__ uint32_t vert_header(const GroupLane& L, uint32_t d, 
 // load); entries past the end are masked, not branched around, and root and
 // parallelogram vertices differ only in selects.
 template <bool kShared, bool kWide>
-__device__ __forceinline__ void vert_axis(const DecodeArgs& a, const GroupLane& L, uint32_t d, const uint32_t* w,
-                                          uint32_t rbase, PlaneT<kWide>* plane, VertLane& S) {
+__device__ __forceinline__ void vert_axis(const DecodeArgs& a, const GroupLane& L, uint32_t d,
+                                          const uint32_t* __restrict__ w, uint32_t rbase,
+                                          PlaneT<kWide>* __restrict__ plane, VertLane& S) {
     const uint32_t n_local = L.d.counts0 & 0xFFFFu;
     const uint32_t n_walk = L.d.walk >> 16;
     const uint32_t end = L.d.end_bit;
@@ -1239,7 +1240,7 @@ __device__ __forceinline__ void vert_round(const DecodeArgs& a, const GroupLane&
 // A CTA decodes one group of 32 meshlets with three warps, warp d = axis d;
 // the group's residual bits are staged once and read by all three.
 template <bool kWide>
-__global__ void __maxnreg__(112) vert_kernel(DecodeArgs a, uint32_t stage_bytes, uint32_t code_bytes,
+__global__ void __launch_bounds__(96, 1) vert_kernel(DecodeArgs a, uint32_t stage_bytes, uint32_t code_bytes,
                                                   int persistent) {
     extern __shared__ __align__(128) uint8_t smem[];
     __shared__ uint32_t s_group;
