@@ -282,7 +282,7 @@ __device__ __forceinline__ void ring_fetch(uint32_t* ring, const uint8_t* src, u
 
 // The BitWin cursor over a lane ring.
 struct RingWin {
-    const uint32_t* ring;
+    const uint32_t* __restrict__ ring;
     uint32_t rbase, pos, w0, w1, w2;
     __device__ __forceinline__ uint32_t at(uint32_t i) const { return bswap32(ring[i & (kLaneRingWords - 1u)]); }
     __device__ __forceinline__ void seek(uint32_t p) {
@@ -711,8 +711,8 @@ __device__ __forceinline__ uint32_t bar_empty(uint32_t c) { return 2u + c; }
 // of time to land; a refill overwrites the chunk two behind, which the
 // window has passed (its last words are in registers).
 template <int G>
-__device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, uint32_t* ring, uint32_t* recs,
-                           uint32_t* counts, uint32_t pair, int lane) {
+__device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, uint32_t* __restrict__ ring,
+                           uint32_t* __restrict__ recs, uint32_t* __restrict__ counts, uint32_t pair, int lane) {
     const uint32_t n_local = L.d.counts0 & 0xFFFFu;
     const uint32_t n_tris = L.d.counts0 >> 16;
     const uint32_t ib = max(1u, 32u - __clz(n_local));
@@ -820,8 +820,9 @@ __device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
 
 // Assembler warp.
 template <int G>
-__device__ void conn_assemble(const DecodeArgs& a, const GroupLane& L, bool act, uint32_t* seen, uint32_t* tring,
-                              uint32_t* wring, const uint32_t* recs, const uint32_t* counts, uint32_t pair,
+__device__ void conn_assemble(const DecodeArgs& a, const GroupLane& L, bool act, uint32_t* __restrict__ seen,
+                              uint32_t* __restrict__ tring, uint32_t* __restrict__ wring,
+                              const uint32_t* __restrict__ recs, const uint32_t* __restrict__ counts, uint32_t pair,
                               int lane) {
 #pragma unroll
     for (int i = 0; i < 8; i++) seen[i * 32 + lane] = 0u;
