@@ -5,4 +5,4 @@ Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 (``meshpress_gb300``) never imports it.
 """
 from .oracle import (OracleError, bitcodec_read, decode, decode_mt,  # noqa: F401
-                     parse_header, build, library_path)
+                     parse_header, build, library_path, side_table)

@@ -69,6 +69,7 @@ def _load():
                                      ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
         lib.so_bitcodec_read.argtypes = [u8p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
                                          ctypes.c_int32, ctypes.c_void_p]
+        lib.so_side_table.argtypes = [u8p, ctypes.c_uint64] + [ctypes.c_void_p] * 7
         _lib = lib
     return _lib
 
@@ -162,3 +163,22 @@ def bitcodec_read(data: bytes, ops):
     _check(lib.so_bitcodec_read(p, len(arr), kinds.ctypes.data, ks.ctypes.data,
                                 len(ops), out.ctypes.data))
     return [int(x) for x in out]
+
+
+def side_table(data: bytes):
+    """Per-meshlet side table of the reference GPU harness's blob, from the
+    DPR4 bytes: start_bit, n_local, n_tris, n_strips, resid_bit (the anchor),
+    n_kind0 and sub_offs (M, 5) -- starts of dy, dz, px, py, pz relative to
+    the anchor.  Bit positions are absolute in ``data``."""
+    lib = _load()
+    h = parse_header(data)
+    arr, p = _buf(data)
+    M = h.n_meshlets
+    out = {"start_bit": np.zeros(M, np.uint64), "n_local": np.zeros(M, np.uint32),
+           "n_tris": np.zeros(M, np.uint32), "n_strips": np.zeros(M, np.uint32),
+           "resid_bit": np.zeros(M, np.uint64), "n_kind0": np.zeros(M, np.uint32),
+           "sub_offs": np.zeros((M, 5), np.uint16)}
+    _check(lib.so_side_table(p, len(arr), *[out[k].ctypes.data for k in
+                                            ("start_bit", "n_local", "n_tris", "n_strips", "resid_bit",
+                                             "n_kind0", "sub_offs")]))
+    return out

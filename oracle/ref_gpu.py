@@ -1,0 +1,168 @@
+"""The reference's own CUDA decoder, run on this GPU as a baseline.
+
+TEST INFRASTRUCTURE ONLY (used by tests/test_gpu_reference_kernel.py).
+The reference ships a STRIDE decode-throughput harness,
+bench_cpp/stride_dup_decode_bench.cu: one warp per meshlet, lane 0 parses
+the connectivity, lanes 0-2 the three axes, lane 0 predicts, the warp
+writes fp32 positions and uint32 indices.  Its kernel is not bit-exact by
+design (fp32 dequantisation, int16 code storage) and it reads a side table
+that is not in the DPR4 bytes (per-meshlet residual offsets and substream
+sub-offsets, written by the reference's scripts/dump_stride_dup_blob.py
+from encoder metadata).
+
+build() compiles that kernel, unmodified, from the reference source into a
+cubin (oracle/_ref/, git-ignored; it travels with the tree to the GPU
+machine, where the reference sources do not exist).  RefKernel loads the
+cubin with the CUDA driver API, derives the side table from the DPR4 bytes
+with the C oracle (so_side_table), and launches the kernel the way the
+reference harness does (stride_dup_decode_bench.cu:662-685): a persistent
+grid of min(n_meshlets, 16 x SMs) blocks of 128 threads, its work counter
+zeroed before every launch.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_DIR = os.path.join(HERE, "_ref")
+CUBIN = os.path.join(REF_DIR, "stride_dup_decode.cubin")
+ENTRY = os.path.join(REF_DIR, "stride_dup_decode.entry")
+REF_SRC = "/root/reference/bench_cpp/stride_dup_decode_bench.cu"
+
+
+def build(force: bool = False) -> bool:
+    """Compile the reference kernel to a sm_103a cubin when the reference
+    tree is present (the build machine only); True when a cubin exists."""
+    if os.path.exists(REF_SRC) and (force or not os.path.exists(CUBIN) or not os.path.exists(ENTRY)
+                                    or os.path.getmtime(CUBIN) < os.path.getmtime(REF_SRC)):
+        os.makedirs(REF_DIR, exist_ok=True)
+        r = subprocess.run(["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
+                            "-std=c++17", "-Xptxas", "-v", REF_SRC, "-o", CUBIN + ".tmp"],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference kernel build failed:\n{r.stderr}")
+        m = re.search(r"Compiling entry function '([^']*stride_dup_decode_kernel[^']*)'", r.stdout + r.stderr)
+        if not m:
+            raise RuntimeError("reference kernel entry name not found in the ptxas report")
+        os.replace(CUBIN + ".tmp", CUBIN)
+        with open(ENTRY, "w") as f:
+            f.write(m.group(1) + "\n")
+    return os.path.exists(CUBIN) and os.path.exists(ENTRY)
+
+
+def available() -> bool:
+    return os.path.exists(CUBIN) and os.path.exists(ENTRY)
+
+
+_cuda = None
+
+
+def _driver():
+    global _cuda
+    if _cuda is None:
+        lib = ctypes.CDLL("libcuda.so.1")
+        vp, u = ctypes.c_void_p, ctypes.c_uint
+        lib.cuModuleLoadData.argtypes = [ctypes.POINTER(vp), vp]
+        lib.cuModuleGetFunction.argtypes = [ctypes.POINTER(vp), vp, ctypes.c_char_p]
+        lib.cuModuleUnload.argtypes = [vp]
+        lib.cuLaunchKernel.argtypes = [vp, u, u, u, u, u, u, u, vp, vp, vp]
+        _cuda = lib
+    return _cuda
+
+
+def _ck(rc: int, what: str):
+    if rc != 0:
+        raise RuntimeError(f"{what}: CUDA driver error {rc}")
+
+
+class RefKernel:
+    """The reference kernel prepared for one DPR4 stream on the current
+    torch device (torch owns the device memory and the stream)."""
+
+    WARPS_PER_BLOCK = 4  # stride_dup_decode_bench.cu:190
+
+    def __init__(self, data: bytes):
+        import torch
+
+        from . import oracle as orc
+        if not available():
+            raise RuntimeError("reference kernel not built (oracle/_ref)")
+        h = orc.parse_header(data)
+        st = orc.side_table(data)
+        M = h.n_meshlets
+        body_bit = (86 + 4 * M) * 8  # the offset table ends byte-aligned
+        dev = torch.device("cuda", torch.cuda.current_device())
+        body = np.frombuffer(data, np.uint8)[body_bit // 8:]
+        # the reference's buffered reader prefetches up to 32 bytes past a
+        # meshlet (stride_dup_decode_bench.cu:636-637): pad with zeros
+        buf = np.zeros(len(body) + 32, np.uint8)
+        buf[:len(body)] = body
+        v_off = np.concatenate([[0], np.cumsum(st["n_local"][:-1], dtype=np.int64)]).astype(np.uint32)
+        t_off = np.concatenate([[0], np.cumsum(st["n_tris"][:-1], dtype=np.int64)]).astype(np.uint32)
+
+        def dput(a):
+            return torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).copy()).to(dev)
+
+        self.d = {
+            "buf": dput(buf),
+            "off": dput((st["start_bit"] - body_bit).astype(np.uint64)),
+            "n_local": dput(st["n_local"]), "n_tris": dput(st["n_tris"]), "n_strips": dput(st["n_strips"]),
+            "v_off": dput(v_off), "t_off": dput(t_off),
+            "resid": dput((st["resid_bit"] - body_bit).astype(np.uint64)),
+            "n_kind0": dput(st["n_kind0"]), "axis": dput(st["sub_offs"]),
+            "counter": torch.zeros(4, dtype=torch.uint8, device=dev),
+        }
+        self.n_v, self.n_t, self.n_meshlets = int(st["n_local"].sum()), int(st["n_tris"].sum()), M
+        self.verts = torch.empty((self.n_v, 3), dtype=torch.float32, device=dev)
+        self.tris = torch.empty((self.n_t, 3), dtype=torch.int32, device=dev)
+        self.h = h
+        drv = _driver()
+        self._mod = ctypes.c_void_p()
+        self._fn = ctypes.c_void_p()
+        with open(CUBIN, "rb") as f:
+            image = f.read()
+        self._image = ctypes.create_string_buffer(image, len(image))
+        _ck(drv.cuModuleLoadData(ctypes.byref(self._mod), ctypes.cast(self._image, ctypes.c_void_p)),
+            "cuModuleLoadData")
+        name = open(ENTRY).read().strip().encode()
+        _ck(drv.cuModuleGetFunction(ctypes.byref(self._fn), self._mod, name), "cuModuleGetFunction")
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        self.grid = min(M, 16 * sms)
+        self._params = self._pack()
+
+    def _pack(self):
+        h = self.h
+        P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+        vals = [P(self.d["buf"]), P(self.d["off"]), P(self.d["n_local"]), P(self.d["n_tris"]),
+                P(self.d["n_strips"]), P(self.d["v_off"]), P(self.d["t_off"]), P(self.d["resid"]),
+                P(self.d["n_kind0"]), P(self.d["axis"]), ctypes.c_int(self.n_meshlets)]
+        vals += [ctypes.c_float(float(x)) for x in h.g_min]
+        vals += [ctypes.c_float(float(x)) for x in h.g_range]
+        vals += [ctypes.c_int(int(x)) for x in h.g_bits]
+        vals += [ctypes.c_float(float(x)) for x in h.center] + [ctypes.c_float(float(h.scale))]
+        for d in range(3):
+            vals += [ctypes.c_int(int(h.pred_n[d, 0])), ctypes.c_int(int(h.pred_n[d, 1])),
+                     ctypes.c_int(int(h.pred_n[d, 2])), ctypes.c_int(int(h.pred_k[d]))]
+        vals += [P(self.verts), P(self.tris), P(self.d["counter"])]
+        self._vals = vals
+        arr = (ctypes.c_void_p * len(vals))(*[ctypes.cast(ctypes.pointer(v), ctypes.c_void_p) for v in vals])
+        return arr
+
+    def launch(self, stream) -> None:
+        """One decode on `stream` (a torch.cuda.Stream), as the reference
+        harness's launch(): zero the work counter, launch."""
+        self.d["counter"].zero_()
+        _ck(_driver().cuLaunchKernel(self._fn, self.grid, 1, 1, 32 * self.WARPS_PER_BLOCK, 1, 1, 0,
+                                     ctypes.c_void_p(int(stream.cuda_stream)),
+                                     ctypes.cast(self._params, ctypes.c_void_p), None),
+            "cuLaunchKernel")
+
+    def close(self):
+        if self._mod:
+            _driver().cuModuleUnload(self._mod)
+            self._mod = ctypes.c_void_p()

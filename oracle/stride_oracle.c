@@ -281,11 +281,14 @@ static double dequant(const so_header* h, int d, int64_t code) {
 /* Decode the meshlet whose header starts at r->pos.  Writes n_local positions
  * (and codes, if requested) at v_base and the emitted triangles at t_base.
  * Returns counts through n_local_out / n_tris_out. */
+/* side (optional, 7 entries): the absolute bit of the anchor (start of the
+ * residual part), the absolute starts of dy, dz, px, py, pz, and n_kind0.
+ * pos == NULL decodes without writing outputs. */
 static int decode_meshlet(so_br* r, const so_header* h, so_scratch* s,
                           uint64_t v_base, uint64_t t_base,
                           float* pos, int64_t* idx, int64_t* codes_out,
                           uint64_t cap_v, uint64_t cap_t,
-                          uint32_t* n_local_out, uint64_t* n_tris_out) {
+                          uint32_t* n_local_out, uint64_t* n_tris_out, uint64_t* side) {
     uint32_t n_local = (uint32_t)br_read(r, 16);
     (void)br_read(r, 16); /* n_tris: not used by the reference decoder */
     uint32_t n_strips = (uint32_t)br_read(r, 16);
@@ -346,6 +349,7 @@ static int decode_meshlet(so_br* r, const so_header* h, so_scratch* s,
             p0 = a; p1 = b; p2 = nv;
         }
     }
+    if (side) side[0] = r->pos;
     /* anchor + (tag, k) headers */
     int64_t anchor[3];
     for (int d = 0; d < 3; d++) {
@@ -362,7 +366,9 @@ static int decode_meshlet(so_br* r, const so_header* h, so_scratch* s,
     /* residual substreams: dx, dy, dz, px, py, pz; stored per walk kind slot */
     int64_t* dres = s->resid;               /* n_delta x 3 */
     int64_t* pres = s->resid + 3 * n_delta; /* n_kind1 x 3 */
+    if (side) side[6] = n_kind0;
     for (int sub = 0; sub < 6; sub++) {
+        if (side && sub) side[sub] = r->pos;
         int d = sub % 3;
         uint64_t n = sub < 3 ? n_delta : n_kind1;
         int64_t* dst = sub < 3 ? dres : pres;
@@ -409,6 +415,11 @@ static int decode_meshlet(so_br* r, const so_header* h, so_scratch* s,
         }
         prev[0] = cv[0]; prev[1] = cv[1]; prev[2] = cv[2];
     }
+    if (!pos) {
+        *n_local_out = n_local;
+        *n_tris_out = n_tris;
+        return SO_OK;
+    }
     if (v_base + n_local > cap_v || t_base + n_tris > cap_t) return SO_ERR_CAPACITY;
     for (uint32_t v = 0; v < n_local; v++) {
         for (int d = 0; d < 3; d++) {
@@ -439,7 +450,7 @@ int so_decode(const uint8_t* data, uint64_t len, float* pos, int64_t* idx,
     for (uint32_t m = 0; m < h.n_meshlets && !rc; m++) {
         uint32_t nl;
         uint64_t nt;
-        rc = decode_meshlet(&r, &h, &s, v_base, t_base, pos, idx, codes, cap_v, cap_t, &nl, &nt);
+        rc = decode_meshlet(&r, &h, &s, v_base, t_base, pos, idx, codes, cap_v, cap_t, &nl, &nt, NULL);
         v_base += nl;
         t_base += nt;
     }
@@ -481,7 +492,7 @@ static void* so_worker(void* arg) {
         uint32_t nl;
         uint64_t nt;
         j->rc = decode_meshlet(&r, j->h, &s, j->vb[m], j->tb[m], j->pos, j->idx, NULL,
-                               j->cap_v, j->cap_t, &nl, &nt);
+                               j->cap_v, j->cap_t, &nl, &nt, NULL);
         if (!j->rc && (j->vb[m] + nl != j->vb[m + 1] || j->tb[m] + nt != j->tb[m + 1]))
             j->rc = SO_ERR_LAYOUT;
         if (!j->rc && r.pos != j->off[m + 1]) {
@@ -538,6 +549,44 @@ int so_decode_mt(const uint8_t* data, uint64_t len, float* pos, int64_t* idx,
     *n_v_out = vb[M];
     *n_t_out = tb[M];
     free(off); free(vb); free(tb);
+    return rc;
+}
+
+/* Side table of the reference GPU bench's blob (DPRB v4, written by
+ * scripts/dump_stride_dup_blob.py:104-160 from encoder metadata and read by
+ * bench_cpp/stride_dup_decode_bench.cu:527-596), derived here from the DPR4
+ * bytes alone: per meshlet its start bit, header counts, the bit where its
+ * anchor (residual part) starts, n_kind0, and the starts of dy, dz, px, py,
+ * pz relative to the anchor (paradelta_v5_dup.py:290-313).  All bit
+ * positions are absolute in `data`. */
+int so_side_table(const uint8_t* data, uint64_t len, uint64_t* start_bit, uint32_t* n_local,
+                  uint32_t* n_tris, uint32_t* n_strips, uint64_t* resid_bit, uint32_t* n_kind0,
+                  uint16_t* sub_offs) {
+    so_header h;
+    int rc = so_parse_header(data, len, &h);
+    if (rc) return rc;
+    so_scratch s;
+    if ((rc = scratch_init(&s))) { scratch_free(&s); return rc; }
+    so_br r = {data, len * 8ull, h.body_bit, 0};
+    for (uint32_t m = 0; m < h.n_meshlets && !rc; m++) {
+        uint64_t side[7] = {0, 0, 0, 0, 0, 0, 0};
+        start_bit[m] = r.pos;
+        so_br hr = r;
+        n_local[m] = (uint32_t)br_read(&hr, 16);
+        n_tris[m] = (uint32_t)br_read(&hr, 16);
+        n_strips[m] = (uint32_t)br_read(&hr, 16);
+        uint32_t nl;
+        uint64_t nt;
+        rc = decode_meshlet(&r, &h, &s, 0, 0, NULL, NULL, NULL, 0, 0, &nl, &nt, side);
+        resid_bit[m] = side[0];
+        n_kind0[m] = (uint32_t)side[6];
+        for (int k = 0; k < 5 && !rc; k++) {
+            const uint64_t d = side[1 + k] - side[0];
+            if (d > 0xFFFFu) rc = SO_ERR_UNSUPPORTED; /* the blob stores them as u16 */
+            sub_offs[5ull * m + k] = (uint16_t)d;
+        }
+    }
+    scratch_free(&s);
     return rc;
 }
 

@@ -44,3 +44,20 @@ def test_oracle_errors():
         oracle.decode(bytes(v))
     with pytest.raises(oracle.OracleError):
         oracle.decode(bytes(data[: len(data) // 2]))
+
+
+@pytest.mark.parametrize("name", ["grid129_b12", "ico3_b12", "torus_b10"])
+def test_side_table_layout(name):
+    """The reference GPU harness's side table, derived from the bytes: every
+    substream starts after the anchor and the six (tag, k) bytes, in the
+    order dy dz px py pz, and the residual part ends before the next meshlet."""
+    g = _golden.load(name)
+    st = oracle.side_table(g["data"])
+    h = oracle.parse_header(g["data"])
+    assert st["n_local"].sum() == h.n_v_total and st["n_tris"].sum() == h.n_t
+    assert (st["resid_bit"] >= st["start_bit"] + 48).all()
+    sub = st["sub_offs"].astype(np.int64)
+    assert (sub[:, 0] >= int(h.g_bits.sum()) + 96).all()
+    assert (np.diff(sub, axis=1) >= 0).all()
+    assert (st["start_bit"][1:].astype(np.int64) >= st["resid_bit"][:-1].astype(np.int64) + sub[:-1, 4]).all()
+    assert ((st["n_kind0"] >= 1) & (st["n_kind0"] <= st["n_local"])).all()
