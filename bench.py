@@ -58,7 +58,9 @@ def parse_args(argv=None):
     ap.add_argument("--grid", type=int, default=2049)
     ap.add_argument("--tune", type=int, default=1, help="autotune the launch shape before timing")
     ap.add_argument("--batch-meshes", type=int, default=4096)
-    ap.add_argument("--rates", default="50,200,1000,2000", help="serve: Poisson arrival rates (requests/s)")
+    ap.add_argument("--rates", default="50,100,200,500,1000,2000", help="serve: Poisson arrival rates (requests/s)")
+    ap.add_argument("--serve-host-rate", type=float, default=500.0,
+                    help="serve: one more pass at this rate with every response copied to host memory (0 = none)")
     ap.add_argument("--serve-seconds", type=float, default=3.0, help="serve: arrivals per rate span this long")
     ap.add_argument("--serve-pool", type=int, default=48, help="serve: distinct encoded blobs drawn from")
     ap.add_argument("--serve-budget-gb", type=int, default=40)
@@ -669,11 +671,15 @@ def run_serve(args):
         for rid in [warm.submit(x) for x in blobs[:4]]:
             assert warm.wait(rid).ok
             warm.release(rid)
-    for rate in rates:
+    runs = [(r, False) for r in rates] + ([(args.serve_host_rate, True)] if args.serve_host_rate > 0 else [])
+    alone_host = None
+    for rate, to_host in runs:
         n_req = max(20, int(rate * args.serve_seconds))
         gaps = rng.exponential(1.0 / rate, n_req)
         picks = rng.integers(0, len(blobs), n_req)
-        srv = DecodeServer(args.serve_budget_gb << 30, n_streams=3, max_batch=256)
+        if to_host and alone_host is None:
+            alone_host = [(t.cpu().numpy(), v.cpu().numpy()) for t, v in alone]
+        srv = DecodeServer(args.serve_budget_gb << 30, n_streams=3, max_batch=256, copy_to_host=to_host)
         ids = [None] * n_req
         lat, ok, failed = [], [0, 0], {}
         first_submit = [None]
@@ -698,6 +704,11 @@ def run_serve(args):
             r = srv.wait(ids[i])
             if not r.ok:
                 failed[r.status] = failed.get(r.status, 0) + 1
+            elif to_host:
+                at, av = alone_host[picks[i]]
+                good = np.array_equal(r.host_tris.view(np.int32), at) and \
+                    np.array_equal(r.host_verts.view(np.int32), av)
+                ok[0 if good else 1] += 1
             else:
                 good = torch.equal(r.tris.view(torch.int32), alone[picks[i]][0]) and \
                     torch.equal(r.verts.view(torch.int32), alone[picks[i]][1])
@@ -719,14 +730,15 @@ def run_serve(args):
                 "unit": "M tris/s", "n_gpus": world, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "int32+f32 (exact f64 expression)",
                 "data": "synthetic (seeded mixed meshes)",
-                "config": {"workload": f"serve_poisson_{int(rate)}rps", "rate_rps": rate, "requests": n_req,
+                "config": {"workload": f"serve_poisson_{int(rate)}rps" + ("_to_host" if to_host else ""),
+                           "rate_rps": rate, "requests": n_req,
                            "pool": len(blobs), "pool_triangles": int(sum(tris)),
                            "sizes": "log-uniform [5K, 2M] triangles from the many-mesh generator (seed 5)",
                            "hbm_budget_gb": args.serve_budget_gb, "streams": 3, "max_batch": 256},
                 "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3),
                                "p99": round(float(np.percentile(lat, 99)), 3),
                                "max": round(float(np.max(lat)), 3),
-                               "to": "outputs resident on the device"},
+                               "to": "outputs in pinned host memory" if to_host else "outputs resident on the device"},
                 "achieved_rps": round(n_req / span_s, 1), "launches": st["launches"],
                 "mean_requests_per_launch": round(n_req / max(1, st["launches"]), 2),
                 "arena_peak_gb": round(st["arena_peak_bytes"] / 2 ** 30, 3),
