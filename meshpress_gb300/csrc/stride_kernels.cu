@@ -971,14 +971,50 @@ __device__ __forceinline__ bool residual(const uint32_t* w, uint32_t rbase, uint
     return ok;
 }
 
+// Codeword skipping by table.  Entry [eg][k][b] describes the whole
+// Rice(k) (eg = 0) or Exp-Golomb(k) (eg = 1) codewords at the start of the 8
+// bits b (MSB first): their count | their total length << 4.  A compile-time
+// constant in device memory, never written, so it is read through L1.
+struct SkipTable {
+    uint8_t e[2][8][256];
+};
+
+constexpr SkipTable make_skip_table() {
+    SkipTable t{};
+    for (int eg = 0; eg < 2; eg++)
+        for (int k = 0; k < 8; k++)
+            for (int b = 0; b < 256; b++) {
+                int at = 0, cnt = 0;
+                for (;;) {
+                    int z = 0;
+                    while (at + z < 8 && ((b >> (7 - at - z)) & 1) == 0) z++;
+                    if (at + z >= 8) break;  // no terminating one inside the byte
+                    const int len = z + 1 + (eg ? z : 0) + k;
+                    if (at + len > 8) break;
+                    at += len;
+                    cnt++;
+                }
+                t.e[eg][k][b] = static_cast<uint8_t>(cnt | (at << 4));
+            }
+    return t;
+}
+
+__device__ const SkipTable g_skip_table = make_skip_table();
+
 // Skip n codewords (substream boundaries are not stored in the stream).
-// Up to four codewords that lie wholly inside the 32-bit window are taken
-// per step; a codeword longer than the window goes to the general reader.
+// In a long substream (32 codewords or more, k < 8), while at least eight
+// remain, one table read takes every whole codeword of the next 8 bits (a
+// bit scan per codeword measured about 80 cycles each on one warp; the
+// table's first reads miss L1, which short substreams would not repay);
+// otherwise up to four codewords that lie wholly inside the 32-bit window
+// are taken per step; a codeword longer than the window goes to the general
+// reader.
 template <bool kShared>
 __device__ __forceinline__ bool skip_codes(const uint32_t* w, uint32_t rbase, uint32_t& pos, uint32_t tk,
                                            uint32_t n, uint32_t limit) {
     const uint32_t k = tk & 0x3Fu;
     const bool eg = (tk & 0x80u) != 0u;
+    const uint8_t* tab = (k < 8u && n >= 32u) ? g_skip_table.e[eg ? 1 : 0][k] : nullptr;
     bool ok = true;
     BitWin<kShared> b;
     b.w = w;
@@ -987,14 +1023,20 @@ __device__ __forceinline__ bool skip_codes(const uint32_t* w, uint32_t rbase, ui
     while (n > 0u) {
         const uint32_t x = b.peek();
         uint32_t used = 0u, cnt = 0u;
+        const uint32_t e = (tab && n >= 8u) ? __ldg(tab + (x >> 24)) : 0u;
+        if (e & 15u) {
+            cnt = e & 15u;
+            used = e >> 4;
+        } else {
 #pragma unroll
-        for (int s = 0; s < 4; s++) {
-            const uint32_t xx = __funnelshift_lc(0u, x, used);  // the window past the codewords taken
-            const uint32_t z = __clz(xx);                       // 32 when nothing is left
-            const uint32_t len = z + 1u + (eg ? z : 0u) + k;
-            const bool fits = (used + len <= 32u) & (cnt < n);
-            used += fits ? len : 0u;
-            cnt += fits ? 1u : 0u;
+            for (int s = 0; s < 4; s++) {
+                const uint32_t xx = __funnelshift_lc(0u, x, used);  // the window past the codewords taken
+                const uint32_t z = __clz(xx);                       // 32 when nothing is left
+                const uint32_t len = z + 1u + (eg ? z : 0u) + k;
+                const bool fits = (used + len <= 32u) & (cnt < n);
+                used += fits ? len : 0u;
+                cnt += fits ? 1u : 0u;
+            }
         }
         if (cnt) {
             b.advance(used);
