@@ -134,6 +134,40 @@ int stride_decode_host(stride_handle* h, void* stream, uint32_t* h_idx, float* h
  * *bad_meshlet (optional) receives the first failing meshlet. */
 int stride_status(stride_handle* h, int wait, uint32_t* bad_meshlet);
 
+/* The side table of the last decode, derived on the device: per meshlet the
+ * stream bit where its anchor (residual part) starts (d_resid_bit, n_meshlets
+ * uint64) and the starts of the dy, dz, px, py, pz substreams relative to it
+ * (d_sub_offs, 5 x n_meshlets uint16, 0xFFFF when farther than 65,534 bits).
+ * The reference GPU harness reads the same table from files its encoder
+ * writes (scripts/dump_stride_dup_blob.py:120-160; there the anchor bit is
+ * relative to the first meshlet).  Waits for the last decode; fails with its
+ * status if that decode failed. */
+int stride_side_table(stride_handle* h, void* stream, uint64_t* d_resid_bit, uint16_t* d_sub_offs);
+
+/* ---- meshlet-native outputs (the consumer step after decode) ------------
+ * No counterpart in the reference's decoder.  For a consumer that works per
+ * meshlet (a renderer's meshlet pipeline): where each meshlet's rows lie in
+ * the outputs, its bounds, and frustum culling of those bounds.  The first
+ * two wait for the handle's last decode and fail with its status. */
+
+/* Exclusive prefix sums, n_meshlets + 1 entries each (the last holds the
+ * totals): meshlet m owns vertex rows [d_v_first[m], d_v_first[m+1]) and
+ * triangle rows [d_t_first[m], d_t_first[m+1]) of the decode's outputs. */
+int stride_meshlet_ranges(stride_handle* h, void* stream, uint64_t* d_v_first, uint64_t* d_t_first);
+
+/* Axis-aligned bounds of each meshlet's rows of d_pos (the last decode's
+ * positions): 6 floats per meshlet, min x y z then max x y z. */
+int stride_meshlet_bounds(stride_handle* h, void* stream, const float* d_pos, float* d_bounds);
+
+/* Frustum culling of n meshlet bounds (6 floats each, device) against six
+ * planes (host, 24 floats: a b c d per plane, inside where
+ * a x + b y + c z + d >= 0).  A meshlet is culled when its box lies wholly
+ * outside one plane (or is empty).  Writes one visibility bit per meshlet
+ * (d_visible, ceil(n / 32) uint32 words, bit m % 32 of word m / 32) and the
+ * number of visible meshlets (*d_count, device).  Asynchronous. */
+int stride_cull_meshlets(const float* d_bounds, uint32_t n, const float* planes, void* stream, uint32_t* d_visible,
+                         uint32_t* d_count);
+
 /* Measurement entry point (no reference counterpart): one decode like
  * stride_decode, with CUDA events recorded on `stream` between its three
  * kernels; waits and writes their durations in milliseconds to

@@ -4,5 +4,5 @@
 name (utils/paradelta_v5_cuda.py:580-718); ``BatchDecoder`` decodes many
 streams in one launch; ``StrideServer`` is the continuous-batching service.
 """
-from .decoder import ParaDeltaV5GpuDecoder, decode_to_device  # noqa: F401
+from .decoder import ParaDeltaV5GpuDecoder, cull_meshlets, decode_to_device  # noqa: F401
 from ._lib import StrideDeviceError, StrideFormatError  # noqa: F401

@@ -90,6 +90,10 @@ SIGNATURES = [
     ("stride_decode_host", _I, [_P, _P, _P, _P]),
     ("stride_status", _I, [_P, _I, ctypes.POINTER(_U32)]),
     ("stride_decode_timed", _I, [_P, _P, _P, _P, _P]),
+    ("stride_side_table", _I, [_P, _P, _P, _P]),
+    ("stride_meshlet_ranges", _I, [_P, _P, _P, _P]),
+    ("stride_meshlet_bounds", _I, [_P, _P, _P, _P]),
+    ("stride_cull_meshlets", _I, [_P, ctypes.c_uint32, _P, _P, _P, _P]),
     ("stride_set_config", _I, [_P, ctypes.POINTER(LaunchCfg)]),
     ("stride_close", None, [_P]),
     ("stride_decode_static", _I, [_P, _SZ, _P, _P, _P]),

@@ -473,6 +473,62 @@ int stride_status(stride_handle* h, int wait, uint32_t* bad_meshlet) {
     return STRIDE_OK;
 }
 
+int stride_side_table(stride_handle* h, void* stream, uint64_t* d_resid_bit, uint16_t* d_sub_offs) {
+    if (!h) return fail(STRIDE_ERR_ARG, "null handle");
+    const uint32_t n = h->params.n_meshlets;
+    if (n && (!d_resid_bit || !d_sub_offs)) return fail(STRIDE_ERR_ARG, "null output pointer");
+    if (!h->launched) return fail(STRIDE_ERR_ARG, "no decode yet");
+    const int rc = stride_status(h, 1, nullptr);
+    if (rc) return rc;
+    const int r2 = enqueue_side_table(h->d_descs, n, reinterpret_cast<unsigned long long*>(d_resid_bit), d_sub_offs,
+                                      stream);
+    return r2 ? fail(r2, "side table launch failed") : STRIDE_OK;
+}
+
+int stride_meshlet_ranges(stride_handle* h, void* stream, uint64_t* d_v_first, uint64_t* d_t_first) {
+    if (!h || !d_v_first || !d_t_first) return fail(STRIDE_ERR_ARG, "null argument");
+    if (!h->launched) return fail(STRIDE_ERR_ARG, "no decode yet");
+    const int rc = stride_status(h, 1, nullptr);
+    if (rc) return rc;
+    const uint32_t n = h->params.n_meshlets;
+    if (n == 0u) {
+        const uint64_t z[1] = {0};
+        cudaStream_t s = static_cast<cudaStream_t>(stream);
+        if (cudaMemcpyAsync(d_v_first, z, 8, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaMemcpyAsync(d_t_first, z, 8, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+            return cuda_fail(cudaGetLastError(), "meshlet ranges");
+        return STRIDE_OK;
+    }
+    const int r2 = enqueue_meshlet_ranges(h->d_descs, h->d_blk_prefix, n,
+                                          reinterpret_cast<unsigned long long*>(d_v_first),
+                                          reinterpret_cast<unsigned long long*>(d_t_first), stream);
+    return r2 ? fail(r2, "meshlet ranges launch failed") : STRIDE_OK;
+}
+
+int stride_meshlet_bounds(stride_handle* h, void* stream, const float* d_pos, float* d_bounds) {
+    if (!h || (!d_pos && h->params.n_v) || (!d_bounds && h->params.n_meshlets)) return fail(STRIDE_ERR_ARG, "null argument");
+    if ((reinterpret_cast<uintptr_t>(d_pos) & 3u) || (reinterpret_cast<uintptr_t>(d_bounds) & 3u))
+        return fail(STRIDE_ERR_ARG, "positions and bounds must be 4-byte aligned");
+    if (!h->launched) return fail(STRIDE_ERR_ARG, "no decode yet");
+    const int rc = stride_status(h, 1, nullptr);
+    if (rc) return rc;
+    const int r2 = enqueue_meshlet_bounds(h->d_descs, h->d_blk_prefix, h->params.n_meshlets, d_pos, d_bounds, stream);
+    return r2 ? fail(r2, "meshlet bounds launch failed") : STRIDE_OK;
+}
+
+int stride_cull_meshlets(const float* d_bounds, uint32_t n, const float* planes, void* stream, uint32_t* d_visible,
+                         uint32_t* d_count) {
+    if (!planes || !d_count || (n && (!d_bounds || !d_visible))) return fail(STRIDE_ERR_ARG, "null argument");
+    if ((reinterpret_cast<uintptr_t>(d_bounds) & 3u) || (reinterpret_cast<uintptr_t>(d_visible) & 3u) ||
+        (reinterpret_cast<uintptr_t>(d_count) & 3u))
+        return fail(STRIDE_ERR_ARG, "bounds, visibility and count must be 4-byte aligned");
+    Planes pl;
+    for (int i = 0; i < 24; i++) pl.p[i] = planes[i];
+    const int r2 = enqueue_cull(d_bounds, n, pl, d_visible, d_count, stream);
+    return r2 ? fail(r2, "cull launch failed") : STRIDE_OK;
+}
+
 int stride_decode_host(stride_handle* h, void* stream, uint32_t* h_idx, float* h_pos) {
     if (!h || (!h_idx && h->params.n_t) || (!h_pos && h->params.n_v)) return fail(STRIDE_ERR_ARG, "null argument");
     cudaError_t e;

@@ -85,8 +85,11 @@ struct __align__(16) MeshletDesc {
     uint32_t anchor_bit;   // end of connectivity = anchor codes
     uint32_t walk;         // n_kind0 | n_walk << 16
     uint32_t slot_meshlet; // meshlet decoded at slot i (= this record's index)
-    uint32_t pad[5];
+    uint16_t sub_offs[5];  // vertex kernel: starts of dy dz px py pz after anchor_bit (0xFFFF: too far)
+    uint16_t pad16;
+    uint32_t pad[2];
 };
+static_assert(sizeof(MeshletDesc) == 64, "meshlet records are four 16-byte loads");
 
 struct BlockPrefix {
     unsigned long long v, t, wp, pad;
@@ -153,6 +156,26 @@ int parse_header(const uint8_t* data, size_t len, MeshParams* p, char* why, size
 // scan kernel, after it, after the connectivity kernel and after the vertex
 // kernel.
 int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void* const* ev = nullptr);
+
+// Meshlet-native outputs of a finished decode: each meshlet's first vertex
+// and triangle row (n + 1 entries, the last the totals); the bounds (min
+// xyz, max xyz) of its rows of `pos`; frustum culling of such bounds into a
+// visibility bit per meshlet and a visible count.
+struct Planes {
+    float p[24];  // six planes (a, b, c, d): inside where a x + b y + c z + d >= 0
+};
+int enqueue_meshlet_ranges(const MeshletDesc* descs, const BlockPrefix* bp, uint32_t n, unsigned long long* v_first,
+                           unsigned long long* t_first, void* stream);
+int enqueue_meshlet_bounds(const MeshletDesc* descs, const BlockPrefix* bp, uint32_t n, const float* pos,
+                           float* bounds, void* stream);
+int enqueue_cull(const float* bounds, uint32_t n, const Planes& planes, uint32_t* visible, uint32_t* count,
+                 void* stream);
+
+// Gathers the side table of a finished decode from its meshlet records:
+// per meshlet the stream bit of its anchor and the five substream starts
+// relative to it.
+int enqueue_side_table(const MeshletDesc* descs, uint32_t n, unsigned long long* resid_bit, uint16_t* sub_offs,
+                       void* stream);
 
 // STRIDE_OK when `cfg` is a launchable shape.
 int check_config(const LaunchCfg& cfg, bool wide);

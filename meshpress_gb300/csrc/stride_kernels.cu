@@ -1266,6 +1266,13 @@ __device__ __forceinline__ void vert_round(const DecodeArgs& a, const GroupLane&
             if (ok) ok = skip_codes<kShared>(w, rbase, pos, e == 0u ? tk[3] : tk[4], n_para, end);
         S.cp = pos;
         S.bad = !ok;
+        if (ok) {  // the side table: this axis' substream starts after the anchor
+            const uint32_t base = L.d.anchor_bit;
+            uint16_t* so = a.descs[L.m].sub_offs;
+            const uint32_t rp = min(S.cp - base, 0xFFFFu), rd = min(S.cdd - base, 0xFFFFu);
+            if (d != 0u) so[d - 1u] = static_cast<uint16_t>(rd);  // dy, dz (dx follows the tags)
+            so[2u + d] = static_cast<uint16_t>(rp);                // px, py, pz
+        }
     }
     PlaneT<kWide>* plane = reinterpret_cast<PlaneT<kWide>*>(planes + code_off);
     if (act && !S.bad) vert_axis<kShared, kWide>(a, L, d, w, rbase, plane, S);
@@ -1512,6 +1519,15 @@ int device_sm_count() {
     return cached[dev];
 }
 
+__global__ void side_table_kernel(const MeshletDesc* __restrict__ descs, uint32_t n,
+                                  unsigned long long* __restrict__ resid_bit, uint16_t* __restrict__ sub_offs) {
+    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    resid_bit[m] = __ldcg(&descs[m].anchor_bit);
+#pragma unroll
+    for (int k = 0; k < 5; k++) sub_offs[5ull * m + k] = __ldcg(&descs[m].sub_offs[k]);
+}
+
 int check_config(const LaunchCfg& cfg, bool wide) {
     if (cfg.warps_per_cta != 1 && cfg.warps_per_cta != 2 && cfg.warps_per_cta != 4) return STRIDE_ERR_ARG;
     // one meshlet of kMaxLocal vertices, its plane padded to an odd word count
@@ -1549,6 +1565,127 @@ int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void
     }
     record(ev, 3, s);
     return STRIDE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Meshlet-native outputs: ranges, bounds, frustum culling
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void meshlet_rows(const MeshletDesc* descs, const BlockPrefix* bp, uint32_t m,
+                                             unsigned long long& v0, unsigned long long& t0, uint32_t& nv,
+                                             uint32_t& nt) {
+    const BlockPrefix& p = bp[m / kScanThreads];
+    const uint32_t c = __ldcg(&descs[m].counts0);
+    v0 = __ldcg(&p.v) + __ldcg(&descs[m].v_pref);
+    t0 = __ldcg(&p.t) + __ldcg(&descs[m].t_pref);
+    nv = c & 0xFFFFu;
+    nt = c >> 16;
+}
+
+__global__ void meshlet_ranges_kernel(const MeshletDesc* __restrict__ descs, const BlockPrefix* __restrict__ bp,
+                                      uint32_t n, unsigned long long* __restrict__ v_first,
+                                      unsigned long long* __restrict__ t_first) {
+    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= n) return;
+    unsigned long long v0, t0;
+    uint32_t nv, nt;
+    meshlet_rows(descs, bp, m, v0, t0, nv, nt);
+    v_first[m] = v0;
+    t_first[m] = t0;
+    if (m + 1u == n) {
+        v_first[n] = v0 + nv;
+        t_first[n] = t0 + nt;
+    }
+}
+
+// One warp per meshlet: min / max of each coordinate over its rows of pos.
+__global__ void meshlet_bounds_kernel(const MeshletDesc* __restrict__ descs, const BlockPrefix* __restrict__ bp,
+                                      uint32_t n, const float* __restrict__ pos, float* __restrict__ bounds) {
+    const uint32_t m = blockIdx.x * (blockDim.x / 32u) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (m >= n) return;  // warp-uniform
+    unsigned long long v0, t0;
+    uint32_t nv, nt;
+    meshlet_rows(descs, bp, m, v0, t0, nv, nt);
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    const float* base = pos + 3ull * v0;
+    for (uint32_t i = lane; i < 3u * nv; i += 32u) {  // the meshlet's floats, coalesced
+        const float x = __ldcg(base + i);
+        const uint32_t d = i % 3u;  // base is a row start
+        lo[0] = d == 0u ? fminf(lo[0], x) : lo[0];
+        lo[1] = d == 1u ? fminf(lo[1], x) : lo[1];
+        lo[2] = d == 2u ? fminf(lo[2], x) : lo[2];
+        hi[0] = d == 0u ? fmaxf(hi[0], x) : hi[0];
+        hi[1] = d == 1u ? fmaxf(hi[1], x) : hi[1];
+        hi[2] = d == 2u ? fmaxf(hi[2], x) : hi[2];
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            lo[d] = fminf(lo[d], __shfl_xor_sync(kFull, lo[d], o));
+            hi[d] = fmaxf(hi[d], __shfl_xor_sync(kFull, hi[d], o));
+        }
+    }
+    if (lane < 6) bounds[6ull * m + lane] = lane < 3 ? lo[lane] : hi[lane - 3];
+}
+
+// A box is culled when it lies wholly on the outer side of one plane: its
+// corner furthest along the plane normal (the p-vertex) has
+// a x + b y + c z + d < 0.  Evaluated left to right without contraction.
+// An empty meshlet's box (min > max) is culled.
+__global__ void cull_kernel(const float* __restrict__ bounds, uint32_t n, Planes pl, uint32_t* __restrict__ visible,
+                            uint32_t* __restrict__ count) {
+    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+    bool vis = false;
+    if (m < n) {
+        const float* b = bounds + 6ull * m;
+        const float x0 = b[0], y0 = b[1], z0 = b[2], x1 = b[3], y1 = b[4], z1 = b[5];
+        vis = x0 <= x1 && y0 <= y1 && z0 <= z1;
+#pragma unroll
+        for (int k = 0; k < 6; k++) {
+            const float a = pl.p[4 * k], bb = pl.p[4 * k + 1], c = pl.p[4 * k + 2], d = pl.p[4 * k + 3];
+            const float px = a >= 0.f ? x1 : x0, py = bb >= 0.f ? y1 : y0, pz = c >= 0.f ? z1 : z0;
+            const float s = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(a, px), __fmul_rn(bb, py)), __fmul_rn(c, pz)), d);
+            vis = vis && !(s < 0.f);
+        }
+    }
+    const uint32_t word = __ballot_sync(kFull, vis);
+    if ((threadIdx.x & 31) == 0 && m < n) {  // lane 0 holds the warp's first meshlet: word m / 32 exists
+        visible[m / 32u] = word;
+        if (word) atomicAdd(count, static_cast<uint32_t>(__popc(word)));
+    }
+}
+
+int enqueue_meshlet_ranges(const MeshletDesc* descs, const BlockPrefix* bp, uint32_t n, unsigned long long* v_first,
+                           unsigned long long* t_first, void* stream) {
+    if (n == 0u) return STRIDE_OK;
+    meshlet_ranges_kernel<<<(n + 255u) / 256u, 256, 0, static_cast<cudaStream_t>(stream)>>>(descs, bp, n, v_first,
+                                                                                              t_first);
+    return cudaGetLastError() == cudaSuccess ? STRIDE_OK : STRIDE_ERR_CUDA;
+}
+
+int enqueue_meshlet_bounds(const MeshletDesc* descs, const BlockPrefix* bp, uint32_t n, const float* pos,
+                           float* bounds, void* stream) {
+    if (n == 0u) return STRIDE_OK;
+    meshlet_bounds_kernel<<<(n + 7u) / 8u, 256, 0, static_cast<cudaStream_t>(stream)>>>(descs, bp, n, pos, bounds);
+    return cudaGetLastError() == cudaSuccess ? STRIDE_OK : STRIDE_ERR_CUDA;
+}
+
+int enqueue_cull(const float* bounds, uint32_t n, const Planes& planes, uint32_t* visible, uint32_t* count,
+                 void* stream) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (cudaMemsetAsync(count, 0, sizeof(uint32_t), s) != cudaSuccess) return STRIDE_ERR_CUDA;
+    if (n == 0u) return STRIDE_OK;
+    cull_kernel<<<(n + 255u) / 256u, 256, 0, s>>>(bounds, n, planes, visible, count);
+    return cudaGetLastError() == cudaSuccess ? STRIDE_OK : STRIDE_ERR_CUDA;
+}
+
+int enqueue_side_table(const MeshletDesc* descs, uint32_t n, unsigned long long* resid_bit, uint16_t* sub_offs,
+                       void* stream) {
+    if (n == 0u) return STRIDE_OK;
+    side_table_kernel<<<(n + 255u) / 256u, 256, 0, static_cast<cudaStream_t>(stream)>>>(descs, n, resid_bit,
+                                                                                          sub_offs);
+    return cudaGetLastError() == cudaSuccess ? STRIDE_OK : STRIDE_ERR_CUDA;
 }
 
 }  // namespace stride

@@ -97,6 +97,47 @@ class ParaDeltaV5GpuDecoder:
         bad = ctypes.c_uint32()
         _lib.check(self._lib.stride_status(self._h, 1, ctypes.byref(bad)), "stride decode")
 
+    def meshlet_ranges(self, *, stream=None):
+        """Where each meshlet's rows lie in the last decode's outputs ->
+        (v_first, t_first) torch.int64 (n_meshlets + 1,) exclusive prefix
+        sums; meshlet m owns vertex rows v_first[m]:v_first[m+1]."""
+        torch = _torch()
+        dev = torch.device("cuda", torch.cuda.current_device())
+        v = torch.empty(self.n_meshlets + 1, dtype=torch.int64, device=dev)
+        t = torch.empty(self.n_meshlets + 1, dtype=torch.int64, device=dev)
+        _lib.check(self._lib.stride_meshlet_ranges(self._h, ctypes.c_void_p(_stream_handle(stream)),
+                                                   ctypes.c_void_p(v.data_ptr()), ctypes.c_void_p(t.data_ptr())),
+                   "stride_meshlet_ranges")
+        return v, t
+
+    def meshlet_bounds(self, verts, *, stream=None):
+        """Axis-aligned bounds of each meshlet's rows of ``verts`` (the last
+        decode's positions, CUDA float32 (n_v, 3)) -> torch.float32
+        (n_meshlets, 6): min x y z, max x y z."""
+        torch = _torch()
+        assert verts.is_cuda and verts.dtype == torch.float32 and verts.is_contiguous()
+        assert verts.numel() >= 3 * self.n_v_total
+        out = torch.empty((self.n_meshlets, 6), dtype=torch.float32, device=verts.device)
+        _lib.check(self._lib.stride_meshlet_bounds(self._h, ctypes.c_void_p(_stream_handle(stream)),
+                                                   ctypes.c_void_p(verts.data_ptr()), ctypes.c_void_p(out.data_ptr())),
+                   "stride_meshlet_bounds")
+        return out
+
+    def side_table(self, *, stream=None):
+        """The last decode's side table, derived on the device -> (resid_bit
+        torch.int64 (n_meshlets,): the stream bit of each meshlet's anchor,
+        sub_offs torch.int16 (n_meshlets, 5): dy dz px py pz starts after
+        it, as uint16 bit patterns).  The reference GPU harness reads this
+        table from encoder-written files instead."""
+        torch = _torch()
+        dev = torch.device("cuda", torch.cuda.current_device())
+        resid = torch.empty(self.n_meshlets, dtype=torch.int64, device=dev)
+        subs = torch.empty((self.n_meshlets, 5), dtype=torch.int16, device=dev)
+        _lib.check(self._lib.stride_side_table(self._h, ctypes.c_void_p(_stream_handle(stream)),
+                                               ctypes.c_void_p(resid.data_ptr()), ctypes.c_void_p(subs.data_ptr())),
+                   "stride_side_table")
+        return resid, subs
+
     def decode_to_device(self, *, stream=None, check: bool = True):
         """-> (triangles torch.uint32 (n_t, 3), positions torch.float32 (n_v, 3))
         in world space, resident on the GPU.  The tensors are reused by later
@@ -158,3 +199,22 @@ def decode_to_device(data: bytes):
     dec = ParaDeltaV5GpuDecoder(data)
     tris, verts = dec.decode_to_device()
     return tris.clone(), verts.clone()
+
+
+def cull_meshlets(bounds, planes, *, stream=None):
+    """Frustum culling of meshlet bounds (CUDA float32 (n, 6), as
+    meshlet_bounds returns) against six planes (24 numbers: a b c d per
+    plane, inside where a x + b y + c z + d >= 0) -> (visible bits
+    torch.int32 (ceil(n / 32),), visible count torch.int32 (1,)), on the
+    device.  A meshlet is culled when its box lies wholly outside a plane."""
+    torch = _torch()
+    assert bounds.is_cuda and bounds.dtype == torch.float32 and bounds.is_contiguous() and bounds.shape[-1] == 6
+    n = bounds.shape[0]
+    pl = np.ascontiguousarray(np.asarray(planes, np.float32).reshape(24))
+    vis = torch.empty(max(1, (n + 31) // 32), dtype=torch.int32, device=bounds.device)
+    cnt = torch.empty(1, dtype=torch.int32, device=bounds.device)
+    lib = _lib.load()
+    _lib.check(lib.stride_cull_meshlets(ctypes.c_void_p(bounds.data_ptr()), n, ctypes.c_void_p(pl.ctypes.data),
+                                        ctypes.c_void_p(_stream_handle(stream)), ctypes.c_void_p(vis.data_ptr()),
+                                        ctypes.c_void_p(cnt.data_ptr())), "stride_cull_meshlets")
+    return vis, cnt

@@ -255,3 +255,20 @@ def test_bit_flip_fuzz(torch_cuda):
         else:
             rejected += 1
     assert rejected > 0
+
+
+@pytest.mark.parametrize("name", ["grid129_b12", "ico3_b12", "torus_b10"])
+def test_device_side_table_matches_oracle(torch_cuda, name):
+    """The substream starts the vertex kernel finds on the device equal the
+    side table the oracle derives from the same bytes."""
+    torch = torch_cuda
+    from meshpress_gb300 import ParaDeltaV5GpuDecoder
+    g = _golden.load(name)
+    dec = ParaDeltaV5GpuDecoder(g["data"])
+    dec.decode_to_device()
+    resid, subs = dec.side_table()
+    torch.cuda.synchronize()
+    st = oracle.side_table(g["data"])
+    assert np.array_equal(resid.cpu().numpy().astype(np.uint64), st["resid_bit"])
+    assert np.array_equal(subs.cpu().numpy().view(np.uint16), st["sub_offs"])
+    dec.close()
