@@ -59,6 +59,41 @@ def available() -> bool:
     return os.path.exists(CUBIN) and os.path.exists(ENTRY)
 
 
+def dprb_blob(data: bytes) -> bytes:
+    """The DPR4 stream as the reference GPU harness's input file (DPRB v4:
+    a 112-byte little-endian header, the meshlet bits, then the per-meshlet
+    tables; layout of scripts/dump_stride_dup_blob.py:121-156, read by
+    bench_cpp/stride_dup_decode_bench.cu:527-596).  The side tables come
+    from the bytes (so_side_table) instead of encoder metadata, so the file
+    can be written for any stream."""
+    import struct
+
+    from . import oracle as orc
+    h = orc.parse_header(data)
+    st = orc.side_table(data)
+    M = h.n_meshlets
+    body_bit = (86 + 4 * M) * 8
+    body = data[body_bit // 8:]
+    n_local, n_tris = st["n_local"], st["n_tris"]
+    v_off = np.concatenate([[0], np.cumsum(n_local[:-1], dtype=np.int64)]).astype(np.uint32)
+    t_off = np.concatenate([[0], np.cumsum(n_tris[:-1], dtype=np.int64)]).astype(np.uint32)
+    head = struct.pack("<II", 0x42525044, 4)
+    head += struct.pack("<III", M, int(n_local.sum()), int(n_tris.sum()))
+    head += struct.pack("<I", len(body)) + struct.pack("<II", 0, 0)
+    head += struct.pack("<fff", *[float(x) for x in h.center]) + struct.pack("<f", h.scale)
+    head += struct.pack("<f", h.per_coord_err)
+    head += struct.pack("<fff", *[float(x) for x in h.g_min]) + struct.pack("<fff", *[float(x) for x in h.g_range])
+    head += struct.pack("<III", *[int(x) for x in h.g_bits])
+    head += struct.pack("<9h", *[int(x) for x in h.pred_n.reshape(9)]) + struct.pack("<3B", *[int(x) for x in h.pred_k])
+    head += b"\x00\x00\x00"
+    assert len(head) == 112
+    parts = [head, body, (st["start_bit"] - body_bit).astype("<u8").tobytes(), n_local.astype("<u4").tobytes(),
+             n_tris.astype("<u4").tobytes(), st["n_strips"].astype("<u4").tobytes(), v_off.astype("<u4").tobytes(),
+             t_off.astype("<u4").tobytes(), (st["resid_bit"] - body_bit).astype("<u8").tobytes(),
+             st["n_kind0"].astype("<u4").tobytes(), st["sub_offs"].astype("<u2").tobytes()]
+    return b"".join(parts)
+
+
 _cuda = None
 
 

@@ -61,3 +61,29 @@ def test_side_table_layout(name):
     assert (np.diff(sub, axis=1) >= 0).all()
     assert (st["start_bit"][1:].astype(np.int64) >= st["resid_bit"][:-1].astype(np.int64) + sub[:-1, 4]).all()
     assert ((st["n_kind0"] >= 1) & (st["n_kind0"] <= st["n_local"])).all()
+
+
+def test_dprb_blob_layout():
+    """The reference GPU harness's input file written from DPR4 bytes: header
+    fields, section sizes and tables where its loader reads them."""
+    import struct
+
+    from oracle import ref_gpu
+    g = _golden.load("grid129_b12")
+    blob = ref_gpu.dprb_blob(g["data"])
+    h = oracle.parse_header(g["data"])
+    st = oracle.side_table(g["data"])
+    M = h.n_meshlets
+    magic, ver, m, nv, nt, buf_size = struct.unpack_from("<IIIIII", blob, 0)
+    assert (magic, ver, m, nv, nt) == (0x42525044, 4, M, h.n_v_total, h.n_t)
+    assert buf_size == len(g["data"]) - (86 + 4 * M)
+    assert struct.unpack_from("<3I", blob, 76) == tuple(int(x) for x in h.g_bits)
+    assert len(blob) == 112 + buf_size + M * (8 + 4 * 5 + 8 + 4 + 10)
+    at = 112 + buf_size
+    off = np.frombuffer(blob, "<u8", M, at)
+    assert np.array_equal(off + (86 + 4 * M) * 8, st["start_bit"])
+    at += 8 * M + 4 * 5 * M
+    resid = np.frombuffer(blob, "<u8", M, at)
+    assert np.array_equal(resid + (86 + 4 * M) * 8, st["resid_bit"])
+    subs = np.frombuffer(blob, "<u2", 5 * M, at + 8 * M + 4 * M).reshape(M, 5)
+    assert np.array_equal(subs, st["sub_offs"])
