@@ -974,72 +974,66 @@ __device__ __forceinline__ bool residual(const uint32_t* w, uint32_t rbase, uint
     return ok;
 }
 
-// Codeword skipping by table.  Entry [eg][k][b] describes the whole
-// Rice(k) (eg = 0) or Exp-Golomb(k) (eg = 1) codewords at the start of the 8
-// bits b (MSB first): their count | their total length << 4.  A compile-time
-// constant in device memory, never written, so it is read through L1.
-struct SkipTable {
-    uint8_t e[2][8][256];
-};
-
-constexpr SkipTable make_skip_table() {
-    SkipTable t{};
-    for (int eg = 0; eg < 2; eg++)
-        for (int k = 0; k < 8; k++)
-            for (int b = 0; b < 256; b++) {
-                int at = 0, cnt = 0;
-                for (;;) {
-                    int z = 0;
-                    while (at + z < 8 && ((b >> (7 - at - z)) & 1) == 0) z++;
-                    if (at + z >= 8) break;  // no terminating one inside the byte
-                    const int len = z + 1 + (eg ? z : 0) + k;
-                    if (at + len > 8) break;
-                    at += len;
-                    cnt++;
-                }
-                t.e[eg][k][b] = static_cast<uint8_t>(cnt | (at << 4));
-            }
-    return t;
-}
-
-__device__ const SkipTable g_skip_table = make_skip_table();
-
 // Skip n codewords (substream boundaries are not stored in the stream).
-// In a long substream (32 codewords or more, k < 8), while at least eight
-// remain, one table read takes every whole codeword of the next 8 bits (a
-// bit scan per codeword measured about 80 cycles each on one warp; the
-// table's first reads miss L1, which short substreams would not repay);
-// otherwise up to four codewords that lie wholly inside the 32-bit window
-// are taken per step; a codeword longer than the window goes to the general
-// reader.
+// Rice(0) codewords (the common case: smooth residuals) are skipped by
+// counting one bits, about twenty per step; others up to four per step,
+// those that lie wholly inside the 32-bit window (a bit scan per codeword,
+// about 80 cycles each measured on one warp); a codeword longer than the
+// window goes to the general reader.  (An 8-bit table of whole codewords
+// per step measured slower than both on mixed warps.)
 template <bool kShared>
 __device__ __forceinline__ bool skip_codes(const uint32_t* w, uint32_t rbase, uint32_t& pos, uint32_t tk,
                                            uint32_t n, uint32_t limit) {
     const uint32_t k = tk & 0x3Fu;
     const bool eg = (tk & 0x80u) != 0u;
-    const uint8_t* tab = (k < 8u && n >= 32u) ? g_skip_table.e[eg ? 1 : 0][k] : nullptr;
     bool ok = true;
     BitWin<kShared> b;
     b.w = w;
     b.rbase = rbase;
     b.seek(pos);
+    if (!eg && k == 0u) {
+        // Rice(0) codewords are unary: each ends at a one bit, so skipping n
+        // of them is finding the n-th one bit -- a population count per 32
+        // bits, then a five-step halving search inside the last window.
+        while (n > 0u) {
+            const uint32_t x = b.peek();
+            const uint32_t c = __popc(x);
+            if (c < n) {
+                b.advance(32u);
+                n -= c;
+            } else {
+                uint32_t y = x, at = 0u, need = n;
+#pragma unroll
+                for (uint32_t wd = 16u; wd >= 1u; wd >>= 1) {
+                    const uint32_t t = __popc(y >> (32u - wd));  // ones in the top wd bits
+                    const bool skip = t < need;
+                    need -= skip ? t : 0u;
+                    y = skip ? (y << wd) : y;
+                    at += skip ? wd : 0u;
+                }
+                b.advance(at + 1u);  // through the n-th one
+                n = 0u;
+            }
+            if (b.pos > limit) {  // only a corrupt stream runs past its meshlet
+                ok = false;
+                b.seek(limit);
+                break;
+            }
+        }
+        pos = b.pos;
+        return ok;
+    }
     while (n > 0u) {
         const uint32_t x = b.peek();
         uint32_t used = 0u, cnt = 0u;
-        const uint32_t e = (tab && n >= 8u) ? __ldg(tab + (x >> 24)) : 0u;
-        if (e & 15u) {
-            cnt = e & 15u;
-            used = e >> 4;
-        } else {
 #pragma unroll
-            for (int s = 0; s < 4; s++) {
-                const uint32_t xx = __funnelshift_lc(0u, x, used);  // the window past the codewords taken
-                const uint32_t z = __clz(xx);                       // 32 when nothing is left
-                const uint32_t len = z + 1u + (eg ? z : 0u) + k;
-                const bool fits = (used + len <= 32u) & (cnt < n);
-                used += fits ? len : 0u;
-                cnt += fits ? 1u : 0u;
-            }
+        for (int s = 0; s < 4; s++) {
+            const uint32_t xx = __funnelshift_lc(0u, x, used);  // the window past the codewords taken
+            const uint32_t z = __clz(xx);                       // 32 when nothing is left
+            const uint32_t len = z + 1u + (eg ? z : 0u) + k;
+            const bool fits = (used + len <= 32u) & (cnt < n);
+            used += fits ? len : 0u;
+            cnt += fits ? 1u : 0u;
         }
         if (cnt) {
             b.advance(used);
