@@ -26,7 +26,7 @@ ENCODER_LIB = os.path.join(HERE, "libstride_encode.so")
 CUDA_SOURCES = ["stride_kernels.cu", "stride_api.cu", "stride_batch.cu", "stride_serve.cu", "stride_static.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3",
               "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off",
-              "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills", "-Xptxas", "-dlcm=cg"]
+              "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
 
 
 def _nvcc() -> str:
