@@ -5,9 +5,9 @@ Workloads (``--workload``):
   heightfield   (default) one 2049 x 2049 heightfield mesh, 8,388,608
                 triangles, 12-bit bbox quantisation (``--bits``), seeded
                 value-noise heights, encoded by the project encoder.  One step
-                = one decode of the whole stream (scan, connectivity and
-                vertex kernels: one stride_decode call) into resident device
-                buffers.
+                = one decode of the whole stream (the scan kernel, then one
+                fused connectivity + vertex kernel: one stride_decode call)
+                into resident device buffers.
   icosphere     the level-8 displaced icosphere (1,310,720 triangles).
   batch         many meshes with log-uniform sizes decoded in one persistent
                 launch (CUDA graph), next to per-mesh launches.
@@ -198,6 +198,19 @@ def measured_peak():
             p = json.load(f)
         return float(p["hbm_gbs"]), "measured (MEASURED_PEAKS.json hbm_gbs, burst copy)"
     return 6800.0, "fallback 6.8 TB/s"
+
+
+def kernel_split(kern, fused: bool, stream_bytes: int, n_v: int, n_t: int):
+    """Names of the decode's kernels, the dominant one and its algorithmic
+    bytes, from the per-kernel times (scan, connectivity, vertex; the fused
+    kernel's time in the second slot)."""
+    if fused:  # the fused kernel reads the stream and writes both outputs
+        return ("scan_kernel", "flow_kernel"), 1, stream_bytes + 12 * (n_v + n_t)
+    # connectivity reads the stream and writes the indices (12 B per
+    # triangle); the vertex kernel writes the positions (12 B per vertex)
+    # from residual bits already counted in the stream
+    dom = 1 + int(np.argmax(kern[1:3]))
+    return ("scan_kernel", "conn_kernel", "vert_kernel"), dom, (stream_bytes + 12 * n_t) if dom == 1 else 12 * n_v
 
 
 def ncu_traffic(kernel: str, workload: str):
@@ -402,17 +415,12 @@ def run_single(args):
     mean_step = reduce_max(sum(step_ms) / len(step_ms), dev)
     value = replica_value(n_t, world, mean_step / 1e3) / 1e6
 
-    # Dominant kernel: the slower of connectivity / vertex kernels.  Its
-    # algorithmic bytes: connectivity reads the whole stream and writes the
-    # indices (12 B per triangle); the vertex kernel writes the positions
-    # (12 B per vertex) from the residual bits, which are already counted in
-    # the stream.  The step's algorithmic bytes are stream + both outputs.
+    # Dominant kernel and its algorithmic bytes; the step's algorithmic
+    # bytes are stream + both outputs.
     alg_bytes = len(data) + 12 * (n_v + n_t)
     peak, peak_src = measured_peak()
     k = np.array(kern_ms).mean(axis=0)
-    names = ("scan_kernel", "conn_kernel", "vert_kernel")
-    dom = 1 + int(np.argmax(k[1:]))
-    dom_bytes = (len(data) + 12 * n_t) if dom == 1 else 12 * n_v
+    names, dom, dom_bytes = kernel_split(k, int(dec.info.kernels) == 2, len(data), n_v, n_t)
     achieved = dom_bytes / (k[dom] / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": ncu_traffic(names[dom], cfg["workload"]),
@@ -485,13 +493,15 @@ def run_batch(args):
     blobs, cfg = batch_streams(args.batch_meshes, args.bits)
     n_t_all = cfg["triangles"]
     lib = _lib.load()
-    # scan (with the dequantisation tables) + connectivity + vertex kernels
-    per_step_kernels = 3
     b = BatchDecoder(blobs)
     launch = None
     if args.tune:
         best, best_ms = b.autotune(iters=2)
         launch = dict(best.as_dict(), tuned_ms=round(best_ms, 4))
+    # scan (with the dequantisation tables), then the fused kernel or the
+    # connectivity and vertex kernels
+    fused = int(b.config().persistent) == 2
+    per_step_kernels = 2 if fused else 3
     stream = torch.cuda.Stream(device=dev)
     with torch.cuda.stream(stream):
         b.capture_graph(stream)
@@ -541,6 +551,7 @@ def run_batch(args):
 
     # per-mesh plain launches (one ParaDeltaV5GpuDecoder per mesh, own outputs)
     decs = [ParaDeltaV5GpuDecoder(x) for x in blobs]
+    per_mesh_launches = sum(int(d.info.kernels) for d in decs)
     outs = [(torch.empty((d.n_t_total, 3), dtype=torch.int32, device=dev),
              torch.empty((d.n_v_total, 3), dtype=torch.float32, device=dev)) for d in decs]
     sh = ctypes.c_void_p(int(stream.cuda_stream))
@@ -604,9 +615,7 @@ def run_batch(args):
 
     if rank == 0:
         peak, peak_src = measured_peak()
-        names = ("scan_kernel", "conn_kernel", "vert_kernel")
-        dom = 1 + int(np.argmax(kern[1:]))
-        dom_bytes = (cfg["stream_bytes"] + 12 * b.n_t_total) if dom == 1 else 12 * b.n_v_total
+        names, dom, dom_bytes = kernel_split(kern, fused, cfg["stream_bytes"], b.n_v_total, b.n_t_total)
         achieved = dom_bytes / (kern[dom] / 1e3) / 1e9
         alg = cfg["stream_bytes"] + 12 * (b.n_t_total + b.n_v_total)
         cfg = dict(cfg)
@@ -621,7 +630,7 @@ def run_batch(args):
             "data": "synthetic (seeded mixed meshes; reference meshes not available)", "config": cfg,
             "per_mesh": {"value": round(replica_value(n_t_all, world, per_mesh_ms / 1e3) / 1e6, 3),
                          "unit": "M tris/s", "ms_per_step": round(per_mesh_ms, 4),
-                         "launches_per_step": 3 * len(blobs), "same_output_as_batched": bool(same_as_batch)},
+                         "launches_per_step": per_mesh_launches, "same_output_as_batched": bool(same_as_batch)},
             "batched_over_per_mesh": round(per_mesh_ms / batched_ms, 3),
             "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                          "frac": round(achieved / peak, 4), "traffic": ncu_traffic(names[dom], cfg["workload"]),

@@ -59,9 +59,12 @@ typedef struct {
     float scale;
     int32_t pred_n[9];
     int32_t pred_k[3];
-    uint32_t kernels;    /* kernel launches one decode makes: 3 (scan, which also
-                            fills any per-code dequantisation tables;
-                            connectivity; vertex), 0 for an empty stream     */
+    uint32_t kernels;    /* kernel launches one decode makes: 2 with the
+                            default launch shape (scan, which also fills any
+                            per-code dequantisation tables; one fused
+                            connectivity + vertex kernel), 3 with the
+                            two-kernel shapes (persistent 0 or 1), 0 for an
+                            empty stream                                      */
 } stride_info_t;
 
 /* Launch shape of the decode kernel (the autotuner's search space). */
@@ -70,7 +73,13 @@ typedef struct {
                                 (1, 2) or two (4) parser/assembler warp pairs
                                 of 32 meshlets each; the vertex kernel's CTA is
                                 always three warps (one per axis)            */
-    int32_t persistent;      /* 1 = persistent work-stealing vertex grid     */
+    int32_t persistent;      /* 2 (default) = one persistent kernel for both
+                                phases: CTAs of two pairs take connectivity
+                                groups, then vertex work in the order groups
+                                finish (warps_per_cta must be 4);
+                                1 = connectivity kernel, then a persistent
+                                work-stealing vertex grid; 0 = connectivity
+                                kernel, then one vertex CTA per group        */
     int32_t ctas_per_sm;     /* persistent grid = ctas_per_sm * SMs
                                 (0 = as many as fit)                         */
     uint32_t stage_bytes;    /* the vertex kernel stages a round's residual
@@ -124,8 +133,10 @@ int stride_decode(stride_handle* h, void* stream, uint32_t* d_idx, float* d_pos,
 
 /* Decode with host buffers: enqueue decode into handle-owned device outputs,
  * copy them to h_idx / h_pos (host, n_t*3 uint32 and n_v*3 float32) and
- * synchronise.  Returns the decode status.  Replaces decode_to_host
- * (utils/paradelta_v5_cuda.py:714-718). */
+ * synchronise.  Returns the decode status.  The triangle copy starts when
+ * the connectivity kernel ends, beside the vertex kernel (a fused launch
+ * shape is replaced by the persistent two-kernel one for this call).
+ * Replaces decode_to_host (utils/paradelta_v5_cuda.py:714-718). */
 int stride_decode_host(stride_handle* h, void* stream, uint32_t* h_idx, float* h_pos);
 
 /* Status of the last decode enqueued on this handle.  wait != 0 blocks until
@@ -169,10 +180,11 @@ int stride_cull_meshlets(const float* d_bounds, uint32_t n, const float* planes,
                          uint32_t* d_count);
 
 /* Measurement entry point (no reference counterpart): one decode like
- * stride_decode, with CUDA events recorded on `stream` between its three
+ * stride_decode, with CUDA events recorded on `stream` between its
  * kernels; waits and writes their durations in milliseconds to
  * kernel_ms[0] (meshlet scan), kernel_ms[1] (connectivity) and
- * kernel_ms[2] (vertices + output). */
+ * kernel_ms[2] (vertices + output).  With the fused kernel (persistent 2,
+ * the default) kernel_ms[1] is the fused kernel and kernel_ms[2] is 0. */
 int stride_decode_timed(stride_handle* h, void* stream, uint32_t* d_idx, float* d_pos, float* kernel_ms);
 
 /* Launch shape for this handle's decodes (defaults are used until set). */
@@ -215,7 +227,8 @@ int stride_batch_set_config(stride_batch* b, const stride_launch_cfg* cfg);
 int stride_batch_get_config(const stride_batch* b, stride_launch_cfg* cfg);
 int stride_batch_decode(stride_batch* b, void* stream, uint32_t* d_idx, float* d_pos);
 /* Same decode, synchronous, with the device time of the scan, connectivity
- * and vertex kernels (CUDA events) in kernel_ms[0..2]. */
+ * and vertex kernels (CUDA events) in kernel_ms[0..2] (fused kernel: in
+ * kernel_ms[1], kernel_ms[2] = 0, as for stride_decode_timed). */
 int stride_batch_decode_timed(stride_batch* b, void* stream, uint32_t* d_idx, float* d_pos, float* kernel_ms);
 /* The arena image: stream i sits at blob_offsets[i] of an image_bytes-long
  * buffer (zero bytes elsewhere).  A caller that keeps such an image in

@@ -311,7 +311,7 @@ int stride_device_info(int* sm_count, int* arch) {
     return STRIDE_OK;
 }
 
-static void fill_info(const MeshParams& p, size_t len, stride_info_t* info) {
+static void fill_info(const MeshParams& p, size_t len, int persistent, stride_info_t* info) {
     std::memset(info, 0, sizeof(*info));
     info->n_meshlets = p.n_meshlets;
     for (int i = 0; i < 3; i++) {
@@ -324,7 +324,8 @@ static void fill_info(const MeshParams& p, size_t len, stride_info_t* info) {
     info->n_v = p.n_v;
     info->n_t = p.n_t;
     info->nbytes = len;
-    info->kernels = p.n_meshlets ? 3u : 0u;  // scan (+ tables), connectivity, vertex
+    // scan (+ tables), then one fused kernel or the connectivity and vertex kernels
+    info->kernels = p.n_meshlets ? (persistent == 2 ? 2u : 3u) : 0u;
 }
 
 int stride_inspect(const uint8_t* data, size_t len, stride_info_t* info) {
@@ -333,7 +334,7 @@ int stride_inspect(const uint8_t* data, size_t len, stride_info_t* info) {
     char why[256] = {0};
     const int rc = parse_header(data, len, &p, why, sizeof(why));
     if (rc) return fail(rc, "%s", why);
-    fill_info(p, len, info);
+    fill_info(p, len, LaunchCfg().persistent, info);
     return STRIDE_OK;
 }
 
@@ -391,7 +392,7 @@ int stride_reload(stride_handle* h, const uint8_t* data, size_t len, void* strea
 
 int stride_info(const stride_handle* h, stride_info_t* info) {
     if (!h || !info) return fail(STRIDE_ERR_ARG, "null argument");
-    fill_info(h->params, h->len, info);
+    fill_info(h->params, h->len, h->cfg.persistent, info);
     return STRIDE_OK;
 }
 
@@ -548,9 +549,13 @@ int stride_decode_host(stride_handle* h, void* stream, uint32_t* h_idx, float* h
     // The triangle indices are final when the connectivity kernel ends, so
     // their copy to the host runs beside the vertex kernel; each output goes
     // out in two halves on the handle's two copy streams (two copy engines).
+    // The link is the bound here, so the decode takes the two-kernel shape,
+    // whose connectivity ends first (the fused kernel's ends with it).
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     void* ev[4] = {nullptr, nullptr, h->conn_done, h->vert_done};
-    int rc = enqueue_decode(handle_args(h, h->d_idx, h->d_pos, nullptr), h->cfg, stream, ev);
+    LaunchCfg cfg = h->cfg;
+    if (cfg.persistent == 2) cfg.persistent = 1;
+    int rc = enqueue_decode(handle_args(h, h->d_idx, h->d_pos, nullptr), cfg, stream, ev);
     if (rc) return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     h->launched = true;
     const size_t ib = 12 * h->params.n_t, pb = 12 * h->params.n_v;

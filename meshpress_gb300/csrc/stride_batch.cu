@@ -336,7 +336,7 @@ int stride_batch_autotune(stride_batch* b, void* stream, uint32_t* d_idx, float*
     for (int w : {1, 2, 4})
         for (uint32_t st : stage_opts)
             for (uint32_t cb : code_opts)
-                for (int pers : {0, 1}) {
+                for (int pers : {0, 1, 2}) {
                     LaunchCfg c;
                     c.warps_per_cta = w;
                     c.stage_bytes = st;

@@ -100,12 +100,13 @@ struct Status {
     unsigned int ticket;     // scan blocks finished (the last one scans block sums)
     unsigned int work_conn;  // persistent work counters
     unsigned int work_vert;
-    unsigned int pad[3];
+    unsigned int done_tail;  // entries in the completion list (fused kernel)
+    unsigned int pad[2];
 };
 
 struct LaunchCfg {
     int warps_per_cta = 4;
-    int persistent = 1;
+    int persistent = 2;  // 0: one vertex CTA per group, 1: persistent vertex grid, 2: one fused kernel
     int ctas_per_sm = 0;
     uint32_t stage_bytes = 16 * 1024;  // per-warp payload staging (vertex kernel: half)
     uint32_t code_bytes = 12 * 1024;   // per-warp integer code plane (vertex kernel)

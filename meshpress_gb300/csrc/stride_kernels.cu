@@ -29,6 +29,7 @@
 //     dequantisation, stride_dequant.h).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
 #include <cstring>
 #include <type_traits>
@@ -891,29 +892,17 @@ __device__ void conn_assemble(const DecodeArgs& a, const GroupLane& L, bool act,
     }
 }
 
-// Pair p of a CTA (warps 2p and 2p + 1: parser, assembler) decodes group
-// blockIdx.x * G + p in one round: every lane streams its own meshlet, so
-// no meshlet is too large.  Past the kernel-entry barrier the pairs never
-// wait for one another.
+// Connectivity of group g by one warp pair (its shared memory at `base`):
+// every lane streams its own meshlet, so no meshlet is too large.
 template <int G>
-__global__ void __launch_bounds__(G * 64) conn_kernel(DecodeArgs a) {
-    extern __shared__ __align__(128) uint8_t smem[];
-    const uint32_t pair = threadIdx.x >> 6;
-    const bool parser = ((threadIdx.x >> 5) & 1u) == 0u;
-    const int lane = threadIdx.x & 31;
-    const bool failed = *reinterpret_cast<volatile unsigned long long*>(&a.status->err) != 0ull;
-    if (__syncthreads_or(failed)) return;
-    uint8_t* base = smem + pair * conn_pair_bytes();
+__device__ __forceinline__ void conn_group(const DecodeArgs& a, uint32_t g, uint32_t pair, bool parser, int lane,
+                                           uint8_t* base) {
     uint32_t* rings = reinterpret_cast<uint32_t*>(base);
     uint32_t* recs = rings + 32u * kLaneRingWords;
     uint32_t* counts = recs + 2u * kChunk * 32u;
     uint32_t* seen = counts + 4;
     uint32_t* tring = seen + 8 * 32;
     uint32_t* wring = tring + 32 * kRingRow;
-    const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
-    const uint32_t f = blockIdx.x * G + pair;
-    if (f >= n_groups) return;  // both warps of the pair
-    const uint32_t g = group_at(f, n_groups);
     GroupLane L;
     load_group_lane(a, g, lane, L);
     bool ok = L.valid;
@@ -927,6 +916,23 @@ __global__ void __launch_bounds__(G * 64) conn_kernel(DecodeArgs a) {
     } else {
         conn_assemble<G>(a, L, ok, seen, tring, wring, recs, counts, pair, lane);
     }
+}
+
+// Pair p of a CTA (warps 2p and 2p + 1: parser, assembler) decodes group
+// blockIdx.x * G + p in one round.  Past the kernel-entry barrier the pairs
+// never wait for one another.
+template <int G>
+__global__ void __launch_bounds__(G * 64) conn_kernel(DecodeArgs a) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    const uint32_t pair = threadIdx.x >> 6;
+    const bool parser = ((threadIdx.x >> 5) & 1u) == 0u;
+    const int lane = threadIdx.x & 31;
+    const bool failed = *reinterpret_cast<volatile unsigned long long*>(&a.status->err) != 0ull;
+    if (__syncthreads_or(failed)) return;
+    const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
+    const uint32_t f = blockIdx.x * G + pair;
+    if (f >= n_groups) return;  // both warps of the pair
+    conn_group<G>(a, group_at(f, n_groups), pair, parser, lane, smem + pair * conn_pair_bytes());
 }
 
 // ---------------------------------------------------------------------------
@@ -1287,8 +1293,95 @@ __device__ __forceinline__ void vert_round(const DecodeArgs& a, const GroupLane&
     }
 }
 
-// A CTA decodes one group of 32 meshlets with three warps, warp d = axis d;
-// the group's residual bits are staged once and read by all three.
+// Axis d of group g's 32 meshlets by warp d of the CTA (warps 0..2; a
+// fourth warp, d = 3, only joins the CTA's barriers and the stage pass); the
+// group's residual bits are staged once and read by all three axis warps.
+// False when a stage copy did not arrive in time (reported).
+template <bool kWide>
+__device__ __forceinline__ bool vert_group(const DecodeArgs& a, uint32_t g, uint32_t d, int lane, uint32_t* stage,
+                                           uint8_t* planes, uint64_t* bar, uint32_t& phase, uint32_t vstage,
+                                           uint32_t code_bytes) {
+    GroupLane L;
+    load_group_lane(a, g, lane, L);
+    const uint32_t n_local = L.d.counts0 & 0xFFFFu;
+    bool ok = L.valid;
+    if (ok && !placement_ok(a, L)) {
+        if (d == 0u) report(a.status, kErrCorrupt, L.m);
+        ok = false;
+    }
+    // this lane's residual bits: anchor .. end, 16-byte aligned
+    const unsigned long long src16 = (L.blob_off + (L.d.anchor_bit >> 3)) & ~15ull;
+    const unsigned long long end16 = (L.blob_off + ((L.d.end_bit + 7u) >> 3) + 15ull) & ~15ull;
+    const uint32_t ssz = ok ? static_cast<uint32_t>(end16 - src16) : 0u;
+    // its stage region: an odd number of 16-byte units, for the reason
+    // the code planes have odd word counts (lanes read at about the same
+    // offsets at the same time)
+    const uint32_t sreg = ssz + ((ssz & 16u) ? 0u : 16u);
+    // A lane's code plane is an odd number of words: the walk visits local
+    // ids in about the same order in every meshlet, so the lanes read and
+    // write at about the same offsets at the same time, and odd strides
+    // put those offsets in different banks (16-byte strides used 8).
+    const uint32_t csz = 4u * (((n_local * static_cast<uint32_t>(sizeof(PlaneT<kWide>)) + 3u) >> 2) | 1u);
+    // the three warps see the same descriptors, so they form the same rounds
+    uint32_t todo = __ballot_sync(kFull, ok);
+    while (todo) {
+        const int first = __ffs(todo) - 1;
+        const bool in = (todo >> lane) & 1u;
+        uint32_t cc = in ? csz : 0u, cs = in ? sreg : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t1 = __shfl_up_sync(kFull, cc, o);
+            const uint32_t t2 = __shfl_up_sync(kFull, cs, o);
+            if (lane >= o) {
+                cc += t1;
+                cs += t2;
+            }
+        }
+        const bool fit = in && cc <= code_bytes && cs <= vstage;
+        uint32_t rmask = __ballot_sync(kFull, fit);
+        const bool staged = rmask != 0u;
+        if (!staged) {  // one meshlet whose residuals exceed the stage: global reads
+            rmask = 1u << first;
+            cc = in ? csz : 0u;
+        }
+        todo &= ~rmask;
+        const bool act = (rmask >> lane) & 1u;
+        const uint32_t code_off = act ? cc - csz : 0u;
+        if (staged) {
+            // bytes the copies deliver (the regions' padding is not copied)
+            const uint32_t total = __reduce_add_sync(kFull, act ? ssz : 0u);
+            const uint32_t dst_off = act ? cs - sreg : 0u;
+            if (d == 0u) {
+                if (lane == 0) mbar_expect(bar, total);
+                __syncwarp();
+                if (act && ssz)
+                    bulk_copy(reinterpret_cast<uint8_t*>(stage) + dst_off, a.arena + src16, ssz, bar);
+            }
+            const bool timed_out = !mbar_wait(bar, phase);
+            if (__syncthreads_or(timed_out)) {
+                if (threadIdx.x == 0) report(a.status, kErrTimeout, L.m);
+                mbar_wait(bar, phase);  // let the copies land before the CTA exits
+                return false;
+            }
+            phase ^= 1u;
+            {  // the round's stage in bit order, once for the three warps
+                const uint32_t words = __shfl_sync(kFull, cs, 31 - __clz(rmask)) >> 2;
+                for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) stage[i] = bswap32(stage[i]);
+                __syncthreads();
+            }
+            const uint32_t rbase = static_cast<uint32_t>(L.blob_off * 8ull - src16 * 8ull + dst_off * 8ull);
+            if (d < 3u) vert_round<true, kWide>(a, L, d, act, rmask, stage, rbase, planes, code_off, lane);
+        } else if (d < 3u) {
+            vert_round<false, kWide>(a, L, d, act, rmask,
+                                     reinterpret_cast<const uint32_t*>(a.arena + L.blob_off), 0u, planes,
+                                     code_off, lane);
+        }
+        __syncthreads();  // the next round overwrites the stage
+    }
+    return true;
+}
+
+// A CTA decodes one group of 32 meshlets with three warps, warp d = axis d.
 template <bool kWide>
 __global__ void __launch_bounds__(96, 1) vert_kernel(DecodeArgs a, uint32_t stage_bytes, uint32_t code_bytes,
                                                   int persistent) {
@@ -1313,89 +1406,125 @@ __global__ void __launch_bounds__(96, 1) vert_kernel(DecodeArgs a, uint32_t stag
         f = s_group;
     }
     while (f < n_groups) {
-        const uint32_t g = group_at(f, n_groups);
-        GroupLane L;
-        load_group_lane(a, g, lane, L);
-        const uint32_t n_local = L.d.counts0 & 0xFFFFu;
-        bool ok = L.valid;
-        if (ok && !placement_ok(a, L)) {
-            if (d == 0u) report(a.status, kErrCorrupt, L.m);
-            ok = false;
-        }
-        // this lane's residual bits: anchor .. end, 16-byte aligned
-        const unsigned long long src16 = (L.blob_off + (L.d.anchor_bit >> 3)) & ~15ull;
-        const unsigned long long end16 = (L.blob_off + ((L.d.end_bit + 7u) >> 3) + 15ull) & ~15ull;
-        const uint32_t ssz = ok ? static_cast<uint32_t>(end16 - src16) : 0u;
-        // its stage region: an odd number of 16-byte units, for the reason
-        // the code planes have odd word counts (lanes read at about the same
-        // offsets at the same time)
-        const uint32_t sreg = ssz + ((ssz & 16u) ? 0u : 16u);
-        // A lane's code plane is an odd number of words: the walk visits local
-        // ids in about the same order in every meshlet, so the lanes read and
-        // write at about the same offsets at the same time, and odd strides
-        // put those offsets in different banks (16-byte strides used 8).
-        const uint32_t csz = 4u * (((n_local * static_cast<uint32_t>(sizeof(PlaneT<kWide>)) + 3u) >> 2) | 1u);
-        // the three warps see the same descriptors, so they form the same rounds
-        uint32_t todo = __ballot_sync(kFull, ok);
-        while (todo) {
-            const int first = __ffs(todo) - 1;
-            const bool in = (todo >> lane) & 1u;
-            uint32_t cc = in ? csz : 0u, cs = in ? sreg : 0u;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t t1 = __shfl_up_sync(kFull, cc, o);
-                const uint32_t t2 = __shfl_up_sync(kFull, cs, o);
-                if (lane >= o) {
-                    cc += t1;
-                    cs += t2;
-                }
-            }
-            const bool fit = in && cc <= code_bytes && cs <= vstage;
-            uint32_t rmask = __ballot_sync(kFull, fit);
-            const bool staged = rmask != 0u;
-            if (!staged) {  // one meshlet whose residuals exceed the stage: global reads
-                rmask = 1u << first;
-                cc = in ? csz : 0u;
-            }
-            todo &= ~rmask;
-            const bool act = (rmask >> lane) & 1u;
-            const uint32_t code_off = act ? cc - csz : 0u;
-            if (staged) {
-                // bytes the copies deliver (the regions' padding is not copied)
-                const uint32_t total = __reduce_add_sync(kFull, act ? ssz : 0u);
-                const uint32_t dst_off = act ? cs - sreg : 0u;
-                if (d == 0u) {
-                    if (lane == 0) mbar_expect(bar, total);
-                    __syncwarp();
-                    if (act && ssz)
-                        bulk_copy(reinterpret_cast<uint8_t*>(stage) + dst_off, a.arena + src16, ssz, bar);
-                }
-                const bool timed_out = !mbar_wait(bar, phase);
-                if (__syncthreads_or(timed_out)) {
-                    if (threadIdx.x == 0) report(a.status, kErrTimeout, L.m);
-                    mbar_wait(bar, phase);  // let the copies land before the CTA exits
-                    return;
-                }
-                phase ^= 1u;
-                {  // the round's stage in bit order, once for the three warps
-                    const uint32_t words = __shfl_sync(kFull, cs, 31 - __clz(rmask)) >> 2;
-                    for (uint32_t i = threadIdx.x; i < words; i += 96u) stage[i] = bswap32(stage[i]);
-                    __syncthreads();
-                }
-                const uint32_t rbase = static_cast<uint32_t>(L.blob_off * 8ull - src16 * 8ull + dst_off * 8ull);
-                vert_round<true, kWide>(a, L, d, act, rmask, stage, rbase, planes, code_off, lane);
-            } else {
-                vert_round<false, kWide>(a, L, d, act, rmask,
-                                         reinterpret_cast<const uint32_t*>(a.arena + L.blob_off), 0u, planes,
-                                         code_off, lane);
-            }
-            __syncthreads();  // the next round overwrites the stage
-        }
+        if (!vert_group<kWide>(a, group_at(f, n_groups), d, lane, stage, planes, bar, phase, vstage, code_bytes))
+            return;
         if (!persistent) break;
         __syncthreads();  // every thread has read s_group
         if (threadIdx.x == 0) s_group = atomicAdd(&a.status->work_vert, 1u);
         __syncthreads();
         f = s_group;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 4. one kernel for both phases
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t ld_acquire_u32(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
+    asm volatile("st.release.gpu.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Entry i of the completion list: word pad[0] of meshlet 32 i's record
+// (i < the number of groups, so the record exists; the scan zeroes it), set
+// to group + 1 when the group's connectivity is written.
+__device__ __forceinline__ uint32_t* done_entry(const DecodeArgs& a, uint32_t i) { return &a.descs[32u * i].pad[0]; }
+
+// Named barrier of a pair's two warps for taking and finishing groups
+// (immediate ids 9 and 10, past the record barriers 1..8).
+__device__ __forceinline__ void claim_bar(uint32_t pair) {
+    if (pair == 0u) {
+        bar_sync_imm<9>();
+    } else {
+        bar_sync_imm<10>();
+    }
+}
+
+// The next group of the vertex phase: the next completion-list entry,
+// waited for (bounded, about a second of SM clocks).  n_groups when the list
+// is used up, the decode has failed, or the wait ran out (reported).
+__device__ uint32_t next_done_group(const DecodeArgs& a, uint32_t n_groups) {
+    const uint32_t i = atomicAdd(&a.status->work_vert, 1u);
+    if (i >= n_groups) return n_groups;
+    const uint32_t* e = done_entry(a, i);
+    const long long t0 = clock64();
+    for (;;) {
+        const uint32_t v = ld_acquire_u32(e);
+        if (v != 0u) return v - 1u < n_groups ? v - 1u : n_groups;
+        if (*reinterpret_cast<volatile unsigned long long*>(&a.status->err) != 0ull) return n_groups;
+        if (clock64() - t0 > (1ll << 31)) {
+            report(a.status, kErrTimeout, 32u * i);
+            return n_groups;
+        }
+        __nanosleep(256);
+    }
+}
+
+// Connectivity and vertices in one persistent launch.  Each CTA's two warp
+// pairs take connectivity groups (costliest first) until none is left; a
+// finished group is appended to the completion list.  Then the CTA turns to
+// the vertex phase (its shared memory becomes the stage and the code planes)
+// and takes groups from the list in completion order, so the vertex work of
+// the groups that finish early runs while the costliest connectivity groups
+// are still decoding.  A CTA in the vertex phase waits only for groups that
+// running CTAs have taken (every group is taken before any CTA leaves the
+// connectivity phase, and that phase waits for nothing), so every wait ends.
+// kMinBlocks: CTAs per SM the registers are budgeted for (4: 128 registers
+// a thread; 5: 96, which suits large launches).
+template <bool kWide, int kMinBlocks>
+__global__ void __launch_bounds__(128, kMinBlocks) flow_kernel(DecodeArgs a, uint32_t stage_bytes,
+                                                               uint32_t code_bytes) {
+    extern __shared__ __align__(128) uint8_t smem[];
+    __shared__ uint32_t s_claim[2];
+    __shared__ uint32_t s_group;
+    const uint32_t warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+    const bool failed = *reinterpret_cast<volatile unsigned long long*>(&a.status->err) != 0ull;
+    if (__syncthreads_or(failed)) return;
+    const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
+    {
+        const uint32_t pair = warp >> 1;
+        const bool parser = (warp & 1u) == 0u;
+        uint8_t* base = smem + pair * conn_pair_bytes();
+        // each pair's first group by position, as the connectivity kernel
+        // hands them out (the CTAs dispatched first, one per SM, take two);
+        // later groups are taken from the counter
+        const uint32_t n_first = min(n_groups, 2u * gridDim.x);
+        uint32_t f = blockIdx.x * 2u + pair;
+        for (;;) {
+            if (f >= n_first) {  // pair-uniform
+                if (parser && lane == 0) s_claim[pair] = n_first + atomicAdd(&a.status->work_conn, 1u);
+                claim_bar(pair);
+                f = s_claim[pair];
+            }
+            if (f >= n_groups) break;
+            const uint32_t g = group_at(f, n_groups);
+            conn_group<2>(a, g, pair, parser, lane, base);
+            __threadfence();  // this thread's outputs, before the list entry
+            claim_bar(pair);  // both warps are done with the group
+            if (!parser && lane == 0) st_release_u32(done_entry(a, atomicAdd(&a.status->done_tail, 1u)), g + 1u);
+            f = n_first;
+        }
+    }
+    __syncthreads();  // both pairs are through: the memory becomes the vertex layout
+    const uint32_t vstage = vert_stage_bytes(stage_bytes);
+    uint32_t* stage = reinterpret_cast<uint32_t*>(smem);
+    uint8_t* planes = smem + align16(vstage + 32u) + min(warp, 2u) * vert_axis_bytes(code_bytes);
+    uint64_t* bar = reinterpret_cast<uint64_t*>(smem + align16(vstage + 32u) + 3u * vert_axis_bytes(code_bytes));
+    if (threadIdx.x == 0) mbar_init(bar);
+    __syncthreads();
+    uint32_t phase = 0u;
+    for (;;) {
+        if (threadIdx.x == 0) s_group = next_done_group(a, n_groups);
+        __syncthreads();
+        const uint32_t g = s_group;
+        if (g >= n_groups) return;
+        if (!vert_group<kWide>(a, g, warp, lane, stage, planes, bar, phase, vstage, code_bytes)) return;
+        __syncthreads();  // every thread has read s_group
     }
 }
 
@@ -1485,6 +1614,42 @@ cudaError_t launch_vert(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t 
     return cudaGetLastError();
 }
 
+// Shared memory of a fused CTA: the two pairs' connectivity memory, then
+// the vertex layout in the same bytes.
+size_t flow_cta_bytes(const LaunchCfg& cfg) {
+    return std::max<size_t>(2u * conn_pair_bytes(), vert_cta_bytes(cfg.stage_bytes, cfg.code_bytes));
+}
+
+template <bool kWide, int kMinBlocks>
+cudaError_t launch_flow(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s) {
+    static size_t configured[64] = {0};
+    static OccCache occ;
+    const size_t smem = flow_cta_bytes(cfg);
+    cudaError_t e = opt_in_smem(flow_kernel<kWide, kMinBlocks>, smem, configured);
+    if (e != cudaSuccess) return e;
+    const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
+    // one CTA per group (up to the resident count): the vertex phase runs
+    // one group per CTA at a time, and pairs that find no connectivity
+    // group left go straight to it
+    const uint32_t grid = grid_for(flow_kernel<kWide, kMinBlocks>, 128, smem, cfg, n_groups, 1, occ);
+    if (grid == 0) return cudaSuccess;
+    flow_kernel<kWide, kMinBlocks><<<grid, 128, smem, s>>>(a, cfg.stage_bytes, cfg.code_bytes);
+    return cudaGetLastError();
+}
+
+// Groups from which the fused kernel is budgeted for five CTAs per SM.
+// Measured on one GB300: up to about 700 groups four CTAs of 128 registers
+// are faster (1449^2 heightfield, 666 groups: 164 against 174 us); from
+// about 1,300 groups five CTAs of 96 registers are (2897^2 heightfield,
+// 2,700 groups: 432 against 460 us; 4,096 mixed meshes: 3.84 against 4.19 ms).
+constexpr uint32_t kFlowFiveGroups = 1024u;
+
+cudaError_t launch_flow_any(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s) {
+    const bool five = (a.total_meshlets + 31u) / 32u >= kFlowFiveGroups;
+    if (a.wide_codes) return five ? launch_flow<true, 5>(a, cfg, s) : launch_flow<true, 4>(a, cfg, s);
+    return five ? launch_flow<false, 5>(a, cfg, s) : launch_flow<false, 4>(a, cfg, s);
+}
+
 // ev[k] is recorded when ev and ev[k] are non-null
 void record(void* const* ev, int k, cudaStream_t s) {
     if (ev && ev[k]) cudaEventRecord(static_cast<cudaEvent_t>(ev[k]), s);
@@ -1530,9 +1695,12 @@ __global__ void side_table_kernel(const MeshletDesc* __restrict__ descs, uint32_
 
 int check_config(const LaunchCfg& cfg, bool wide) {
     if (cfg.warps_per_cta != 1 && cfg.warps_per_cta != 2 && cfg.warps_per_cta != 4) return STRIDE_ERR_ARG;
+    if (cfg.persistent < 0 || cfg.persistent > 2 || (cfg.persistent == 2 && cfg.warps_per_cta != 4))
+        return STRIDE_ERR_ARG;
     // one meshlet of kMaxLocal vertices, its plane padded to an odd word count
     if (cfg.code_bytes < kMaxLocal * (wide ? 4u : 2u) + 4u || cfg.stage_bytes < 256u) return STRIDE_ERR_ARG;
     if (conn_smem_bytes(cfg) > 227u * 1024u || vert_smem_bytes(cfg) > 227u * 1024u) return STRIDE_ERR_ARG;
+    if (cfg.persistent == 2 && flow_cta_bytes(cfg) > 227u * 1024u) return STRIDE_ERR_ARG;
     return STRIDE_OK;
 }
 
@@ -1554,10 +1722,15 @@ int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void
     record(ev, 1, s);
     if (a.total_meshlets != 0) {
         cudaError_t e;
-        switch (cfg.warps_per_cta) {
-            case 1: e = launch_pair<1>(a, cfg, s, ev); break;
-            case 2: e = launch_pair<2>(a, cfg, s, ev); break;
-            default: e = launch_pair<4>(a, cfg, s, ev); break;
+        if (cfg.persistent == 2) {  // one kernel: the connectivity/vertex split is not timed
+            e = launch_flow_any(a, cfg, s);
+            record(ev, 2, s);
+        } else {
+            switch (cfg.warps_per_cta) {
+                case 1: e = launch_pair<1>(a, cfg, s, ev); break;
+                case 2: e = launch_pair<2>(a, cfg, s, ev); break;
+                default: e = launch_pair<4>(a, cfg, s, ev); break;
+            }
         }
         if (e != cudaSuccess) return STRIDE_ERR_CUDA;
     } else if (ev) {

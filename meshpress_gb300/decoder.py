@@ -67,6 +67,7 @@ class ParaDeltaV5GpuDecoder:
     # -- launch configuration ------------------------------------------------
     def set_launch_config(self, cfg: _lib.LaunchCfg):
         _lib.check(self._lib.stride_set_config(self._h, ctypes.byref(cfg)), "stride_set_config")
+        _lib.check(self._lib.stride_info(self._h, ctypes.byref(self.info)), "stride_info")  # kernels per decode
 
     # -- decoding --------------------------------------------------------------
     def _outputs(self):

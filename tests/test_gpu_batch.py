@@ -60,8 +60,9 @@ def test_batch_matches_oracle_per_mesh(torch_cuda, mixed_streams):
     b.close()
 
 
-@pytest.mark.parametrize("cfg", [(1, 0, 16 * 1024, 8 * 1024), (2, 1, 12 * 1024, 12 * 1024), (4, 1, 8 * 1024, 6 * 1024)],
-                         ids=["w1", "w2p", "w4p"])
+@pytest.mark.parametrize("cfg", [(1, 0, 16 * 1024, 8 * 1024), (2, 1, 12 * 1024, 12 * 1024), (4, 1, 8 * 1024, 6 * 1024),
+                                 (4, 2, 8 * 1024, 6 * 1024)],
+                         ids=["w1", "w2p", "w4p", "w4fused"])
 def test_batch_launch_shapes(torch_cuda, mixed_streams, cfg):
     from meshpress_gb300.batch import BatchDecoder
     b = BatchDecoder(mixed_streams)

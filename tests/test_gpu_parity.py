@@ -139,7 +139,11 @@ def _cfg(w, pers, stage, code, per_sm=0):
     (1, 0, 20 * 1024, 16 * 1024), (2, 0, 16 * 1024, 8 * 1024), (4, 1, 12 * 1024, 6 * 1024),
     (1, 1, 256, 2048),           # tiny stage: meshlets fall back to global reads
     (2, 0, 64 * 1024, 516),      # code plane of one 256-vertex meshlet (odd word count): one per round
-], ids=["w1", "w2", "w4p", "global_reads", "one_per_round"])
+    (4, 2, 12 * 1024, 6 * 1024),  # fused connectivity + vertex kernel
+    (4, 2, 256, 2048),           # fused, global reads
+    (4, 2, 64 * 1024, 516),      # fused, one meshlet per round
+], ids=["w1", "w2", "w4p", "global_reads", "one_per_round", "fused", "fused_global_reads",
+        "fused_one_per_round"])
 def test_launch_shapes_give_identical_output(torch_cuda, cfg):
     V, T = synth.icosphere(5, seed=11)
     e = encoder.encode(V, T, precision_error=B12, precision_mode="bbox_frac")
@@ -147,7 +151,8 @@ def test_launch_shapes_give_identical_output(torch_cuda, cfg):
     assert_same_as_oracle(e.data, pos, idx, codes)
 
 
-@pytest.mark.parametrize("cfg", [(2, 1, 16 * 1024, 1028), (1, 0, 256, 32 * 1024)], ids=["one_per_round", "global_reads"])
+@pytest.mark.parametrize("cfg", [(2, 1, 16 * 1024, 1028), (1, 0, 256, 32 * 1024), (4, 2, 16 * 1024, 1028)],
+                         ids=["one_per_round", "global_reads", "fused_one_per_round"])
 def test_wide_codes_launch_shapes(torch_cuda, cfg):
     """20-bit codes (32-bit code plane) under the smallest plane and stage."""
     V, T = synth.heightfield_grid(129, seed=6)
@@ -156,13 +161,20 @@ def test_wide_codes_launch_shapes(torch_cuda, cfg):
     assert_same_as_oracle(e.data, pos, idx, codes)
 
 
-def test_config_sweep_large_heightfield(torch_cuda):
-    """2049 x 2049 heightfield (8,388,608 triangles) at 12 bits: full-size
-    bit-exact decode against the oracle."""
+@pytest.fixture(scope="module")
+def large_heightfield():
     V, T = synth.noise_heightfield(2049, seed=3)
     e = encoder.encode(V, T, precision_error=B12, precision_mode="bbox_frac")
-    pos, idx, codes = gpu_decode(torch_cuda, e.data)
-    opos, oidx = oracle.decode_mt(e.data, 0)
+    return e, oracle.decode_mt(e.data, 0)
+
+
+@pytest.mark.parametrize("pers", [2, 1], ids=["fused", "two_kernels"])
+def test_config_sweep_large_heightfield(torch_cuda, large_heightfield, pers):
+    """2049 x 2049 heightfield (8,388,608 triangles) at 12 bits: full-size
+    bit-exact decode against the oracle, with the fused kernel (default;
+    1,347 groups take its five-CTA build) and with the two kernels."""
+    e, (opos, oidx) = large_heightfield
+    pos, idx, codes = gpu_decode(torch_cuda, e.data, cfg=_cfg(4, pers, 16 * 1024, 12 * 1024))
     assert np.array_equal(pos.view(np.uint32), opos.view(np.uint32))
     assert np.array_equal(idx.astype(np.int64), oidx)
     assert np.array_equal(codes, e.codes)

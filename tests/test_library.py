@@ -74,7 +74,8 @@ def test_decoder_fails_loudly_without_library(monkeypatch):
 
 
 def test_kernel_count(built_libs):
-    """A decode is three kernel launches: scan (which also fills any per-code
-    dequantisation tables), connectivity, vertex."""
+    """With the default launch shape a decode is two kernel launches: scan
+    (which also fills any per-code dequantisation tables), then the fused
+    connectivity + vertex kernel."""
     for name in ("grid129_b12", "grid9_b12", "grid17_canon_b16", "tri1_b12"):
-        assert _lib.inspect(_golden.load(name)["data"]).kernels == 3
+        assert _lib.inspect(_golden.load(name)["data"]).kernels == 2
