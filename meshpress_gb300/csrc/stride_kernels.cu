@@ -1059,6 +1059,32 @@ __device__ __forceinline__ bool skip_codes(const uint32_t* w, uint32_t rbase, ui
     return ok;
 }
 
+// The same codeword read without a branch, for codewords that fit the
+// 32-bit window (prefix, terminator and value); a longer one sets `longc`
+// and leaves the result undefined.  The walk uses this form so that the
+// compiler can overlap consecutive walk entries (a branch per entry keeps
+// them apart: 5% of the fused kernel on the 2049^2 heightfield).
+template <bool kShared>
+__device__ __forceinline__ bool residual_fast(const uint32_t* w, uint32_t rbase, uint32_t& pos, uint32_t tk,
+                                              uint32_t limit, int32_t& r, bool& longc) {
+    const uint32_t x = peek32<kShared>(w, pos + rbase);
+    const uint32_t z = __clz(x);
+    const uint32_t k = tk & 0x3Fu;
+    const bool eg = (tk & 0x80u) != 0u;
+    const uint32_t nb = (eg ? z : 0u) + k;
+    const uint32_t len = z + 1u + nb;
+    const uint32_t t = __funnelshift_lc(0u, x, z + 1u);
+    const uint32_t val = __funnelshift_rc(t, 0u, 32u - nb);
+    const uint32_t base = eg ? ((1u << (z & 31u)) - 1u) : z;
+    const uint32_t u = (base << k) + val;
+    const uint32_t np = pos + len;
+    longc = longc | (len > 32u);
+    const bool ok = np <= limit;
+    pos = min(np, limit);
+    r = unzigzag(u);
+    return ok;
+}
+
 // Per-lane state of one axis of one meshlet.
 struct VertLane {
     int32_t anc;      // anchor code of the axis
@@ -1104,7 +1130,10 @@ __device__ __forceinline__ uint32_t vert_header(const GroupLane& L, uint32_t d, 
 // vertex; the first one is the anchor) or a parallelogram vertex predicted
 // from three earlier ones.  Four walk entries per iteration (one 16-byte
 // load); entries past the end are masked, not branched around, and root and
-// parallelogram vertices differ only in selects.
+// parallelogram vertices differ only in selects.  The walk reads codewords
+// with the branch-free reader; a lane that met a codeword longer than its
+// window walks its axis again with the general reader (every plane entry
+// the walk reaches is written again, in the same order).
 template <bool kShared, bool kWide>
 __device__ __forceinline__ void vert_axis(const DecodeArgs& a, const GroupLane& L, uint32_t d,
                                           const uint32_t* __restrict__ w, uint32_t rbase,
@@ -1126,6 +1155,7 @@ __device__ __forceinline__ void vert_axis(const DecodeArgs& a, const GroupLane& 
     uint32_t cdd = S.cdd, cp = S.cp;
     int32_t prev = 0;
     bool fail = false;
+    bool longc = false, fast = true;
     auto step = [&](uint32_t e, bool valid, bool anchor) {
         e = valid ? e : 0u;  // a masked entry reads plane[0] and commits nothing
         const uint32_t v = e & 0xFFu;
@@ -1137,7 +1167,8 @@ __device__ __forceinline__ void vert_axis(const DecodeArgs& a, const GroupLane& 
         const int32_t pred = para ? (n0 * ca + n1 * cb + n2 * cc + half) >> K : prev;
         uint32_t p = para ? cp : cdd;
         int32_t r;
-        const bool okr = residual<kShared>(w, rbase, p, para ? tp : td, end, r);
+        const bool okr = fast ? residual_fast<kShared>(w, rbase, p, para ? tp : td, end, r, longc)
+                              : residual<kShared>(w, rbase, p, para ? tp : td, end, r);
         const bool commit = valid & !anchor;  // the anchor has no residual
         cp = (commit & para) ? p : cp;
         cdd = (commit & !para) ? p : cdd;
@@ -1150,16 +1181,32 @@ __device__ __forceinline__ void vert_axis(const DecodeArgs& a, const GroupLane& 
     // walk entries (v | a << 8 | b << 16 | c << 24), 16-byte aligned per meshlet
     const uint4* wq = reinterpret_cast<const uint4*>(a.walk_scratch + L.wp_base);
     // two quads in flight: the walk is read from L2
-    uint4 qn = n_walk ? __ldcg(wq) : make_uint4(0u, 0u, 0u, 0u);
-    uint4 qm = n_walk > 4u ? __ldcg(wq + 1) : qn;
-    for (uint32_t i = 0; i < n_walk; i += 4u) {
-        const uint4 q = qn;
-        qn = qm;
-        if (i + 8u < n_walk) qm = __ldcg(wq + (i >> 2) + 2u);
-        step(q.x, true, i == 0u);
-        step(q.y, i + 1u < n_walk, false);
-        step(q.z, i + 2u < n_walk, false);
-        step(q.w, i + 3u < n_walk, false);
+    {
+        uint4 qn = n_walk ? __ldcg(wq) : make_uint4(0u, 0u, 0u, 0u);
+        uint4 qm = n_walk > 4u ? __ldcg(wq + 1) : qn;
+        for (uint32_t i = 0; i < n_walk; i += 4u) {
+            const uint4 q = qn;
+            qn = qm;
+            if (i + 8u < n_walk) qm = __ldcg(wq + (i >> 2) + 2u);
+            step(q.x, true, i == 0u);
+            step(q.y, i + 1u < n_walk, false);
+            step(q.z, i + 2u < n_walk, false);
+            step(q.w, i + 3u < n_walk, false);
+        }
+    }
+    if (longc) {  // rare: the lane's axis again, from its substream starts
+        fast = false;
+        cdd = S.cdd;
+        cp = S.cp;
+        prev = 0;
+        fail = false;
+        for (uint32_t i = 0; i < n_walk; i += 4u) {
+            const uint4 q = __ldcg(wq + (i >> 2));
+            step(q.x, true, i == 0u);
+            step(q.y, i + 1u < n_walk, false);
+            step(q.z, i + 2u < n_walk, false);
+            step(q.w, i + 3u < n_walk, false);
+        }
     }
     S.cp = cp;
     S.bad = S.bad || fail;
@@ -1383,7 +1430,7 @@ __device__ __forceinline__ bool vert_group(const DecodeArgs& a, uint32_t g, uint
 
 // A CTA decodes one group of 32 meshlets with three warps, warp d = axis d.
 template <bool kWide>
-__global__ void __launch_bounds__(96, 1) vert_kernel(DecodeArgs a, uint32_t stage_bytes, uint32_t code_bytes,
+__global__ void __launch_bounds__(96, 5) vert_kernel(DecodeArgs a, uint32_t stage_bytes, uint32_t code_bytes,
                                                   int persistent) {
     extern __shared__ __align__(128) uint8_t smem[];
     __shared__ uint32_t s_group;
