@@ -1,9 +1,10 @@
-"""ctypes binding of the C oracle (``stride_oracle.c``).
+"""ctypes binding of the C oracles (``stride_oracle.c``, ``pldt5_oracle.c``).
 
-TEST INFRASTRUCTURE ONLY.  The C file restates the reference CPU decoder
-``decode_dup`` (encoder/paradelta_v5_dup.py:471-618); this module builds it
-with gcc (no FMA contraction, so the float64 dequantisation rounds exactly
-like numpy) and exposes it as numpy functions.
+TEST INFRASTRUCTURE ONLY.  The C files restate the reference CPU decoders
+``decode_dup`` (STRIDE DPR4 v3, encoder/paradelta_v5_dup.py:471-618) and
+``decode_paradelta_v5`` (PLDT v5, encoder/paradelta_v5.py:286-462); this
+module builds them with gcc (no FMA contraction, so the float64 arithmetic
+rounds exactly like numpy) and exposes them as numpy functions.
 """
 from __future__ import annotations
 
@@ -16,6 +17,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "stride_oracle.c")
+SOURCES = [SRC, os.path.join(HERE, "pldt5_oracle.c")]
+HEADERS = [os.path.join(HERE, "so_bits.h")]
 LIB = os.path.join(HERE, "libstride_oracle.so")
 
 _lib = None
@@ -28,10 +31,11 @@ class OracleError(RuntimeError):
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with gcc (-O2, no FMA contraction)."""
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+    """Compile the oracles with gcc (-O2, no FMA contraction)."""
+    stale = not os.path.exists(LIB) or any(os.path.getmtime(LIB) < os.path.getmtime(f) for f in SOURCES + HEADERS)
+    if force or stale:
         cmd = ["gcc", "-O2", "-std=gnu11", "-ffp-contract=off", "-fno-fast-math",
-               "-fPIC", "-shared", "-pthread", SRC, "-o", LIB + ".tmp", "-lm"]
+               "-fPIC", "-shared", "-pthread", *SOURCES, "-o", LIB + ".tmp", "-lm"]
         subprocess.run(cmd, check=True)
         os.replace(LIB + ".tmp", LIB)
     return LIB
@@ -52,6 +56,17 @@ class _Header(ctypes.Structure):
                 ("n_meshlets", ctypes.c_uint32), ("body_bit", ctypes.c_uint64)]
 
 
+class _P5Header(ctypes.Structure):
+    _fields_ = [("magic", ctypes.c_uint32), ("version", ctypes.c_uint32),
+                ("code_width", ctypes.c_uint32),
+                ("center", ctypes.c_float * 3), ("scale", ctypes.c_float),
+                ("per_coord_err", ctypes.c_float), ("g_min", ctypes.c_float * 3),
+                ("g_range", ctypes.c_float * 3), ("g_bits", ctypes.c_uint32 * 3),
+                ("n_v", ctypes.c_uint32), ("n_t", ctypes.c_uint32),
+                ("n_boundary", ctypes.c_uint32), ("n_meshlets", ctypes.c_uint32),
+                ("lin3_w", ctypes.c_float * 3), ("boundary_bit", ctypes.c_uint64)]
+
+
 def _load():
     global _lib
     if _lib is None:
@@ -70,6 +85,9 @@ def _load():
         lib.so_bitcodec_read.argtypes = [u8p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p,
                                          ctypes.c_int32, ctypes.c_void_p]
         lib.so_side_table.argtypes = [u8p, ctypes.c_uint64] + [ctypes.c_void_p] * 7
+        lib.p5_parse_header.argtypes = [u8p, ctypes.c_uint64, ctypes.POINTER(_P5Header)]
+        lib.p5_decode.argtypes = [u8p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                  ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
         _lib = lib
     return _lib
 
@@ -182,3 +200,28 @@ def side_table(data: bytes):
                                             ("start_bit", "n_local", "n_tris", "n_strips", "resid_bit",
                                              "n_kind0", "sub_offs")]))
     return out
+
+
+# ---------------------------------------------------------------- PLDT v5 --
+def parse_header_v5(data: bytes) -> _P5Header:
+    """Global header of a PLDT v5 stream (encoder/paradelta_v5.py:290-306)."""
+    lib = _load()
+    arr, p = _buf(data)
+    h = _P5Header()
+    _check(lib.p5_parse_header(p, len(arr), ctypes.byref(h)))
+    return h
+
+
+def decode_v5(data: bytes):
+    """Decode a PLDT v5 stream like ``decode_paradelta_v5``: returns
+    (positions float32 (n_v, 3), triangles int64 (n_t, 3)); the rows are the
+    boundary vertices, then every meshlet's interior vertices."""
+    lib = _load()
+    arr, p = _buf(data)
+    nv, nt = ctypes.c_uint64(), ctypes.c_uint64()
+    _check(lib.p5_decode(p, len(arr), None, None, 0, 0, ctypes.byref(nv), ctypes.byref(nt)))
+    pos = np.empty((nv.value, 3), np.float32)
+    idx = np.empty((nt.value, 3), np.int64)
+    _check(lib.p5_decode(p, len(arr), pos.ctypes.data, idx.ctypes.data, nv.value, nt.value,
+                         ctypes.byref(nv), ctypes.byref(nt)))
+    return pos, idx

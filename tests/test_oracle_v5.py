@@ -1,0 +1,52 @@
+"""PLDT v5 oracle (oracle/pldt5_oracle.c) against golden vectors produced by
+the reference itself (tests/golden/make_golden_v5.py: the reference encoder
+``encode_from_prepared_v5`` and decoder ``decode_paradelta_v5``,
+encoder/paradelta_v5.py:144-462)."""
+import glob
+import json
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from tests import _golden
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+V5_CASES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "golden", "v5_*.npz")))
+
+
+def _load(name):
+    z = np.load(os.path.join(HERE, "golden", name + ".npz"))
+    return z["blob"].tobytes(), z["pos"], z["idx"], json.loads(str(z["meta"]))
+
+
+def test_fixtures_present():
+    assert len(V5_CASES) >= 8
+
+
+@pytest.mark.parametrize("name", V5_CASES)
+def test_oracle_matches_reference_decoder(name):
+    data, pos, idx, meta = _load(name)
+    opos, oidx = oracle.decode_v5(data)
+    assert opos.shape == pos.shape and oidx.shape == idx.shape
+    assert np.array_equal(opos.view(np.uint32), pos.view(np.uint32))  # bit-exact float32
+    assert np.array_equal(oidx, idx)
+    h = oracle.parse_header_v5(data)
+    assert h.n_meshlets == meta["n_meshlets"] and h.n_boundary == meta["n_boundary"]
+    assert list(h.g_bits) == meta["g_bits"]
+    # rows: the boundary vertices, then every meshlet's interior vertices
+    assert len(opos) == meta["n_src_v"] and len(oidx) == meta["n_src_t"]
+
+
+def test_rejects_other_formats_and_truncation():
+    data, _, _, _ = _load("v5_grid33_b12")
+    with pytest.raises(oracle.OracleError):
+        oracle.decode_v5(_golden.load("grid33_b12")["data"])  # a DPR4 stream: bad magic
+    bad = bytearray(data)
+    bad[4] = 4  # version 4
+    with pytest.raises(oracle.OracleError):
+        oracle.decode_v5(bytes(bad))
+    for cut in (3, 40, len(data) // 2, len(data) - 2):
+        with pytest.raises(oracle.OracleError):
+            oracle.decode_v5(data[:cut])
