@@ -291,6 +291,43 @@ int stride_server_stats(stride_server* s, uint64_t* launches, uint64_t* complete
                         uint64_t* arena_peak_bytes);
 void stride_server_destroy(stride_server* s);
 
+/* ---- PLDT v5 streams ------------------------------------------------------
+ * The format the reference's CuPy decoder reads (magic 0x504C4454, version
+ * 5: a global boundary table, per-meshlet boundary references, strip
+ * connectivity, a float64 lin3 predictor).  Decoded bit-exactly like the
+ * reference CPU decoder decode_paradelta_v5 (encoder/paradelta_v5.py:286-462);
+ * rows are the boundary vertices, then every meshlet's interior vertices.
+ * Stricter than that decoder on invalid streams: boundary references must
+ * be rows of the boundary table, the strips must yield the header's triangle
+ * count, and meshlets must lie back to back as the offset table says. */
+typedef struct pldt5_handle pldt5_handle;
+
+typedef struct {
+    uint32_t n_meshlets;
+    uint32_t n_boundary;
+    uint32_t g_bits[3];
+    uint64_t n_v;        /* decoded rows: boundary + interior vertices        */
+    uint64_t n_t;
+    uint64_t nbytes;
+    float center[3];
+    float scale;
+    float lin3_w[3];
+} pldt5_info_t;
+
+/* Host parse of the header, the boundary table and the meshlet headers, then
+ * a device copy.  Replaces parse_globals_v5 + ParaDeltaV5GpuDecoder.__init__
+ * (utils/paradelta_v5_cuda.py:515-684). */
+int pldt5_open(const uint8_t* data, size_t len, pldt5_handle** out);
+int pldt5_info(const pldt5_handle* h, pldt5_info_t* info);
+/* Enqueue the decode on `stream`: triangles (n_t x 3 uint32, global rows)
+ * and world-space positions (n_v x 3 float32) into device buffers.
+ * Replaces ParaDeltaV5GpuDecoder.decode (:686-712) plus the world transform
+ * of decode_to_host (:714-717). */
+int pldt5_decode(pldt5_handle* h, void* stream, uint32_t* d_idx, float* d_pos);
+/* Like stride_status (wait != 0 blocks until the decode ends). */
+int pldt5_status(pldt5_handle* h, int wait);
+void pldt5_close(pldt5_handle* h);
+
 #ifdef __cplusplus
 }
 #endif

@@ -78,6 +78,15 @@ _I = ctypes.c_int
 _U32 = ctypes.c_uint32
 _U64 = ctypes.c_uint64
 _SZ = ctypes.c_size_t
+
+
+class Pldt5Info(ctypes.Structure):
+    _fields_ = [("n_meshlets", ctypes.c_uint32), ("n_boundary", ctypes.c_uint32),
+                ("g_bits", ctypes.c_uint32 * 3), ("n_v", ctypes.c_uint64), ("n_t", ctypes.c_uint64),
+                ("nbytes", ctypes.c_uint64), ("center", ctypes.c_float * 3), ("scale", ctypes.c_float),
+                ("lin3_w", ctypes.c_float * 3)]
+
+
 SIGNATURES = [
     ("stride_last_error_message", ctypes.c_char_p, []),
     ("stride_error_string", ctypes.c_char_p, [_I]),
@@ -119,6 +128,11 @@ SIGNATURES = [
     ("stride_server_hold", _I, [_P, _I]),
     ("stride_server_stats", _I, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
     ("stride_server_destroy", None, [_P]),
+    ("pldt5_open", _I, [_P, _SZ, ctypes.POINTER(_P)]),
+    ("pldt5_info", _I, [_P, ctypes.POINTER(Pldt5Info)]),
+    ("pldt5_decode", _I, [_P, _P, _P, _P]),
+    ("pldt5_status", _I, [_P, _I]),
+    ("pldt5_close", None, [_P]),
 ]
 
 _lib = None

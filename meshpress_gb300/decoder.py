@@ -4,7 +4,9 @@ Reference: utils/paradelta_v5_cuda.py:580-718.  Same class name, constructor
 (``data``, ``meshlets_per_block`` in [1, 16]) and ``decode()`` /
 ``decode_to_host()`` methods, plus ``decode_to_device()``.  The input is the
 DPR4 v3 bitstream that ``STRIDEEncoder`` writes
-(encoder/paradelta_v5_dup.py:316-464); a PLDT (v4/v5) stream is rejected
+(encoder/paradelta_v5_dup.py:316-464), or a PLDT v5 stream (the reference
+class's own format), for which the constructor returns a
+``pldt5.PldtV5Decoder``; any other stream (PLDT v4 included) is rejected
 with ``ValueError`` like any other bad magic (utils/paradelta_v5_cuda.py:520).
 
 Everything runs in ``libstride_gb300.so`` through its C ABI; PyTorch only
@@ -39,6 +41,12 @@ class ParaDeltaV5GpuDecoder:
     ``n_t_total``, ``meshlets_per_block`` (accepted for compatibility; the
     reference kernel ignores it too, utils/paradelta_v5_cuda.py:259-260).
     """
+
+    def __new__(cls, data: bytes = b"", meshlets_per_block: int = 1):
+        from .pldt5 import PldtV5Decoder, is_pldt5
+        if cls is ParaDeltaV5GpuDecoder and is_pldt5(data):
+            return PldtV5Decoder(data, meshlets_per_block)  # __init__ below is not run for it
+        return super().__new__(cls)
 
     def __init__(self, data: bytes, meshlets_per_block: int = 1):
         if meshlets_per_block < 1 or meshlets_per_block > 16:

@@ -17,7 +17,7 @@ REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def declared_functions():
     text = open(os.path.join(REPO, "include", "stride_gb300.h")).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"^[A-Za-z_][\w \*]*?\b(stride_\w+)\s*\(", text, flags=re.M)))
+    return sorted(set(re.findall(r"^[A-Za-z_][\w \*]*?\b((?:stride|pldt5)_\w+)\s*\(", text, flags=re.M)))
 
 
 def test_library_builds_and_exports_every_declared_symbol(built_libs):
