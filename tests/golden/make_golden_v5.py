@@ -88,6 +88,10 @@ def main():
     V, T = synth.torus(24, 12)
     case(ref, "torus_b10", V, T, precision_error=synth.bbox_bits_error(10), precision_mode="bbox_frac",
          max_verts=48, max_tris=64)
+    V, T = synth.noise_heightfield(129, seed=11)
+    case(ref, "noise129_mv128", V, T, precision_error=b12, precision_mode="bbox_frac", max_verts=128, max_tris=128)
+    V, T = synth.icosphere(5, seed=6)
+    case(ref, "ico5_b14", V, T, precision_error=synth.bbox_bits_error(14), precision_mode="bbox_frac")
     V = np.array([[0.0, 0.0, 0.0], [1.0, 0.0, 0.0], [0.0, 1.0, 0.5]])
     T = np.array([[0, 1, 2]])
     case(ref, "tri1_b12", V, T, precision_error=b12, precision_mode="bbox_frac")
