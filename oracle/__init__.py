@@ -6,4 +6,5 @@ Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
 (``meshpress_gb300``) never imports it.
 """
 from .oracle import (OracleError, bitcodec_read, decode, decode_mt,  # noqa: F401
-                     decode_v5, parse_header, parse_header_v5, build, library_path, side_table)
+                     decode_v5, parse_header, parse_header_v5, build, library_path, side_table,
+                     tables_v5)

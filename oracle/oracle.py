@@ -88,6 +88,7 @@ def _load():
         lib.p5_parse_header.argtypes = [u8p, ctypes.c_uint64, ctypes.POINTER(_P5Header)]
         lib.p5_decode.argtypes = [u8p, ctypes.c_uint64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
                                   ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64)]
+        lib.p5_tables.argtypes = [u8p, ctypes.c_uint64] + [ctypes.c_void_p] * 6
         _lib = lib
     return _lib
 
@@ -225,3 +226,19 @@ def decode_v5(data: bytes):
     _check(lib.p5_decode(p, len(arr), pos.ctypes.data, idx.ctypes.data, nv.value, nt.value,
                          ctypes.byref(nv), ctypes.byref(nt)))
     return pos, idx
+
+
+def tables_v5(data: bytes):
+    """Per-meshlet tables of a PLDT v5 stream as the reference GPU decoder
+    derives them (utils/paradelta_v5_cuda.py:515-660): absolute start bits,
+    n_bnd, n_int, n_tris, n_strips (int32) and the float64 boundary rows."""
+    lib = _load()
+    arr, p = _buf(data)
+    h = parse_header_v5(data)
+    M, nb = h.n_meshlets, h.n_boundary
+    out = {"off_bits": np.zeros(M, np.uint64), "n_bnd": np.zeros(M, np.int32), "n_int": np.zeros(M, np.int32),
+           "n_tris": np.zeros(M, np.int32), "n_strips": np.zeros(M, np.int32),
+           "bnd_rows": np.zeros((nb, 3), np.float64)}
+    _check(lib.p5_tables(p, len(arr), *[out[k].ctypes.data for k in
+                                        ("off_bits", "n_bnd", "n_int", "n_tris", "n_strips", "bnd_rows")]))
+    return out

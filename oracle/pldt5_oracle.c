@@ -372,3 +372,51 @@ fail:
     free(o.t);
     return rc;
 }
+
+/* Per-meshlet tables of a PLDT v5 stream, as the reference GPU decoder
+ * derives them (parse_globals_v5 and its sizes kernel,
+ * utils/paradelta_v5_cuda.py:515-660): each meshlet's absolute start bit
+ * from the offset table and its four header fields, and the boundary rows
+ * in float64 (g_min + code / mx * g_range).  Any output may be NULL. */
+int p5_tables(const uint8_t* data, uint64_t len, uint64_t* off_bits, int32_t* n_bnd, int32_t* n_int,
+              int32_t* n_tris, int32_t* n_strips, double* bnd_rows) {
+    so_br r = {data, len * 8ull, 0, 0};
+    p5_header h;
+    int rc = p5_header_read(&r, &h);
+    if (rc) return rc;
+    const uint64_t nb = h.n_boundary;
+    int64_t* bc = (int64_t*)calloc((size_t)(nb ? nb : 1) * 3, sizeof(int64_t));
+    if (!bc) return SO_ERR_NOMEM;
+    for (int d = 0; d < 3 && nb > 0; d++) {
+        bc[d] = (int64_t)br_read(&r, (int)h.g_bits[d]);
+        if (nb > 1) {
+            const int k = (int)br_read(&r, 8);
+            for (uint64_t i = 1; i < nb && !r.err; i++) bc[3 * i + d] = bc[3 * (i - 1) + d] + unzigzag(br_rice(&r, k));
+        }
+    }
+    if (r.err) { free(bc); return r.err; }
+    if (bnd_rows) {
+        for (uint64_t i = 0; i < nb; i++)
+            for (int d = 0; d < 3; d++) {
+                const uint64_t mx = (1ull << h.g_bits[d]) - 1ull;
+                bnd_rows[3 * i + d] = mx == 0 ? (double)h.g_min[d]
+                                              : (double)h.g_min[d] + ((double)bc[3 * i + d] / (double)mx) * (double)h.g_range[d];
+            }
+    }
+    free(bc);
+    r.pos += (uint64_t)((-(int64_t)r.pos) & 7);
+    for (uint32_t m = 0; m < h.n_meshlets; m++) {
+        const uint64_t o = br_read(&r, 32);
+        if (r.err) return r.err;
+        so_br q = {data, len * 8ull, o, 0};
+        const int32_t b = (int32_t)br_read(&q, 16), i = (int32_t)br_read(&q, 16);
+        const int32_t t = (int32_t)br_read(&q, 16), s = (int32_t)br_read(&q, 16);
+        if (q.err) return q.err;
+        if (off_bits) off_bits[m] = o;
+        if (n_bnd) n_bnd[m] = b;
+        if (n_int) n_int[m] = i;
+        if (n_tris) n_tris[m] = t;
+        if (n_strips) n_strips[m] = s;
+    }
+    return SO_OK;
+}

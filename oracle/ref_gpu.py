@@ -94,6 +94,43 @@ def dprb_blob(data: bytes) -> bytes:
     return b"".join(parts)
 
 
+def sblb_blob(data: bytes, meshlets_per_block: int = 1) -> bytes:
+    """A PLDT v5 stream as the reference PLDT v5 GPU harness's input file
+    (SBLB v1: a 64-byte little-endian header, the stream, the per-meshlet
+    tables, the float32 boundary rows; layout of scripts/dump_stride_blob.py:
+    7-31 and 82-108, read by bench_cpp/stride_decode_bench.cu).  The
+    reference takes the tables from its CuPy decoder
+    (utils/paradelta_v5_cuda.py:515-684); here they come from the bytes
+    (tables_v5), with the same per-warp shared-memory size (:662-678)."""
+    import struct
+
+    from . import oracle as orc
+    h = orc.parse_header_v5(data)
+    t = orc.tables_v5(data)
+    M, nb = int(h.n_meshlets), int(h.n_boundary)
+    n_bnd, n_int, n_tris, n_strips = t["n_bnd"], t["n_int"], t["n_tris"], t["n_strips"]
+    tris_off = np.concatenate([[0], np.cumsum(n_tris, dtype=np.int64)]).astype(np.int32)
+    int_cur = np.concatenate([[0], np.cumsum(n_int[:-1], dtype=np.int64)]).astype(np.int32)[:M]
+    n_v_total = nb + int(n_int.sum())
+    n_t_total = int(tris_off[-1])
+    # parse_globals_v5 keeps the float64 boundary expression as float32 (:553-562)
+    bnd_pos = t["bnd_rows"].astype(np.float32)
+    code_bytes = 4 if h.code_width else 2
+    mx = (lambda a: int(a.max()) if len(a) else 0)  # noqa: E731
+    shared = (mx(n_bnd + n_int) * 16 + mx(n_bnd) * 4 + 32 + mx(n_int) * 3 * code_bytes + mx(n_int) * 8
+              + mx(n_tris) * 3)
+    per_warp = (shared + 15) & ~15
+    delta = float(np.float32(2.0 * float(h.per_coord_err)))
+    head = struct.pack("<IIIIIIIIffffIIII", 0x424C4253, 1, int(h.code_width), M, nb, n_v_total, n_t_total,
+                       len(data), float(h.lin3_w[0]), float(h.lin3_w[1]), float(h.lin3_w[2]), delta, per_warp,
+                       int(meshlets_per_block), 0, 0)
+    assert len(head) == 64
+    parts = [head, bytes(data), t["off_bits"].astype("<u8").tobytes(), n_bnd.astype("<i4").tobytes(),
+             n_int.astype("<i4").tobytes(), n_tris.astype("<i4").tobytes(), n_strips.astype("<i4").tobytes(),
+             tris_off.astype("<i4").tobytes(), int_cur.astype("<i4").tobytes(), bnd_pos.astype("<f4").tobytes()]
+    return b"".join(parts)
+
+
 _cuda = None
 
 

@@ -50,3 +50,36 @@ def test_rejects_other_formats_and_truncation():
     for cut in (3, 40, len(data) // 2, len(data) - 2):
         with pytest.raises(oracle.OracleError):
             oracle.decode_v5(data[:cut])
+
+
+def test_sblb_blob_layout():
+    """The reference PLDT v5 harness's input file written from the bytes
+    (oracle.ref_gpu.sblb_blob; layout of scripts/dump_stride_blob.py)."""
+    import struct
+
+    from oracle import ref_gpu
+    data, pos, idx, meta = _load("v5_noise129_mv128")
+    blob = ref_gpu.sblb_blob(data)
+    f = struct.unpack("<IIIIIIIIffffIIII", blob[:64])
+    magic, version, code_width, M, nb, n_v, n_t, size = f[:8]
+    assert (magic, version) == (0x424C4253, 1)
+    assert M == meta["n_meshlets"] and nb == meta["n_boundary"]
+    assert n_v == len(pos) and n_t == len(idx) and size == len(data)
+    assert blob[64:64 + size] == data
+    o = 64 + size
+    off = np.frombuffer(blob, "<u8", M, o)
+    o += 8 * M
+    n_bnd, n_int, n_tris, n_strips = (np.frombuffer(blob, "<i4", M, o + 4 * M * i) for i in range(4))
+    o += 16 * M
+    tris_off = np.frombuffer(blob, "<i4", M + 1, o)
+    o += 4 * (M + 1)
+    int_cur = np.frombuffer(blob, "<i4", M, o)
+    o += 4 * M
+    bnd = np.frombuffer(blob, "<f4", 3 * nb, o).reshape(nb, 3)
+    assert o + 12 * nb == len(blob)
+    assert np.all(np.diff(off.astype(np.int64)) > 0) and tris_off[-1] == n_t
+    assert nb + n_int.sum() == n_v and int_cur[-1] + n_int[-1] == n_v - nb
+    # the boundary rows in world space are the decoder's first rows
+    h = oracle.parse_header_v5(data)
+    world = (bnd.astype(np.float64) * np.float32(h.scale) + np.array(h.center, np.float32)).astype(np.float32)
+    assert np.abs(world - pos[:nb]).max() < 1e-5 * max(1.0, float(np.abs(pos).max()))
