@@ -177,8 +177,14 @@ __device__ __forceinline__ int p5_vert(P5Bits& b, P5Fifo& f, int idx_bits, bool&
     return x;
 }
 
-__global__ void __launch_bounds__(128) p5_decode_kernel(P5Args a) {
-    const uint32_t m = blockIdx.x * blockDim.x + threadIdx.x;
+// Lane l < per_warp of warp w decodes meshlet w * per_warp + l: the lanes of
+// a warp take different branches on almost every token, so a stream with
+// few meshlets gets one per warp, spread over the SMs.
+__global__ void __launch_bounds__(128) p5_decode_kernel(P5Args a, uint32_t per_warp) {
+    const uint32_t lane = threadIdx.x & 31u;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (lane >= per_warp) return;
+    const uint32_t m = warp * per_warp + lane;
     if (m >= a.n_meshlets) return;
     const unsigned long long s0 = a.start[m], s1 = a.start[m + 1];
     const bool last = m + 1 == a.n_meshlets;
@@ -589,7 +595,11 @@ int pldt5_decode(pldt5_handle* h, void* stream, uint32_t* d_idx, float* d_pos) {
         a.w2 = h->w[2];
         a.delta = h->delta;
         a.status = h->d_status;
-        p5_decode_kernel<<<static_cast<uint32_t>((M + 127) / 128), 128, 0, s>>>(a);
+        // about sixteen busy warps per SM, at most 32 meshlets per warp
+        const uint64_t target = 16ull * static_cast<uint64_t>(device_sm_count());
+        const uint32_t per_warp = static_cast<uint32_t>(std::min<uint64_t>(32, std::max<uint64_t>(1, (M + target - 1) / target)));
+        const uint64_t warps = (M + per_warp - 1) / per_warp;
+        p5_decode_kernel<<<static_cast<uint32_t>((warps + 3) / 4), 128, 0, s>>>(a, per_warp);
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "p5_decode_kernel");
     }
     if (rows) {
