@@ -10,11 +10,11 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def names():
-    """The STRIDE (DPR4 v3) fixtures (the PLDT v5 ones are named v5_*)."""
+    """The STRIDE (DPR4 v3) fixtures (the PLDT v5 ones are named v5_* and v5x_*)."""
     out = []
     for f in sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))):
         b = os.path.basename(f)[:-4]
-        if b.endswith(".l2g") or b == "bitcodec" or b.startswith("v5_"):
+        if b.endswith(".l2g") or b == "bitcodec" or b.startswith(("v5_", "v5x_")):
             continue
         out.append(b)
     return out

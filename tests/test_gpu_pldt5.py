@@ -13,7 +13,8 @@ import oracle
 pytestmark = pytest.mark.gpu
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-V5_CASES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "golden", "v5_*.npz")))
+# encoded meshes (v5_*) and crafted corner cases (v5x_*)
+V5_CASES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "golden", "v5*_*.npz")))
 
 
 @pytest.fixture(scope="module")

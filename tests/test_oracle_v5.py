@@ -13,7 +13,8 @@ import oracle
 from tests import _golden
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-V5_CASES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "golden", "v5_*.npz")))
+# encoded meshes (v5_*) and crafted corner cases (v5x_*)
+V5_CASES = sorted(os.path.basename(p)[:-4] for p in glob.glob(os.path.join(HERE, "golden", "v5*_*.npz")))
 
 
 def _load(name):
@@ -22,7 +23,7 @@ def _load(name):
 
 
 def test_fixtures_present():
-    assert len(V5_CASES) >= 8
+    assert sum(c.startswith("v5_") for c in V5_CASES) >= 10 and sum(c.startswith("v5x_") for c in V5_CASES) >= 4
 
 
 @pytest.mark.parametrize("name", V5_CASES)
@@ -35,8 +36,8 @@ def test_oracle_matches_reference_decoder(name):
     h = oracle.parse_header_v5(data)
     assert h.n_meshlets == meta["n_meshlets"] and h.n_boundary == meta["n_boundary"]
     assert list(h.g_bits) == meta["g_bits"]
-    # rows: the boundary vertices, then every meshlet's interior vertices
-    assert len(opos) == meta["n_src_v"] and len(oidx) == meta["n_src_t"]
+    if meta["kind"] == "pldt_v5":  # rows: the boundary vertices, then every meshlet's interior vertices
+        assert len(opos) == meta["n_src_v"] and len(oidx) == meta["n_src_t"]
 
 
 def test_rejects_other_formats_and_truncation():
