@@ -11,8 +11,8 @@ sub-offsets, written by the reference's scripts/dump_stride_dup_blob.py
 from encoder metadata).
 
 build() compiles that kernel, unmodified, from the reference source into a
-cubin (oracle/_ref/, git-ignored; it travels with the tree to the GPU
-machine, where the reference sources do not exist).  RefKernel loads the
+cubin (oracle/_ref/, git-ignored; it travels with the tree to machines
+without the reference sources).  RefKernel loads the
 cubin with the CUDA driver API, derives the side table from the DPR4 bytes
 with the C oracle (so_side_table), and launches the kernel the way the
 reference harness does (stride_dup_decode_bench.cu:662-685): a persistent
@@ -37,7 +37,7 @@ REF_SRC = "/root/reference/bench_cpp/stride_dup_decode_bench.cu"
 
 def build(force: bool = False) -> bool:
     """Compile the reference kernel to a sm_103a cubin when the reference
-    tree is present (the build machine only); True when a cubin exists."""
+    tree is present; True when a cubin exists."""
     if os.path.exists(REF_SRC) and (force or not os.path.exists(CUBIN) or not os.path.exists(ENTRY)
                                     or os.path.getmtime(CUBIN) < os.path.getmtime(REF_SRC)):
         os.makedirs(REF_DIR, exist_ok=True)
