@@ -27,7 +27,7 @@ CUDA_SOURCES = ["stride_kernels.cu", "stride_api.cu", "stride_batch.cu", "stride
                 "pldt5.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3",
               "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off",
-              "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]
+              "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills", "-Xptxas", "-dlcm=cg"]
 
 
 def _nvcc() -> str:

@@ -55,7 +55,8 @@ __device__ __forceinline__ void p5_report(Status* st, int code, uint32_t m) {
     atomicCAS(&st->err, 0ull, v);
 }
 
-// MSB-first reads from global memory; a read never passes `limit`.
+// MSB-first reads from global memory (through L2, as every global read of
+// the library); a read never passes `limit`.
 struct P5Bits {
     const uint8_t* buf;
     unsigned long long pos, limit;
@@ -65,7 +66,7 @@ struct P5Bits {
         const unsigned long long b = pos >> 3;
         unsigned long long v = 0ull;
 #pragma unroll
-        for (int i = 0; i < 8; i++) v = (v << 8) | __ldg(buf + b + i);
+        for (int i = 0; i < 8; i++) v = (v << 8) | __ldcg(buf + b + i);
         return v << (pos & 7ull);
     }
     __device__ __forceinline__ uint32_t bits(int n) {  // n <= 32

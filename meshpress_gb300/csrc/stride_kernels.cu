@@ -1253,15 +1253,12 @@ __device__ void emit_axis(const DecodeArgs& a, const GroupLane& L, uint32_t rmas
         }
         const PlaneT<kWide>* pj = reinterpret_cast<const PlaneT<kWide>*>(planes + off);
         float* dst = a.pos + 3ull * vb + d;
-        // Every table read of the meshlet (<= 256 vertices) in flight at once,
-        // cached in L1: a meshlet's codes of one axis span a narrow range, so
-        // its reads share a few lines (5% off the vertex kernel on the batch).
-        if (has_lut) {
+        if (has_lut) {  // every table read of the meshlet (<= 256 vertices) in flight at once
             float y[kMaxLocal / 32];
 #pragma unroll
             for (uint32_t k = 0; k < kMaxLocal / 32u; k++) {
                 const uint32_t v = lane + 32u * k;
-                y[k] = v < nv ? __ldca(lut + min(static_cast<uint32_t>(pj[v]), qmax)) : 0.f;
+                y[k] = v < nv ? __ldcg(lut + min(static_cast<uint32_t>(pj[v]), qmax)) : 0.f;
             }
 #pragma unroll
             for (uint32_t k = 0; k < kMaxLocal / 32u; k++) {
