@@ -79,3 +79,17 @@ def test_kernel_count(built_libs):
     connectivity + vertex kernel."""
     for name in ("grid129_b12", "grid9_b12", "grid17_canon_b16", "tri1_b12"):
         assert _lib.inspect(_golden.load(name)["data"]).kernels == 2
+
+
+def test_global_reads_through_l2_only():
+    """The serving engine rewrites arena ranges (streams, mesh tables,
+    dequantisation tables) for a new launch while launches on other streams
+    still run on the same SMs, so the library is built with every plain
+    global load cached in L2 only, and its kernels read no global data
+    through L1 or the read-only cache."""
+    assert "-dlcm=cg" in _build.NVCC_FLAGS
+    for name in os.listdir(_build.CSRC):
+        if name.endswith((".cu", ".cuh")):
+            src = open(os.path.join(_build.CSRC, name)).read()
+            for op in ("__ldg(", "__ldca(", "ld.global.ca", "ld.global.nc"):
+                assert op not in src, f"{name} reads global memory with {op}"
