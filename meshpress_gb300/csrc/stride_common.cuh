@@ -152,10 +152,11 @@ inline unsigned long long walk_scratch_words(unsigned long long n_v, unsigned lo
 // Host-side header parse + kernel parameters; returns 0 or a STRIDE_ERR_*.
 int parse_header(const uint8_t* data, size_t len, MeshParams* p, char* why, size_t why_len);
 
-// Enqueue scan + connectivity + vertex kernels for `a` on `stream`.  When
-// `ev` is non-null, its non-null entries of four are recorded: before the
-// scan kernel, after it, after the connectivity kernel and after the vertex
-// kernel.
+// Enqueue the scan kernel and then the fused kernel (cfg.persistent == 2) or
+// the connectivity and vertex kernels for `a` on `stream`.  When `ev` is
+// non-null, its non-null entries of four are recorded: before the scan
+// kernel, after it, after the connectivity (or fused) kernel and after the
+// vertex kernel (right after the fused one).
 int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void* const* ev = nullptr);
 
 // Meshlet-native outputs of a finished decode: each meshlet's first vertex

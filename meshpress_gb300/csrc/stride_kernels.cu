@@ -1,32 +1,35 @@
 // STRIDE (DPR4 v3) decode kernels for sm_103a.
 //
-// Three launches per decode (a memset of the status word comes first):
+// A decode is a memset of the status word, then:
 //
-//  1. scan_kernel -- one thread per meshlet: offset table entry + 48-bit
-//     meshlet header (n_local, n_tris, n_strips), range checks, and a
-//     device-wide exclusive scan of n_local / n_tris (output placement) and
-//     of n_local rounded up to four (walk scratch placement): block scans
-//     plus a last-block scan of the block sums.
+//  1. scan_kernel -- one thread per meshlet: offset table entry and 48-bit
+//     meshlet header (n_local, n_tris, n_strips), range checks, exclusive
+//     scans of n_local / n_tris (output placement) and of n_local rounded up
+//     to four (walk scratch placement), and a per-256-meshlet rank by token
+//     count (groups of 32 similar meshlets).  Extra blocks of the same launch
+//     fill per-code dequantisation tables.
 //
-//  2. conn_kernel -- a warp owns 32 consecutive meshlets, one per lane.  One
-//     bulk copy (cp.async.bulk + mbarrier) stages the group's bytes in
-//     shared memory; each lane replays its meshlet's strip connectivity
-//     (decode_dup's strip loop, encoder/paradelta_v5_dup.py:513-542) with the
-//     16-entry move-to-tail FIFO (_read_vert, encoder/paradelta_codec.py:
-//     330-340) held in registers, writes the final triangle indices (four
-//     triangles = three aligned 16-byte stores) and the first-occurrence walk
-//     (vertex, kind, IRLP references) to scratch, and records where the
-//     connectivity ends (the anchor).
+//  2. flow_kernel (default) -- one persistent launch for both phases.  A CTA's
+//     two warp pairs decode connectivity groups (32 meshlets, one per lane):
+//     the parser warp streams each lane's meshlet through a per-lane ring
+//     (cp.async) and runs the token chain -- strip headers, token widths, the
+//     16-entry move-to-tail FIFO in registers (_read_vert,
+//     encoder/paradelta_codec.py:330-340) -- and the assembler warp replays
+//     strip state, triangles and first occurrences (decode_dup's strip loop,
+//     encoder/paradelta_v5_dup.py:513-542).  Finished groups go into a
+//     completion list; when no connectivity group is left, the CTA decodes
+//     the vertices of listed groups: the residual bits staged once by bulk
+//     copies, three axis warps skipping to their substreams and
+//     reconstructing integer codes in walk order (IRLP,
+//     encoder/paradelta_v5_dup.py:91-104 and 581-600), then writing exact
+//     positions (stride_dequant.h).
 //
-//  3. vert_kernel -- same warp/lane mapping.  Each lane bulk-copies its
-//     meshlet's residual bits (anchor to end) into shared memory, skips the
-//     three short delta substreams, then reconstructs the integer codes one
-//     axis at a time in walk order (IRLP, encoder/paradelta_v5_dup.py:91-104
-//     and 581-600).  Each pass leaves the parallelogram cursor at the next
-//     axis' substream, so no substream boundary has to be searched for, and
-//     only one axis of codes lives in shared memory at a time: after each
-//     pass the warp writes that coordinate of every vertex (exact
-//     dequantisation, stride_dequant.h).
+//     The same per-group code also runs as two kernels (conn_kernel, then
+//     vert_kernel), the launch shape of host-output decodes and of the
+//     autotuner's other candidates.
+//
+// Every global read goes through L2 only (the serving engine rewrites arena
+// ranges while other launches run; see the bit access helpers below).
 #include <cuda_runtime.h>
 
 #include <algorithm>
