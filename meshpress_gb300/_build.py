@@ -89,7 +89,8 @@ def build_encoder(force: bool = False) -> str:
     if not force and not _stale(ENCODER_LIB, [src]):
         return ENCODER_LIB
     tmp = ENCODER_LIB + ".tmp"
-    subprocess.run(["g++", "-O2", "-std=c++17", "-fPIC", "-shared", src, "-o", tmp], check=True)
+    # no contraction: the PLDT v5 writer replays the decoder's float64 arithmetic
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", src, "-o", tmp], check=True)
     os.replace(tmp, ENCODER_LIB)
     return ENCODER_LIB
 

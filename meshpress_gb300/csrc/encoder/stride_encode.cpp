@@ -352,6 +352,67 @@ inline int64_t irlp(const int64_t* n, int K, int64_t a, int64_t b, int64_t c) {
     return static_cast<int64_t>(s);
 }
 
+// Normalisation and global quantisation (prepare_paradelta_arrays,
+// encoder/paradelta_codec.py:767-786, and _quantize_global, :149-165).
+struct Quant {
+    double center[3] = {0, 0, 0}, scale = 1.0, pce = 0.0, gmin[3], grange[3];
+    uint32_t g_bits[3] = {0, 0, 0};
+    std::vector<int32_t> gcodes;  // n_v x 3
+};
+
+// 0, or -2 with g_err set when an axis needs more than 24 bits.
+int quantize(const double* verts, uint64_t n_v, double precision_error, int precision_mode, Quant& Q) {
+    double* center = Q.center;
+    for (uint64_t i = 0; i < n_v; i++)
+        for (int d = 0; d < 3; d++) center[d] += verts[3 * i + d];
+    for (int d = 0; d < 3; d++) center[d] /= static_cast<double>(n_v);
+    double scale = 0, bmin[3], bmax[3];
+    for (int d = 0; d < 3; d++) { bmin[d] = INFINITY; bmax[d] = -INFINITY; }
+    for (uint64_t i = 0; i < n_v; i++) {
+        double s = 0;
+        for (int d = 0; d < 3; d++) {
+            double x = verts[3 * i + d];
+            bmin[d] = std::min(bmin[d], x);
+            bmax[d] = std::max(bmax[d], x);
+            double c = x - center[d];
+            s += c * c;
+        }
+        scale = std::max(scale, std::sqrt(s));
+    }
+    if (!(scale > 0)) scale = 1.0;
+    Q.scale = scale;
+    if (precision_mode == 0) {
+        Q.pce = precision_error / scale / std::sqrt(3.0);
+    } else {
+        double ext = std::max(bmax[0] - bmin[0], std::max(bmax[1] - bmin[1], bmax[2] - bmin[2]));
+        Q.pce = (precision_error * ext) / (2.0 * scale);
+    }
+    Q.gcodes.assign(3 * n_v, 0);
+    for (int d = 0; d < 3; d++) {
+        double lo = INFINITY, hi = -INFINITY;
+        for (uint64_t i = 0; i < n_v; i++) {
+            double x = (verts[3 * i + d] - center[d]) / scale;
+            lo = std::min(lo, x);
+            hi = std::max(hi, x);
+        }
+        Q.gmin[d] = lo;
+        Q.grange[d] = hi - lo;
+        double step = 2.0 * Q.pce;
+        if (!(Q.grange[d] > 0)) { Q.g_bits[d] = 1; continue; }
+        int nb = std::max(1, static_cast<int>(std::ceil(std::log2(Q.grange[d] / step + 1.0))));
+        if (nb > 24) { g_err = "precision needs more than 24 bits per axis"; return -2; }
+        Q.g_bits[d] = static_cast<uint32_t>(nb);
+        double mx = static_cast<double>((1u << nb) - 1u);
+        for (uint64_t i = 0; i < n_v; i++) {
+            double x = ((verts[3 * i + d] - center[d]) / scale - Q.gmin[d]) / Q.grange[d] * mx;
+            double q = std::nearbyint(x);  // round half to even, like np.round
+            q = std::min(std::max(q, 0.0), mx);
+            Q.gcodes[3 * i + d] = static_cast<int32_t>(q);
+        }
+    }
+    return 0;
+}
+
 struct Result {
     std::vector<uint8_t> data;
     std::vector<uint32_t> l2g;
@@ -361,6 +422,30 @@ struct Result {
     int32_t pred_n[9];
     uint32_t pred_k[3];
 };
+
+// A PLDT v5 encode: the stream and, per decoded row, its source vertex.
+struct Result5 {
+    std::vector<uint8_t> data;
+    std::vector<uint32_t> rows;
+    uint32_t n_meshlets = 0, n_boundary = 0;
+};
+
+int best_rice_k(const std::vector<uint64_t>& u, int kmax) {
+    uint64_t best = ~0ull;
+    int k = 0;
+    for (int kk = 0; kk <= kmax; kk++) {
+        const uint64_t b = rice_bits(u, kk);
+        if (b < best) { best = b; k = kk; }
+    }
+    return k;
+}
+
+inline uint32_t f32bits(double x) {
+    const float f = static_cast<float>(x);
+    uint32_t b;
+    std::memcpy(&b, &f, 4);
+    return b;
+}
 
 }  // namespace
 
@@ -385,57 +470,15 @@ int stride_encode(const double* verts, uint64_t n_v, const int64_t* tris, uint64
         }
         for (uint64_t i = 0; i < 3 * n_t; i++)
             if (tris[i] < 0 || static_cast<uint64_t>(tris[i]) >= n_v) { g_err = "triangle index out of range"; return -1; }
+        Quant Q;
+        if (quantize(verts, n_v, o->precision_error, o->precision_mode, Q)) return -2;
         Result* R = new Result();
-        // ---- normalise + quantise (paradelta_codec.py:767-786, :149-165)
-        double center[3] = {0, 0, 0};
-        for (uint64_t i = 0; i < n_v; i++)
-            for (int d = 0; d < 3; d++) center[d] += verts[3 * i + d];
-        for (int d = 0; d < 3; d++) center[d] /= static_cast<double>(n_v);
-        double scale = 0, bmin[3], bmax[3];
-        for (int d = 0; d < 3; d++) { bmin[d] = INFINITY; bmax[d] = -INFINITY; }
-        for (uint64_t i = 0; i < n_v; i++) {
-            double s = 0;
-            for (int d = 0; d < 3; d++) {
-                double x = verts[3 * i + d];
-                bmin[d] = std::min(bmin[d], x);
-                bmax[d] = std::max(bmax[d], x);
-                double c = x - center[d];
-                s += c * c;
-            }
-            scale = std::max(scale, std::sqrt(s));
-        }
-        if (!(scale > 0)) scale = 1.0;
-        double pce;
-        if (o->precision_mode == 0) {
-            pce = o->precision_error / scale / std::sqrt(3.0);
-        } else {
-            double ext = std::max(bmax[0] - bmin[0], std::max(bmax[1] - bmin[1], bmax[2] - bmin[2]));
-            pce = (o->precision_error * ext) / (2.0 * scale);
-        }
-        double gmin[3], grange[3];
-        std::vector<int32_t> gcodes(3 * n_v, 0);
-        for (int d = 0; d < 3; d++) {
-            double lo = INFINITY, hi = -INFINITY;
-            for (uint64_t i = 0; i < n_v; i++) {
-                double x = (verts[3 * i + d] - center[d]) / scale;
-                lo = std::min(lo, x);
-                hi = std::max(hi, x);
-            }
-            gmin[d] = lo;
-            grange[d] = hi - lo;
-            double step = 2.0 * pce;
-            if (!(grange[d] > 0)) { R->g_bits[d] = 1; continue; }
-            int nb = std::max(1, static_cast<int>(std::ceil(std::log2(grange[d] / step + 1.0))));
-            if (nb > 24) { delete R; g_err = "precision needs more than 24 bits per axis"; return -2; }
-            R->g_bits[d] = static_cast<uint32_t>(nb);
-            double mx = static_cast<double>((1u << nb) - 1u);
-            for (uint64_t i = 0; i < n_v; i++) {
-                double x = ((verts[3 * i + d] - center[d]) / scale - gmin[d]) / grange[d] * mx;
-                double q = std::nearbyint(x);  // round half to even, like np.round
-                q = std::min(std::max(q, 0.0), mx);
-                gcodes[3 * i + d] = static_cast<int32_t>(q);
-            }
-        }
+        for (int d = 0; d < 3; d++) R->g_bits[d] = Q.g_bits[d];
+        const double* center = Q.center;
+        const double scale = Q.scale, pce = Q.pce;
+        const double* gmin = Q.gmin;
+        const double* grange = Q.grange;
+        const std::vector<int32_t>& gcodes = Q.gcodes;
         // ---- partition + strips
         Encoder E{verts, n_v, tris, n_t, o->max_verts, o->max_tris, {}, {}, {}, 0};
         E.lmap.assign(n_v, -1);
@@ -633,6 +676,254 @@ int stride_encode(const double* verts, uint64_t n_v, const int64_t* tris, uint64
         return -4;
     }
 }
+
+// PLDT v5 (the reference's CuPy decoder format, written by
+// encode_from_prepared_v5, encoder/paradelta_v5.py:144-279, and read by
+// decode_paradelta_v5, :286-462) from the same partition, strips and
+// quantisation: vertices used by more than one meshlet form the global
+// boundary table; a meshlet numbers its boundary vertices first (by
+// boundary index), then its interior vertices; interior residuals follow
+// the decoder's float64 reconstruction (canonical lin3 weights 1, 1, -1,
+// boundary mean for strip roots), so every decoded interior position lies
+// within half a step (2 * per_coord_err) of its normalised source position.
+int pldt5_encode(const double* verts, uint64_t n_v, const int64_t* tris, uint64_t n_t,
+                 const stride_encode_opts* o, void** out) {
+    try {
+        if (!verts || !tris || !o || !out || n_v == 0 || n_t == 0) { g_err = "bad arguments"; return -1; }
+        if (o->max_verts < 3 || o->max_verts > 65535 || o->max_tris < 1 || o->max_tris > 65535) {
+            g_err = "max_verts/max_tris out of range"; return -1;
+        }
+        for (uint64_t i = 0; i < 3 * n_t; i++)
+            if (tris[i] < 0 || static_cast<uint64_t>(tris[i]) >= n_v) { g_err = "triangle index out of range"; return -1; }
+        Quant Q;
+        if (quantize(verts, n_v, o->precision_error, o->precision_mode, Q)) return -2;
+        Encoder E{verts, n_v, tris, n_t, o->max_verts, o->max_tris, {}, {}, {}, 0};
+        E.lmap.assign(n_v, -1);
+        E.lstamp.assign(n_v, -1);
+        E.build_adjacency();
+        std::vector<std::vector<uint32_t>> parts = E.partition();
+        std::vector<Meshlet> ms;
+        ms.reserve(parts.size());
+        std::vector<int32_t> tri_local(n_t, -1);
+        for (auto& p : parts) ms.push_back(E.strips(p, tri_local));
+        // boundary: vertices of more than one meshlet
+        std::vector<uint32_t> cnt(n_v, 0);
+        for (auto& m : ms)
+            for (uint32_t g : m.l2g) cnt[g]++;
+        std::vector<int64_t> bidx(n_v, -1);
+        std::vector<uint32_t> blist;
+        for (uint64_t g = 0; g < n_v; g++)
+            if (cnt[g] >= 2) { bidx[g] = static_cast<int64_t>(blist.size()); blist.push_back(static_cast<uint32_t>(g)); }
+        const uint64_t nb = blist.size();
+        // header values as the decoder reads them (f32)
+        double c32[3], gmin32[3], grange32[3];
+        for (int d = 0; d < 3; d++) {
+            c32[d] = static_cast<float>(Q.center[d]);
+            gmin32[d] = static_cast<float>(Q.gmin[d]);
+            grange32[d] = static_cast<float>(Q.grange[d]);
+        }
+        const double scale32 = static_cast<float>(Q.scale);
+        const double delta = 2.0 * static_cast<double>(static_cast<float>(Q.pce));
+        const double w0 = 1.0, w1 = 1.0, w2 = -1.0;
+        auto code_of = [&](uint64_t g, int d) { return static_cast<int64_t>(Q.gcodes[3 * g + d]); };
+        // boundary rows: g_min + code / mx * g_range (decode_paradelta_v5, :322-336)
+        std::vector<double> brow(3 * nb);
+        for (uint64_t b = 0; b < nb; b++)
+            for (int d = 0; d < 3; d++) {
+                const uint64_t mx = (1ull << Q.g_bits[d]) - 1ull;
+                brow[3 * b + d] = mx == 0 ? gmin32[d]
+                                          : gmin32[d] + (static_cast<double>(code_of(blist[b], d)) /
+                                                         static_cast<double>(mx)) * grange32[d];
+            }
+        Result5* R = new Result5();
+        R->n_meshlets = static_cast<uint32_t>(ms.size());
+        R->n_boundary = static_cast<uint32_t>(nb);
+        R->rows.assign(blist.begin(), blist.end());
+        BitWriter body;
+        std::vector<uint64_t> offs;
+        uint64_t max_abs = 0;
+        for (auto& m : ms) {
+            offs.push_back(body.bitpos());
+            const uint32_t nl = static_cast<uint32_t>(m.l2g.size());
+            std::vector<uint32_t> bl, il;  // old local ids of boundary / interior vertices
+            for (uint32_t l = 0; l < nl; l++) (bidx[m.l2g[l]] >= 0 ? bl : il).push_back(l);
+            std::sort(bl.begin(), bl.end(), [&](uint32_t x, uint32_t y) { return bidx[m.l2g[x]] < bidx[m.l2g[y]]; });
+            std::vector<uint32_t> nid(nl);
+            for (size_t i = 0; i < bl.size(); i++) nid[bl[i]] = static_cast<uint32_t>(i);
+            for (size_t i = 0; i < il.size(); i++) nid[il[i]] = static_cast<uint32_t>(bl.size() + i);
+            const uint32_t n_bnd = static_cast<uint32_t>(bl.size()), n_int = static_cast<uint32_t>(il.size());
+            body.put(n_bnd, 16);
+            body.put(n_int, 16);
+            body.put(m.n_tris, 16);
+            body.put(m.strip_lens.size(), 16);
+            if (n_bnd) {  // boundary references: first, then gaps minus one (:350-361)
+                body.put(static_cast<uint64_t>(bidx[m.l2g[bl[0]]]), 32);
+                if (n_bnd > 1) {
+                    std::vector<uint64_t> gaps;
+                    for (size_t i = 1; i < bl.size(); i++)
+                        gaps.push_back(static_cast<uint64_t>(bidx[m.l2g[bl[i]]] - bidx[m.l2g[bl[i - 1]]] - 1));
+                    const int k = best_rice_k(gaps, 11);
+                    body.put(k, 8);
+                    for (uint64_t u : gaps) body.rice(u, k);
+                }
+            }
+            // strips and tokens (new ids), the decoder's first-reach order
+            const int idx_bits = std::max(1, bitlen64(nl));
+            int fifo[kFifo];
+            int flen = 0;
+            std::vector<uint8_t> seen(nl, 0);
+            for (uint32_t l = 0; l < n_bnd; l++) seen[l] = 1;
+            struct Emit { uint32_t v; bool para; uint32_t a, b, c; };
+            std::vector<Emit> emit;
+            auto token = [&](int v) {
+                int at = -1;
+                for (int q = 0; q < flen; q++) if (fifo[q] == v) { at = q; break; }
+                if (at >= 0) { body.put(0, 1); body.put(static_cast<uint64_t>(at), kReuseBits); }
+                else { body.put(1, 1); body.put(static_cast<uint64_t>(v), idx_bits); }
+                if (at >= 0) { std::memmove(&fifo[at], &fifo[at + 1], (flen - at - 1) * sizeof(int)); flen--; }
+                else if (flen == kFifo) { std::memmove(&fifo[0], &fifo[1], (kFifo - 1) * sizeof(int)); flen--; }
+                fifo[flen++] = v;
+            };
+            size_t ti = 0;
+            for (size_t s = 0; s < m.strip_lens.size(); s++) {
+                body.put(m.strip_lens[s], 16);
+                uint32_t r[3];
+                for (int k = 0; k < 3; k++, ti++) {
+                    r[k] = nid[m.tokens[ti] & 0xFFFFu];
+                    token(static_cast<int>(r[k]));
+                }
+                for (int k = 0; k < 3; k++) {
+                    if (r[k] >= n_bnd && !seen[r[k]]) emit.push_back({r[k], false, 0, 0, 0});
+                    seen[r[k]] = 1;
+                }
+                uint32_t q0 = r[0], q1 = r[1], q2 = r[2];
+                for (uint32_t j = 1; j < m.strip_lens[s]; j++, ti++) {
+                    const uint32_t tk = m.tokens[ti];
+                    const uint32_t ec = ((tk >> 16) & 0xFFu) - 1u;
+                    const uint32_t v = nid[tk & 0xFFFFu];
+                    body.put(ec, 1);
+                    token(static_cast<int>(v));
+                    uint32_t a, b, c;
+                    if (ec == 0) { a = q1; b = q2; c = q0; } else { a = q0; b = q2; c = q1; }
+                    if (v >= n_bnd && !seen[v]) emit.push_back({v, true, a, b, c});
+                    seen[v] = 1;
+                    q0 = a; q1 = b; q2 = v;
+                }
+            }
+            if (emit.size() != n_int) { delete R; g_err = "an interior vertex is in no strip"; return -3; }
+            // residual codes from the decoder's reconstruction (:426-445)
+            if (n_int) {
+                std::vector<double> recon(3 * static_cast<size_t>(nl), 0.0);
+                for (uint32_t l = 0; l < n_bnd; l++)
+                    for (int d = 0; d < 3; d++) recon[3 * l + d] = brow[3 * bidx[m.l2g[bl[l]]] + d];
+                double fb[3] = {0.0, 0.0, 0.0};
+                if (n_bnd) {
+                    for (int d = 0; d < 3; d++) {
+                        double sum = recon[d];
+                        for (uint32_t l = 1; l < n_bnd; l++) sum = sum + recon[3 * l + d];
+                        fb[d] = sum / static_cast<double>(n_bnd);
+                    }
+                }
+                std::vector<int64_t> codes(3 * static_cast<size_t>(n_int));
+                for (size_t i = 0; i < emit.size(); i++) {
+                    const Emit& e = emit[i];
+                    const uint64_t g = m.l2g[il[e.v - n_bnd]];
+                    for (int d = 0; d < 3; d++) {
+                        double pred = fb[d];
+                        if (e.para) {
+                            const double t0 = w0 * recon[3 * e.a + d], t1 = w1 * recon[3 * e.b + d];
+                            const double t2 = w2 * recon[3 * e.c + d];
+                            pred = (t0 + t1) + t2;
+                        }
+                        const double target = (verts[3 * g + d] - c32[d]) / scale32;
+                        const double cd = std::nearbyint((target - pred) / delta);
+                        if (!(std::fabs(cd) < 1e15)) { delete R; g_err = "residual out of range"; return -3; }
+                        const int64_t code = static_cast<int64_t>(cd);
+                        codes[3 * i + d] = code;
+                        max_abs = std::max<uint64_t>(max_abs, static_cast<uint64_t>(code < 0 ? -code : code));
+                        recon[3 * e.v + d] = pred + static_cast<double>(code) * delta;
+                    }
+                }
+                for (int d = 0; d < 3; d++) {  // per axis: fixed width, Rice or Exp-Golomb, the smallest
+                    int64_t mn = codes[d], mxv = codes[d];
+                    std::vector<uint64_t> u(n_int);
+                    for (uint32_t i = 0; i < n_int; i++) {
+                        mn = std::min(mn, codes[3 * i + d]);
+                        mxv = std::max(mxv, codes[3 * i + d]);
+                        u[i] = zigzag(codes[3 * i + d]);
+                    }
+                    const int bw = std::max(1, bitlen64(static_cast<uint64_t>(mxv - mn)));
+                    uint64_t best = (mn >= -32768 && mn <= 32767 && bw <= 32) ? 32ull + n_int * static_cast<uint64_t>(bw) : ~0ull;
+                    int tag = 0, k = 0;
+                    const int kr = best_rice_k(u, 11);
+                    if (16 + rice_bits(u, kr) < best) { best = 16 + rice_bits(u, kr); tag = 1; k = kr; }
+                    for (int kk = 0; kk <= 7; kk++)
+                        if (16 + eg_bits(u, kk) < best) { best = 16 + eg_bits(u, kk); tag = 2; k = kk; }
+                    body.put(tag, 8);
+                    if (tag == 0) {
+                        body.put(static_cast<uint64_t>(mn) & 0xFFFFu, 16);
+                        body.put(bw, 8);
+                        for (uint32_t i = 0; i < n_int; i++) body.put(static_cast<uint64_t>(codes[3 * i + d] - mn), bw);
+                    } else {
+                        body.put(k, 8);
+                        for (uint64_t x : u) { if (tag == 1) body.rice(x, k); else body.eg(x, k); }
+                    }
+                }
+            }
+            for (uint32_t i = 0; i < n_int; i++) R->rows.push_back(m.l2g[il[i]]);
+        }
+        std::vector<uint8_t> body_bytes = body.finish();
+        // global header (:228-250) and boundary table (:252-264)
+        BitWriter h;
+        h.put(0x504C4454u, 32);
+        h.put(5, 8);
+        h.put(max_abs > 32767 ? 1 : 0, 8);
+        for (int d = 0; d < 3; d++) h.put(f32bits(Q.center[d]), 32);
+        h.put(f32bits(Q.scale), 32);
+        h.put(f32bits(Q.pce), 32);
+        for (int d = 0; d < 3; d++) h.put(f32bits(Q.gmin[d]), 32);
+        for (int d = 0; d < 3; d++) h.put(f32bits(Q.grange[d]), 32);
+        for (int d = 0; d < 3; d++) h.put(Q.g_bits[d], 8);
+        if (n_v > 0xFFFFFFFFull || n_t > 0xFFFFFFFFull) { delete R; g_err = "mesh too large for u32 header counts"; return -3; }
+        h.put(n_v, 32);
+        h.put(n_t, 32);
+        h.put(nb, 32);
+        h.put(ms.size(), 32);
+        h.put(f32bits(w0), 32);
+        h.put(f32bits(w1), 32);
+        h.put(f32bits(w2), 32);
+        for (int d = 0; d < 3 && nb > 0; d++) {
+            h.put(static_cast<uint64_t>(code_of(blist[0], d)), static_cast<int>(Q.g_bits[d]));
+            if (nb > 1) {
+                std::vector<uint64_t> u;
+                u.reserve(nb - 1);
+                for (uint64_t b = 1; b < nb; b++) u.push_back(zigzag(code_of(blist[b], d) - code_of(blist[b - 1], d)));
+                const int k = best_rice_k(u, 11);
+                h.put(k, 8);
+                for (uint64_t x : u) h.rice(x, k);
+            }
+        }
+        h.put(0, static_cast<int>((8 - h.bitpos() % 8) % 8));
+        const uint64_t start = h.bitpos() + 32ull * ms.size();
+        if (start + body_bytes.size() * 8ull > 0xFFFFFFFFull) { delete R; g_err = "blob exceeds 32-bit bit offsets"; return -3; }
+        for (uint64_t off : offs) h.put(start + off, 32);
+        R->data = h.finish();
+        R->data.insert(R->data.end(), body_bytes.begin(), body_bytes.end());
+        *out = R;
+        return 0;
+    } catch (const std::exception& e) {
+        g_err = e.what();
+        return -4;
+    }
+}
+
+uint64_t pldt5_encode_nbytes(void* r) { return static_cast<Result5*>(r)->data.size(); }
+const uint8_t* pldt5_encode_bytes(void* r) { return static_cast<Result5*>(r)->data.data(); }
+uint64_t pldt5_encode_n_rows(void* r) { return static_cast<Result5*>(r)->rows.size(); }
+const uint32_t* pldt5_encode_rows(void* r) { return static_cast<Result5*>(r)->rows.data(); }
+uint32_t pldt5_encode_n_meshlets(void* r) { return static_cast<Result5*>(r)->n_meshlets; }
+uint32_t pldt5_encode_n_boundary(void* r) { return static_cast<Result5*>(r)->n_boundary; }
+void pldt5_encode_free(void* r) { delete static_cast<Result5*>(r); }
 
 uint64_t stride_encode_nbytes(void* r) { return static_cast<Result*>(r)->data.size(); }
 const uint8_t* stride_encode_bytes(void* r) { return static_cast<Result*>(r)->data.data(); }

@@ -51,6 +51,16 @@ def _load():
             fn.argtypes = [ctypes.c_void_p]
             fn.restype = rt
         lib.stride_encode_free.argtypes = [ctypes.c_void_p]
+        lib.pldt5_encode.argtypes = lib.stride_encode.argtypes
+        lib.pldt5_encode.restype = ctypes.c_int
+        for name, rt in (("pldt5_encode_nbytes", ctypes.c_uint64), ("pldt5_encode_bytes", ctypes.c_void_p),
+                         ("pldt5_encode_n_rows", ctypes.c_uint64), ("pldt5_encode_rows", ctypes.c_void_p),
+                         ("pldt5_encode_n_meshlets", ctypes.c_uint32),
+                         ("pldt5_encode_n_boundary", ctypes.c_uint32)):
+            fn = getattr(lib, name)
+            fn.argtypes = [ctypes.c_void_p]
+            fn.restype = rt
+        lib.pldt5_encode_free.argtypes = [ctypes.c_void_p]
         _lib = lib
     return _lib
 
@@ -101,6 +111,44 @@ def encode(verts, tris, *, max_verts: int = 256, max_tris: int = 256,
     finally:
         lib.stride_encode_free(h)
     return EncodedMesh(data, l2g, codes, nm)
+
+
+@dataclass
+class EncodedPldt5:
+    """A PLDT v5 stream and, per decoded row (the boundary vertices, then
+    every meshlet's interior vertices), its source vertex id."""
+    data: bytes
+    rows: np.ndarray     # uint32 (n_rows,)
+    n_meshlets: int
+    n_boundary: int
+
+
+def encode_pldt5(verts, tris, *, max_verts: int = 256, max_tris: int = 256,
+                 precision_error: float = 0.0005, precision_mode: str = "world") -> EncodedPldt5:
+    """Encode a mesh as PLDT v5, the format of the reference's CuPy decoder
+    (encoder/paradelta_v5.py:144-279), for decoder inputs at scale: this
+    project's partition, strips and quantisation, canonical lin3 weights."""
+    lib = _load()
+    V = np.ascontiguousarray(verts, dtype=np.float64)
+    T = np.ascontiguousarray(tris, dtype=np.int64)
+    if V.ndim != 2 or V.shape[1] != 3 or T.ndim != 2 or T.shape[1] != 3:
+        raise ValueError("verts and tris must be (n, 3) arrays")
+    if precision_mode not in ("world", "bbox_frac"):
+        raise ValueError(f"unknown precision_mode={precision_mode!r}")
+    opts = _Opts(int(max_verts), int(max_tris), float(precision_error), 0 if precision_mode == "world" else 1, 0)
+    h = ctypes.c_void_p()
+    rc = lib.pldt5_encode(V.ctypes.data, V.shape[0], T.ctypes.data, T.shape[0], ctypes.byref(opts), ctypes.byref(h))
+    if rc != 0:
+        raise ValueError(f"pldt5_encode failed: {lib.stride_encode_last_error().decode()}")
+    try:
+        data = ctypes.string_at(lib.pldt5_encode_bytes(h), lib.pldt5_encode_nbytes(h))
+        nr = lib.pldt5_encode_n_rows(h)
+        rows = np.ctypeslib.as_array(ctypes.cast(lib.pldt5_encode_rows(h), ctypes.POINTER(ctypes.c_uint32)),
+                                     shape=(nr,)).copy() if nr else np.zeros(0, np.uint32)
+        out = EncodedPldt5(data, rows, int(lib.pldt5_encode_n_meshlets(h)), int(lib.pldt5_encode_n_boundary(h)))
+    finally:
+        lib.pldt5_encode_free(h)
+    return out
 
 
 @dataclass

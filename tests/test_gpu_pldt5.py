@@ -99,3 +99,17 @@ def test_corrupt_streams_rejected_or_exact(torch_cuda):
         assert np.array_equal(gidx.astype(np.int64), oidx)
         agree += 1
     assert rejected > 0
+
+
+def test_project_encoder_stream_at_scale(torch_cuda):
+    """A 131,072-triangle heightfield (1,348 meshlets of at most 128
+    vertices) written by the project PLDT v5 encoder: the GPU decode equals
+    the oracle's bit for bit."""
+    from meshpress_gb300 import encoder, synth
+    V, T = synth.noise_heightfield(257, seed=3)
+    e = encoder.encode_pldt5(V, T, precision_error=synth.bbox_bits_error(12), precision_mode="bbox_frac",
+                             max_verts=128, max_tris=128)
+    opos, oidx = oracle.decode_v5(e.data)
+    gpos, gidx = _gpu(e.data)
+    assert np.array_equal(gpos.view(np.uint32), opos.view(np.uint32))
+    assert np.array_equal(gidx.astype(np.int64), oidx)
