@@ -318,6 +318,9 @@ typedef struct {
  * a device copy.  Replaces parse_globals_v5 + ParaDeltaV5GpuDecoder.__init__
  * (utils/paradelta_v5_cuda.py:515-684). */
 int pldt5_open(const uint8_t* data, size_t len, pldt5_handle** out);
+/* The same host parse and validation without a device (sizes of the
+ * outputs, header fields); like stride_inspect. */
+int pldt5_inspect(const uint8_t* data, size_t len, pldt5_info_t* info);
 int pldt5_info(const pldt5_handle* h, pldt5_info_t* info);
 /* Enqueue the decode on `stream`: triangles (n_t x 3 uint32, global rows)
  * and world-space positions (n_v x 3 float32) into device buffers.

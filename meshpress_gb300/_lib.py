@@ -129,6 +129,7 @@ SIGNATURES = [
     ("stride_server_stats", _I, [_P, ctypes.POINTER(_U64), ctypes.POINTER(_U64), ctypes.POINTER(_U64)]),
     ("stride_server_destroy", None, [_P]),
     ("pldt5_open", _I, [_P, _SZ, ctypes.POINTER(_P)]),
+    ("pldt5_inspect", _I, [_P, _SZ, ctypes.POINTER(Pldt5Info)]),
     ("pldt5_info", _I, [_P, ctypes.POINTER(Pldt5Info)]),
     ("pldt5_decode", _I, [_P, _P, _P, _P]),
     ("pldt5_status", _I, [_P, _I]),
@@ -164,6 +165,14 @@ def check(rc: int, what: str = "stride"):
     if rc in FORMAT_ERRORS:
         raise StrideFormatError(rc, msg)
     raise StrideDeviceError(rc, msg)
+
+
+def inspect_pldt5(data: bytes) -> Pldt5Info:
+    """Host-only parse/validation of a PLDT v5 stream (no GPU needed)."""
+    info = Pldt5Info()
+    data = bytes(data)
+    check(load().pldt5_inspect(data, len(data), ctypes.byref(info)), "pldt5_inspect")
+    return info
 
 
 def inspect(data: bytes) -> StrideInfo:

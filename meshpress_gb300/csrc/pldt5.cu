@@ -432,14 +432,21 @@ static void pldt5_free(pldt5_handle* h) {
     delete h;
 }
 
-extern "C" {
+// Host parse shared by pldt5_open and pldt5_inspect: header, boundary rows
+// (float64), every meshlet's start bit and output placement.  STRIDE_OK or
+// a STRIDE_ERR_* with the message set.
+struct P5Host {
+    pldt5_info_t info;
+    float per_coord_err;
+    std::vector<double> rows0;    // boundary rows, n_boundary x 3
+    std::vector<uint32_t> meta;   // start (M + 1) | row_base (M) | tri_base (M) | ref_base (M)
+    uint64_t refs = 0;
+};
 
-int pldt5_open(const uint8_t* data, size_t len, pldt5_handle** out) {
-    if (!out || (!data && len)) return fail(STRIDE_ERR_ARG, "null argument");
-    *out = nullptr;
+static int p5_host_parse(const uint8_t* data, size_t len, P5Host& H) {
+    pldt5_info_t& info = H.info;
     HostBits r{data, 8ull * len, 0, false};
     if (8ull * len < kP5HeaderBits) return fail(STRIDE_ERR_TRUNCATED, "PLDT v5 header past the end");
-    pldt5_info_t info;
     std::memset(&info, 0, sizeof(info));
     const uint32_t magic = static_cast<uint32_t>(r.read(32));
     if (magic != kP5Magic) return fail(STRIDE_ERR_MAGIC, "bad magic 0x%08X (PLDT v5 expected)", magic);
@@ -449,6 +456,7 @@ int pldt5_open(const uint8_t* data, size_t len, pldt5_handle** out) {
     for (int d = 0; d < 3; d++) info.center[d] = r.f32();
     info.scale = r.f32();
     const float per_coord_err = r.f32();
+    H.per_coord_err = per_coord_err;
     float g_min[3], g_range[3];
     for (int d = 0; d < 3; d++) g_min[d] = r.f32();
     for (int d = 0; d < 3; d++) g_range[d] = r.f32();
@@ -464,7 +472,8 @@ int pldt5_open(const uint8_t* data, size_t len, pldt5_handle** out) {
     // the CPU decoder (:322-336)
     const uint64_t nb = info.n_boundary;
     if (nb > 8ull * len) return fail(STRIDE_ERR_TRUNCATED, "boundary table past the end");
-    std::vector<double> rows0(3 * nb);
+    std::vector<double>& rows0 = H.rows0;
+    rows0.assign(3 * nb, 0.0);
     {
         std::vector<int64_t> code(3 * nb, 0);
         for (int d = 0; d < 3 && nb > 0; d++) {
@@ -493,7 +502,8 @@ int pldt5_open(const uint8_t* data, size_t len, pldt5_handle** out) {
     r.pos += (0ull - r.pos) & 7ull;
     const uint64_t M = info.n_meshlets;
     if (r.pos + 32ull * M > r.nbits) return fail(STRIDE_ERR_TRUNCATED, "offset table past the end");
-    std::vector<uint32_t> meta(4 * M + 1);
+    std::vector<uint32_t>& meta = H.meta;
+    meta.assign(4 * M + 1, 0u);
     uint32_t* start = meta.data();
     uint32_t* row_base = start + M + 1;
     uint32_t* tri_base = row_base + M;
@@ -502,7 +512,7 @@ int pldt5_open(const uint8_t* data, size_t len, pldt5_handle** out) {
     const uint64_t body = r.pos;
     start[M] = static_cast<uint32_t>(std::min<uint64_t>(8ull * len, 0xFFFFFFFFull));
     if (8ull * len > 0xFFFFFFFFull) return fail(STRIDE_ERR_UNSUPPORTED, "stream above 512 MiB");
-    uint64_t rows = nb, tris = 0, refs = 0, walk = 0;
+    uint64_t rows = nb, tris = 0, refs = 0;
     for (uint64_t m = 0; m < M; m++) {
         // the CPU decoder reads meshlets back to back from the end of the table
         if ((m == 0 && start[0] != body) || start[m] < body || start[m] + 64ull > 8ull * len ||
@@ -521,13 +531,29 @@ int pldt5_open(const uint8_t* data, size_t len, pldt5_handle** out) {
         rows += n_int;
         tris += n_tris;
         refs += n_bnd;
-        walk += n_int;
         if (rows > 0xFFFFFFFFull || tris > 0x55555555ull)
             return fail(STRIDE_ERR_UNSUPPORTED, "more than 2^32 rows or 2^32 indices");
     }
     info.n_v = rows;
     info.n_t = tris;
     info.nbytes = len;
+    H.refs = refs;
+    return STRIDE_OK;
+}
+
+extern "C" {
+
+int pldt5_open(const uint8_t* data, size_t len, pldt5_handle** out) {
+    if (!out || (!data && len)) return fail(STRIDE_ERR_ARG, "null argument");
+    *out = nullptr;
+    P5Host H;
+    const int prc = p5_host_parse(data, len, H);
+    if (prc) return prc;
+    const pldt5_info_t& info = H.info;
+    const uint64_t nb = info.n_boundary, rows = info.n_v, refs = H.refs;
+    const float per_coord_err = H.per_coord_err;
+    const std::vector<double>& rows0 = H.rows0;
+    const std::vector<uint32_t>& meta = H.meta;
 
     pldt5_handle* h = new pldt5_handle();
     h->info = info;
@@ -560,6 +586,15 @@ int pldt5_open(const uint8_t* data, size_t len, pldt5_handle** out) {
         return cuda_fail(e, "pldt5_open upload");
     }
     *out = h;
+    return STRIDE_OK;
+}
+
+int pldt5_inspect(const uint8_t* data, size_t len, pldt5_info_t* info) {
+    if (!info || (!data && len)) return fail(STRIDE_ERR_ARG, "null argument");
+    P5Host H;
+    const int rc = p5_host_parse(data, len, H);
+    if (rc) return rc;
+    *info = H.info;
     return STRIDE_OK;
 }
 

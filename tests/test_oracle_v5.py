@@ -84,3 +84,39 @@ def test_sblb_blob_layout():
     h = oracle.parse_header_v5(data)
     world = (bnd.astype(np.float64) * np.float32(h.scale) + np.array(h.center, np.float32)).astype(np.float32)
     assert np.abs(world - pos[:nb]).max() < 1e-5 * max(1.0, float(np.abs(pos).max()))
+
+
+@pytest.mark.parametrize("name", V5_CASES)
+def test_host_inspect_matches_oracle(name):
+    """pldt5_inspect (the library's host parse, no GPU): header fields and
+    output sizes as the oracle decodes them."""
+    from meshpress_gb300 import _lib
+    data, pos, idx, meta = _load(name)
+    info = _lib.inspect_pldt5(data)
+    h = oracle.parse_header_v5(data)
+    assert (info.n_meshlets, info.n_boundary) == (h.n_meshlets, h.n_boundary)
+    assert list(info.g_bits) == list(h.g_bits) and info.nbytes == len(data)
+    assert (info.n_v, info.n_t) == (len(pos), len(idx))
+    assert info.scale == h.scale and list(info.lin3_w) == list(h.lin3_w)
+
+
+def test_host_inspect_rejects():
+    from meshpress_gb300 import _lib
+    data, _, _, _ = _load("v5_grid33_mv64")
+    with pytest.raises(_lib.StrideFormatError):
+        _lib.inspect_pldt5(_golden.load("grid33_b12")["data"])  # DPR4 bytes
+    bad = bytearray(data)
+    bad[4] = 4
+    with pytest.raises(_lib.StrideFormatError):
+        _lib.inspect_pldt5(bytes(bad))
+    for cut in (10, 60, 200):
+        with pytest.raises(_lib.StrideFormatError):
+            _lib.inspect_pldt5(data[:cut])
+    # meshlet 1's offset equal to meshlet 0's: the table must increase
+    h = oracle.parse_header_v5(data)
+    t = oracle.tables_v5(data)
+    table = int(t["off_bits"][0]) // 8 - 4 * h.n_meshlets  # the table ends where meshlet 0 starts
+    bad = bytearray(data)
+    bad[table + 4:table + 8] = bad[table:table + 4]
+    with pytest.raises(_lib.StrideFormatError):
+        _lib.inspect_pldt5(bytes(bad))
