@@ -200,12 +200,14 @@ def measured_peak():
     return 6800.0, "fallback 6.8 TB/s"
 
 
-def kernel_split(kern, fused: bool, stream_bytes: int, n_v: int, n_t: int):
+def kernel_split(kern, fused: bool, stream_bytes: int, n_v: int, n_t: int, persistent: int = 3):
     """Names of the decode's kernels, the dominant one and its algorithmic
-    bytes, from the per-kernel times (scan, connectivity, vertex; the fused
-    kernel's time in the second slot)."""
-    if fused:  # the fused kernel reads the stream and writes both outputs
-        return ("scan_kernel", "flow_kernel"), 1, stream_bytes + 12 * (n_v + n_t)
+    bytes, from the per-kernel times (scan, connectivity, vertex; a one-kernel
+    decode's time in the second slot: the group kernel, persistent 3, or the
+    fused kernel, persistent 2)."""
+    if fused:  # one kernel reads the stream and writes both outputs
+        name = "group_kernel" if persistent == 3 else "flow_kernel"
+        return ("scan_kernel", name), 1, stream_bytes + 12 * (n_v + n_t)
     # connectivity reads the stream and writes the indices (12 B per
     # triangle); the vertex kernel writes the positions (12 B per vertex)
     # from residual bits already counted in the stream
@@ -420,7 +422,8 @@ def run_single(args):
     alg_bytes = len(data) + 12 * (n_v + n_t)
     peak, peak_src = measured_peak()
     k = np.array(kern_ms).mean(axis=0)
-    names, dom, dom_bytes = kernel_split(k, int(dec.info.kernels) == 2, len(data), n_v, n_t)
+    names, dom, dom_bytes = kernel_split(k, int(dec.info.kernels) == 2, len(data), n_v, n_t,
+                                         int(launch["persistent"]) if launch else 3)
     achieved = dom_bytes / (k[dom] / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": ncu_traffic(names[dom], cfg["workload"]),
@@ -500,7 +503,7 @@ def run_batch(args):
         launch = dict(best.as_dict(), tuned_ms=round(best_ms, 4))
     # scan (with the dequantisation tables), then the fused kernel or the
     # connectivity and vertex kernels
-    fused = int(b.config().persistent) == 2
+    fused = int(b.config().persistent) >= 2
     per_step_kernels = 2 if fused else 3
     stream = torch.cuda.Stream(device=dev)
     with torch.cuda.stream(stream):
@@ -615,7 +618,8 @@ def run_batch(args):
 
     if rank == 0:
         peak, peak_src = measured_peak()
-        names, dom, dom_bytes = kernel_split(kern, fused, cfg["stream_bytes"], b.n_v_total, b.n_t_total)
+        names, dom, dom_bytes = kernel_split(kern, fused, cfg["stream_bytes"], b.n_v_total, b.n_t_total,
+                                             int(b.config().persistent))
         achieved = dom_bytes / (kern[dom] / 1e3) / 1e9
         alg = cfg["stream_bytes"] + 12 * (b.n_t_total + b.n_v_total)
         cfg = dict(cfg)

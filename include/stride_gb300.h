@@ -60,11 +60,11 @@ typedef struct {
     int32_t pred_n[9];
     int32_t pred_k[3];
     uint32_t kernels;    /* kernel launches one decode makes: 2 with the
-                            default launch shape (scan, which also fills any
-                            per-code dequantisation tables; one fused
-                            connectivity + vertex kernel), 3 with the
-                            two-kernel shapes (persistent 0 or 1), 0 for an
-                            empty stream                                      */
+                            one-kernel shapes (scan, which also fills any
+                            per-code dequantisation tables; then the fused
+                            or the group kernel: persistent 2 or 3), 3 with
+                            the two-kernel shapes (persistent 0 or 1), 0 for
+                            an empty stream                                   */
 } stride_info_t;
 
 /* Launch shape of the decode kernel (the autotuner's search space). */
@@ -77,6 +77,10 @@ typedef struct {
                                 phases: CTAs of two pairs take connectivity
                                 groups, then vertex work in the order groups
                                 finish (warps_per_cta must be 4);
+                                3 = group kernel: one warp decodes a group of
+                                32 meshlets through every phase, lane per
+                                meshlet (warps_per_cta 1 or 2; stage_bytes
+                                and code_bytes unused);
                                 1 = connectivity kernel, then a persistent
                                 work-stealing vertex grid; 0 = connectivity
                                 kernel, then one vertex CTA per group        */

@@ -23,7 +23,7 @@ INCLUDE = os.path.join(REPO, "include")
 DECODER_LIB = os.path.join(HERE, "libstride_gb300.so")
 ENCODER_LIB = os.path.join(HERE, "libstride_encode.so")
 
-CUDA_SOURCES = ["stride_kernels.cu", "stride_api.cu", "stride_batch.cu", "stride_serve.cu", "stride_static.cu",
+CUDA_SOURCES = ["stride_kernels.cu", "stride_group.cu", "stride_api.cu", "stride_batch.cu", "stride_serve.cu", "stride_static.cu",
                 "pldt5.cu"]
 NVCC_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3",
               "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler", "-ffp-contract=off",

@@ -324,8 +324,8 @@ static void fill_info(const MeshParams& p, size_t len, int persistent, stride_in
     info->n_v = p.n_v;
     info->n_t = p.n_t;
     info->nbytes = len;
-    // scan (+ tables), then one fused kernel or the connectivity and vertex kernels
-    info->kernels = p.n_meshlets ? (persistent == 2 ? 2u : 3u) : 0u;
+    // scan (+ tables), then one kernel (group or fused) or the connectivity and vertex kernels
+    info->kernels = p.n_meshlets ? (persistent >= 2 ? 2u : 3u) : 0u;
 }
 
 int stride_inspect(const uint8_t* data, size_t len, stride_info_t* info) {

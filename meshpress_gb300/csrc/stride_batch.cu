@@ -346,6 +346,13 @@ int stride_batch_autotune(stride_batch* b, void* stream, uint32_t* d_idx, float*
                     if (check_config(c, b->wide)) continue;
                     cands.push_back(c);
                 }
+    for (int w : {1, 2}) {  // the group kernel: no stage or plane sizes to choose
+        LaunchCfg c;
+        c.warps_per_cta = w;
+        c.persistent = 3;
+        c.ctas_per_sm = 0;
+        cands.push_back(c);
+    }
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);

@@ -106,7 +106,8 @@ struct Status {
 
 struct LaunchCfg {
     int warps_per_cta = 4;
-    int persistent = 2;  // 0: one vertex CTA per group, 1: persistent vertex grid, 2: one fused kernel
+    int persistent = 2;  // 0: one vertex CTA per group, 1: persistent vertex grid, 2: one fused kernel,
+                         // 3: group kernel (one warp per group, every phase; warps_per_cta 1 or 2)
     int ctas_per_sm = 0;
     uint32_t stage_bytes = 16 * 1024;  // per-warp payload staging (vertex kernel: half)
     uint32_t code_bytes = 12 * 1024;   // per-warp integer code plane (vertex kernel)
@@ -178,6 +179,11 @@ int enqueue_cull(const float* bounds, uint32_t n, const Planes& planes, uint32_t
 // relative to it.
 int enqueue_side_table(const MeshletDesc* descs, uint32_t n, unsigned long long* resid_bit, uint16_t* sub_offs,
                        void* stream);
+
+// The group kernel (stride_group.cu): launch for `a` on `stream`, and its
+// shared memory per CTA.
+cudaError_t launch_group(const DecodeArgs& a, const LaunchCfg& cfg, void* stream);
+size_t group_smem_bytes(const LaunchCfg& cfg);
 
 // STRIDE_OK when `cfg` is a launchable shape.
 int check_config(const LaunchCfg& cfg, bool wide);

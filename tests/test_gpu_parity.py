@@ -142,8 +142,10 @@ def _cfg(w, pers, stage, code, per_sm=0):
     (4, 2, 12 * 1024, 6 * 1024),  # fused connectivity + vertex kernel
     (4, 2, 256, 2048),           # fused, global reads
     (4, 2, 64 * 1024, 516),      # fused, one meshlet per round
+    (2, 3, 0, 0),                # group kernel: one warp per group, two warps per CTA
+    (1, 3, 0, 0),                # group kernel, one warp per CTA
 ], ids=["w1", "w2", "w4p", "global_reads", "one_per_round", "fused", "fused_global_reads",
-        "fused_one_per_round"])
+        "fused_one_per_round", "group", "group_w1"])
 def test_launch_shapes_give_identical_output(torch_cuda, cfg):
     V, T = synth.icosphere(5, seed=11)
     e = encoder.encode(V, T, precision_error=B12, precision_mode="bbox_frac")
@@ -151,8 +153,9 @@ def test_launch_shapes_give_identical_output(torch_cuda, cfg):
     assert_same_as_oracle(e.data, pos, idx, codes)
 
 
-@pytest.mark.parametrize("cfg", [(2, 1, 16 * 1024, 1028), (1, 0, 256, 32 * 1024), (4, 2, 16 * 1024, 1028)],
-                         ids=["one_per_round", "global_reads", "fused_one_per_round"])
+@pytest.mark.parametrize("cfg", [(2, 1, 16 * 1024, 1028), (1, 0, 256, 32 * 1024), (4, 2, 16 * 1024, 1028),
+                                 (2, 3, 0, 0)],
+                         ids=["one_per_round", "global_reads", "fused_one_per_round", "group"])
 def test_wide_codes_launch_shapes(torch_cuda, cfg):
     """20-bit codes (32-bit code plane) under the smallest plane and stage."""
     V, T = synth.heightfield_grid(129, seed=6)
