@@ -580,16 +580,17 @@ __device__ void emit_axis(const DecodeArgs& a, const GroupLane& L, uint32_t rmas
         const PlaneT<kWide>* pj = reinterpret_cast<const PlaneT<kWide>*>(planes + off);
         float* dst = a.pos + 3ull * vb + d;
         if (has_lut) {  // every table read of the meshlet (<= 256 vertices) in flight at once
+            const uint32_t ns = (nv + 31u) >> 5;  // slots the meshlet fills (warp-uniform)
             float y[kMaxLocal / 32];
 #pragma unroll
             for (uint32_t k = 0; k < kMaxLocal / 32u; k++) {
                 const uint32_t v = lane + 32u * k;
-                y[k] = v < nv ? __ldcg(lut + min(static_cast<uint32_t>(pj[v]), qmax)) : 0.f;
+                y[k] = (k < ns && v < nv) ? __ldcg(lut + min(static_cast<uint32_t>(pj[v]), qmax)) : 0.f;
             }
 #pragma unroll
             for (uint32_t k = 0; k < kMaxLocal / 32u; k++) {
                 const uint32_t v = lane + 32u * k;
-                if (v < nv) dst[3u * v] = y[k];
+                if (k < ns && v < nv) dst[3u * v] = y[k];
             }
         } else {
             for (uint32_t v = lane; v < nv; v += 32u) {

@@ -240,6 +240,11 @@ __device__ __forceinline__ void gfetch(const DecodeArgs& a, uint32_t* ring, unsi
     ring_fetch(ring, a.arena + s0, avail, rot, c);
 }
 
+// Word r (rotated index) of a lane's byte ring, in bit order.
+__device__ __forceinline__ uint32_t ring_word(const uint32_t* ring, uint32_t r) {
+    return bswap32(ring[r & (kLaneRingWords - 1u)]);
+}
+
 // Masks of the FIFO's move-to-front (depths 0..p of the 16-byte register, as
 // four words), one 16-byte row per p in shared memory: the row is loaded
 // off the FIFO's dependency chain, where computing it would cost nine
@@ -287,8 +292,7 @@ __device__ __forceinline__ void gconn(const DecodeArgs& a, GLane& G, bool act, u
     const uint32_t q0 = act ? L.d.start_bit + 48u - base0 : 0u;
     uint32_t wi = q0 >> 5, off = q0 & 31u;
     uint32_t ri = wi + 2u + rot;
-    auto ld = [ring](uint32_t r) { return bswap32(ring[r & (kLaneRingWords - 1u)]); };
-    uint32_t w0 = ld(ri - 2u), w1 = ld(ri - 1u), w2 = ld(ri);
+    uint32_t w0 = ring_word(ring, ri - 2u), w1 = ring_word(ring, ri - 1u), w2 = ring_word(ring, ri);
     uint32_t* walk_out = a.walk_scratch + L.wp_base;
     const uint32_t vloc = act ? static_cast<uint32_t>(L.v_base - L.P->v_offset) : 0u;
     const uint32_t ph = static_cast<uint32_t>(L.t_base) & 3u;  // ring slot of triangle 0
@@ -385,7 +389,7 @@ __device__ __forceinline__ void gconn(const DecodeArgs& a, GLane& G, bool act, u
             const bool cross = off >= 32u;
             off &= 31u;
             ri += cross ? 1u : 0u;
-            const uint32_t nw = ld(ri);
+            const uint32_t nw = ring_word(ring, ri);
             w0 = cross ? w1 : w0;
             w1 = cross ? w2 : w1;
             w2 = cross ? nw : w2;
@@ -464,7 +468,19 @@ __device__ __forceinline__ bool gwalk_lin(const LinRd& rd, const AxisCode& c, co
     const uint32_t cd0 = cd, cp0 = cp;
     int32_t prev = c.anc;
     uint32_t cmx = 0u, lmx = 0u;
-    auto step = [&](uint32_t e) {
+    // the first walk entry is the anchor (no residual)
+    uint4 q = __ldcg(wq);
+    const uint32_t v0 = q.x & 0xFFu;
+    plane[v0] = static_cast<PlaneT<kWide>>(c.anc);
+    uint4 qn = n_walk > 4u ? __ldcg(wq + 1) : q;
+    // one loop body for every entry: entry j is word j % 4 of quad j / 4,
+    // the next quad in flight
+    for (uint32_t j = 1u; j < n_walk; j++) {
+        if ((j & 3u) == 0u) {
+            q = qn;
+            if (j + 4u < n_walk) qn = __ldcg(wq + (j >> 2) + 1u);
+        }
+        const uint32_t e = (j & 2u) ? ((j & 1u) ? q.w : q.z) : ((j & 1u) ? q.y : q.x);
         const uint32_t v = e & 0xFFu;
         const uint32_t ra = (e >> 8) & 0xFFu, rb = (e >> 16) & 0xFFu, rc = e >> 24;
         const bool para = ra != v;  // roots are stored as (v, v, v, v)
@@ -493,34 +509,6 @@ __device__ __forceinline__ bool gwalk_lin(const LinRd& rd, const AxisCode& c, co
         cmx = max(cmx, static_cast<uint32_t>(code));
         plane[v] = static_cast<PlaneT<kWide>>(code);
         prev = code;
-    };
-    // the first walk entry is the anchor (no residual)
-    const uint4 q0 = __ldcg(wq);
-    plane[q0.x & 0xFFu] = static_cast<PlaneT<kWide>>(c.anc);
-    uint32_t i = 1u;
-    {
-        // entries 1..3 of the first quad
-        if (i < n_walk) step(q0.y);
-        if (i + 1u < n_walk) step(q0.z);
-        if (i + 2u < n_walk) step(q0.w);
-        i = 4u;
-        uint4 qn = n_walk > 4u ? __ldcg(wq + 1) : q0;
-        uint4 qm = n_walk > 8u ? __ldcg(wq + 2) : q0;
-        for (; i + 4u <= n_walk; i += 4u) {  // whole quads
-            const uint4 q = qn;
-            qn = qm;
-            if (i + 12u <= n_walk + 3u) qm = __ldcg(wq + (i >> 2) + 2u);
-            step(q.x);
-            step(q.y);
-            step(q.z);
-            step(q.w);
-        }
-        if (i < n_walk) {  // the last, partial quad
-            const uint4 q = qn;
-            step(q.x);
-            if (i + 1u < n_walk) step(q.y);
-            if (i + 2u < n_walk) step(q.z);
-        }
     }
     bool ok = cmx <= c.cmax && static_cast<uint32_t>(c.anc) <= c.cmax && max(cd, cp) <= lim;
     if (lmx > 32u) {  // rare: a codeword longer than the window; the axis again, general reader
