@@ -55,52 +55,6 @@ constexpr uint32_t kGWorkBytes = 32u * kGFlagStride + 2u * 32u * kGRow * 4u;
 constexpr uint32_t kGWarpBytes = kGRingBytes + kGWorkBytes;  // 21,632 bytes
 
 // ---------------------------------------------------------------------------
-// FIFO: byte i of (f0, f1, f2, f3) is depth i, depth 0 the newest entry;
-// `len` entries are valid.  Deque index fi (0 = oldest) is depth len-1-fi.
-// ---------------------------------------------------------------------------
-struct MtfFifo {
-    uint32_t f0 = 0, f1 = 0, f2 = 0, f3 = 0, len = 0;
-
-    __device__ __forceinline__ uint32_t at(uint32_t s) const {
-        const bool h = (s & 8u) != 0u;
-        return __byte_perm(h ? f2 : f0, h ? f3 : f1, s & 7u) & 0xFFu;
-    }
-    // Remove depth p, move depths 0 .. p-1 one deeper and put v (< 256) at
-    // depth 0, given the masks of depths <= p (mtf_mask_row(p)): word w
-    // takes its shifted value at those depths.
-    __device__ __forceinline__ void mtf_masked(uint32_t v, uint4 m) {
-        const uint32_t s0 = __byte_perm(f0, v, 0x2104u);
-        const uint32_t s1 = __funnelshift_l(f0, f1, 8u);
-        const uint32_t s2 = __funnelshift_l(f1, f2, 8u);
-        const uint32_t s3 = __funnelshift_l(f2, f3, 8u);
-        f0 = (s0 & m.x) | (f0 & ~m.x);
-        f1 = (s1 & m.y) | (f1 & ~m.y);
-        f2 = (s2 & m.z) | (f2 & ~m.z);
-        f3 = (s3 & m.w) | (f3 & ~m.w);
-    }
-    // exact zero-byte flags of f ^ vv at the bytes marked 0x80 in m
-    __device__ __forceinline__ static uint32_t match(uint32_t f, uint32_t vv, uint32_t m) {
-        const uint32_t x = f ^ vv;
-        const uint32_t t = (x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu;
-        return ~(t | x) & m;
-    }
-    // depth of v among the valid entries, or 16
-    __device__ __forceinline__ uint32_t find(uint32_t v) const {
-        const uint32_t vv = __byte_perm(v, 0u, 0u);
-        const int32_t b = static_cast<int32_t>(8u * len);
-        const uint32_t k = 0x80808080u;
-        const uint32_t t0 = match(f0, vv, __funnelshift_lc(0xFFFFFFFFu, 0u, static_cast<uint32_t>(b)) & k);
-        const uint32_t t1 = match(f1, vv, __funnelshift_lc(0xFFFFFFFFu, 0u, static_cast<uint32_t>(max(b - 32, 0))) & k);
-        const uint32_t t2 = match(f2, vv, __funnelshift_lc(0xFFFFFFFFu, 0u, static_cast<uint32_t>(max(b - 64, 0))) & k);
-        const uint32_t t3 = match(f3, vv, __funnelshift_lc(0xFFFFFFFFu, 0u, static_cast<uint32_t>(max(b - 96, 0))) & k);
-        const uint32_t t = t0 | t1 | t2 | t3;  // the entries are distinct: at most one byte is set
-        const uint32_t j = ((t >> 7) * 0x00010203u) >> 24;
-        const uint32_t i = ((t1 | t3) != 0u ? 1u : 0u) | ((t2 | t3) != 0u ? 2u : 0u);
-        return t ? 4u * i + j : 16u;
-    }
-};
-
-// ---------------------------------------------------------------------------
 // Residual reader over the stream in global memory: peek(pos) = the 32 bits
 // from stream bit pos.
 // ---------------------------------------------------------------------------
@@ -243,20 +197,6 @@ __device__ __forceinline__ void gfetch(const DecodeArgs& a, uint32_t* ring, unsi
 // Word r (rotated index) of a lane's byte ring, in bit order.
 __device__ __forceinline__ uint32_t ring_word(const uint32_t* ring, uint32_t r) {
     return bswap32(ring[r & (kLaneRingWords - 1u)]);
-}
-
-// Masks of the FIFO's move-to-front (depths 0..p of the 16-byte register, as
-// four words), one 16-byte row per p in shared memory: the row is loaded
-// off the FIFO's dependency chain, where computing it would cost nine
-// instructions per token.
-__device__ __forceinline__ uint4 mtf_mask_row(uint32_t p) {
-    const int32_t b = static_cast<int32_t>(8u * p + 8u);
-    uint4 m;
-    m.x = __funnelshift_lc(0xFFFFFFFFu, 0u, static_cast<uint32_t>(b));
-    m.y = __funnelshift_lc(0xFFFFFFFFu, 0u, static_cast<uint32_t>(max(b - 32, 0)));
-    m.z = __funnelshift_lc(0xFFFFFFFFu, 0u, static_cast<uint32_t>(max(b - 64, 0)));
-    m.w = __funnelshift_lc(0xFFFFFFFFu, 0u, static_cast<uint32_t>(max(b - 96, 0)));
-    return m;
 }
 
 // Connectivity of the warp's lanes, one token per iteration.  Validity is

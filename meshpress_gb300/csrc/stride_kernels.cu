@@ -250,58 +250,6 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a, uint32
 }
 
 // ---------------------------------------------------------------------------
-// Move-to-tail FIFO of 16 local ids in registers.  Byte i of (f0..f3) is
-// deque position i with the newest entry at byte 15; m0..m3 hold 0x80 at
-// the valid bytes [16 - len, 16).  Deque index fi (0 = oldest) is byte
-// 16 - len + fi.
-// ---------------------------------------------------------------------------
-struct Fifo {
-    uint32_t f0 = 0, f1 = 0, f2 = 0, f3 = 0;
-    uint32_t m0 = 0, m1 = 0, m2 = 0, m3 = 0;
-    uint32_t len = 0;
-
-    __device__ __forceinline__ uint32_t at(uint32_t p) const {
-        const uint32_t w = (p & 8u) ? ((p & 4u) ? f3 : f2) : ((p & 4u) ? f1 : f0);
-        return __byte_perm(w, 0u, 0x4440u | (p & 3u));
-    }
-    // exact zero-byte flags of f ^ v at the valid bytes
-    __device__ __forceinline__ static uint32_t match(uint32_t f, uint32_t vv, uint32_t m) {
-        const uint32_t x = f ^ vv;
-        const uint32_t b = (x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu;
-        return ~(b | x) & m;
-    }
-    // byte position of v among the valid entries, or 16.  The valid entries
-    // are distinct, so at most one byte matches: its word i comes from which
-    // t is set, its byte j from the single bit 8j + 7 (2^(8j) * 0x00010203
-    // has j in its top byte) -- no bit-scan instruction on the chain.
-    __device__ __forceinline__ uint32_t find(uint32_t v) const {
-        const uint32_t vv = __byte_perm(v, 0u, 0u);
-        const uint32_t t0 = match(f0, vv, m0), t1 = match(f1, vv, m1);
-        const uint32_t t2 = match(f2, vv, m2), t3 = match(f3, vv, m3);
-        const uint32_t t = t0 | t1 | t2 | t3;
-        const uint32_t j = ((t >> 7) * 0x00010203u) >> 24;
-        const uint32_t i = ((t1 | t3) != 0u ? 1u : 0u) | ((t2 | t3) != 0u ? 2u : 0u);
-        return t ? 4u * i + j : 16u;
-    }
-    // remove the byte at p, shift the newer bytes down, append v as newest
-    __device__ __forceinline__ void remove_append(uint32_t p, uint32_t v) {
-        const uint32_t w = p >> 2;
-        const uint32_t k4 = (p & 3u) * 4u;
-        const uint32_t tsel = 0x4321u - (0x1111u & ((1u << k4) - 1u));
-        const uint32_t s0 = w > 0u ? 0x3210u : tsel;
-        const uint32_t s1 = w > 1u ? 0x3210u : (w == 1u ? tsel : 0x4321u);
-        const uint32_t s2 = w > 2u ? 0x3210u : (w == 2u ? tsel : 0x4321u);
-        const uint32_t s3 = w == 3u ? tsel : 0x4321u;
-        const uint32_t g0 = __byte_perm(f0, f1, s0), g1 = __byte_perm(f1, f2, s1);
-        const uint32_t g2 = __byte_perm(f2, f3, s2), g3 = __byte_perm(f3, v, s3);
-        const uint32_t n0 = __byte_perm(m0, m1, s0), n1 = __byte_perm(m1, m2, s1);
-        const uint32_t n2 = __byte_perm(m2, m3, s2), n3 = __byte_perm(m3, 0x80u, s3);
-        f0 = g0; f1 = g1; f2 = g2; f3 = g3;
-        m0 = n0; m1 = n1; m2 = n2; m3 = n3;
-    }
-};
-
-// ---------------------------------------------------------------------------
 // 2. connectivity kernel
 // ---------------------------------------------------------------------------
 
@@ -349,7 +297,8 @@ __device__ __forceinline__ uint32_t bar_empty(uint32_t c) { return 2u + c; }
 // window has passed (its last words are in registers).
 template <int G>
 __device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, uint32_t* __restrict__ ring,
-                           uint32_t* __restrict__ recs, uint32_t* __restrict__ counts, uint32_t pair, int lane) {
+                           uint32_t* __restrict__ recs, uint32_t* __restrict__ counts, uint32_t pair, int lane,
+                           const uint4* __restrict__ mtf_masks) {
     const uint32_t n_local = L.d.counts0 & 0xFFFFu;
     const uint32_t n_tris = L.d.counts0 >> 16;
     const uint32_t ib = max(1u, 32u - __clz(n_local));
@@ -370,9 +319,9 @@ __device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
     if (act) win.seek(L.d.start_bit + 48u);
     uint32_t strips_left = L.d.n_strips;
     uint32_t tok_left = 0u, tok_idx = 0u, tris = 0u;
-    Fifo fifo;
+    MtfFifo fifo;
     bool bad = false;
-    bool running = act && strips_left > 0u;
+    bool live = act && strips_left > 0u;  // false for good once the lane's strips are read (or it failed)
     // A strip of length len takes len + 2 tokens and adds len triangles (one
     // for len 0), and a lane stops once its triangles would pass n_tris, so
     // n_tris + 2 n_strips iterations finish (or fail) every lane: the warp
@@ -389,45 +338,49 @@ __device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
         // 2 and 16 are slower)
 #pragma unroll 4
         for (uint32_t i = 0; i < n; i++) {
-            uint32_t rec = 0u;
-            if (running) {
-                // a 32-bit window holds a strip header (16 bits) plus the next
-                // token (at most 1 + 9 bits), or an edge code plus a token
-                const uint32_t x0 = win.peek();
-                uint32_t used = 0u;
-                const bool hdr = tok_left == 0u;  // strip header (paradelta_v5_dup.py:519)
-                const uint32_t len = x0 >> 16;
-                const uint32_t sbody = len > 1u ? len - 1u : 0u;
-                tok_left = hdr ? 3u + sbody : tok_left;
-                tok_idx = hdr ? 0u : tok_idx;
-                strips_left -= hdr ? 1u : 0u;
-                tris += hdr ? 1u + sbody : 0u;
-                used += hdr ? 16u : 0u;
-                uint32_t x = hdr ? (x0 << 16) : x0;
-                const bool body = tok_idx >= 3u;
-                const uint32_t ec = x >> 31;  // edge code of a strip-body token (:528)
-                x = body ? (x << 1) : x;
-                used += body ? 1u : 0u;
-                const bool raw = (x >> 31) != 0u;
-                const uint32_t rid = (x << 1) >> (32u - ib);
-                const uint32_t fi = (x << 1) >> 27;
-                used += raw ? 1u + ib : 6u;
-                // decode_dup raises IndexError on both (FIFO index, local id)
-                const bool invalid = (raw ? rid >= n_local : fi >= fifo.len) | (tris > n_tris);
-                // (find also for FIFO tokens, whose position is known: selecting
-                // between the two compiles to a divergent branch, which costs more)
-                const uint32_t v = raw ? (rid & 0xFFu) : fifo.at((16u - fifo.len + fi) & 15u);
-                const uint32_t at = fifo.find(v);
-                const uint32_t rm = at < 16u ? at : (fifo.len >= 15u ? 0u : 15u - fifo.len);
-                fifo.remove_append(rm, v);
-                fifo.len += ((at == 16u) & (fifo.len < 16u)) ? 1u : 0u;
-                rec = invalid ? 0u : (v | 0x100u | ((body ? ec : 0u) << 9) | (min(tok_idx, 3u) << 10));
-                tok_idx++;
-                tok_left--;
-                win.advance(used);
-                bad = bad | invalid | (win.pos > end);
-                running = !bad & ((tok_left | strips_left) != 0u);
-            }
+            // No branch per token, so consecutive tokens' chains can overlap:
+            // a lane that has finished (or failed) keeps running the body on
+            // whatever bits follow, but its window no longer moves and its
+            // records are empty.
+            // A 32-bit window holds a strip header (16 bits) plus the next
+            // token (at most 1 + 9 bits), or an edge code plus a token.
+            const uint32_t x0 = win.peek();
+            uint32_t used = 0u;
+            const bool hdr = tok_left == 0u;  // strip header (paradelta_v5_dup.py:519)
+            const uint32_t len = x0 >> 16;
+            const uint32_t sbody = len > 1u ? len - 1u : 0u;
+            tok_left = hdr ? 3u + sbody : tok_left;
+            tok_idx = hdr ? 0u : tok_idx;
+            strips_left -= hdr ? 1u : 0u;
+            tris += (hdr & live) ? 1u + sbody : 0u;  // the count the lane is checked against
+            used += hdr ? 16u : 0u;
+            uint32_t x = hdr ? (x0 << 16) : x0;
+            const bool body = tok_idx >= 3u;
+            const uint32_t ec = x >> 31;  // edge code of a strip-body token (:528)
+            x = body ? (x << 1) : x;
+            used += body ? 1u : 0u;
+            const bool raw = (x >> 31) != 0u;
+            const uint32_t rid = (x << 1) >> (32u - ib);
+            const uint32_t fi = (x << 1) >> 27;
+            used += raw ? 1u + ib : 6u;
+            // decode_dup raises IndexError on both (FIFO index, local id)
+            const bool invalid = (raw ? rid >= n_local : fi >= fifo.len) | (tris > n_tris);
+            // the FIFO as a move-to-front register: a FIFO token's entry at
+            // depth len-1-fi, a raw id's at the depth find() gives, or none
+            // (a new id enters, the oldest leaving a full FIFO)
+            const uint32_t sd = (fifo.len - 1u - fi) & 15u;
+            const uint32_t v = raw ? (rid & 0xFFu) : fifo.at(sd);
+            const uint32_t at = raw ? fifo.find(v) : sd;
+            const bool fresh = at == 16u;
+            fifo.mtf_masked(v, mtf_masks[fresh ? min(fifo.len, 15u) : at]);
+            fifo.len += (fresh & (fifo.len < 16u)) ? 1u : 0u;
+            const uint32_t rec = (invalid | !live) ? 0u
+                                                   : (v | 0x100u | ((body ? ec : 0u) << 9) | (min(tok_idx, 3u) << 10));
+            tok_idx++;
+            tok_left--;
+            win.advance(live ? used : 0u);
+            bad = bad | (live & (invalid | (win.pos > end)));
+            live = live & !bad & ((tok_left | strips_left) != 0u);
             rc[i * 32u] = rec;
         }
         it += n;
@@ -438,14 +391,14 @@ __device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
         if (done) break;
         // refill (the previous refill has had a record chunk to land)
         cp_async_wait_all();
-        if (running && kLaneChunkWords * req < win.next_word() - rot + 33u) {
+        if (live && kLaneChunkWords * req < win.next_word() - rot + 33u) {
             ring_fetch(ring, src, avail, rot, req);
             req++;
         }
         cp_async_commit();
     }
     cp_async_wait_all();  // no copy may land after the CTA's shared memory is gone
-    bad = bad | running;      // cannot happen: the count bounds every lane
+    bad = bad | live;  // cannot happen: the count bounds every lane
     // take the assembler's remaining chunk releases: the ring and the
     // barriers are clean
     for (uint32_t j = k >= 2u ? k - 2u : 0u; j < k; j++) pair_bar<G, false>(pair, bar_empty(j & 1u));
@@ -532,7 +485,7 @@ __device__ void conn_assemble(const DecodeArgs& a, const GroupLane& L, bool act,
 // every lane streams its own meshlet, so no meshlet is too large.
 template <int G>
 __device__ __forceinline__ void conn_group(const DecodeArgs& a, uint32_t g, uint32_t pair, bool parser, int lane,
-                                           uint8_t* base) {
+                                           uint8_t* base, const uint4* mtf_masks) {
     uint32_t* rings = reinterpret_cast<uint32_t*>(base);
     uint32_t* recs = rings + 32u * kLaneRingWords;
     uint32_t* counts = recs + 2u * kChunk * 32u;
@@ -548,7 +501,7 @@ __device__ __forceinline__ void conn_group(const DecodeArgs& a, uint32_t g, uint
     }
     if (!__any_sync(kFull, ok)) return;  // both warps see the same lanes
     if (parser) {
-        conn_parse<G>(a, L, ok, rings + lane * kLaneRingWords, recs, counts, pair, lane);
+        conn_parse<G>(a, L, ok, rings + lane * kLaneRingWords, recs, counts, pair, lane, mtf_masks);
     } else {
         conn_assemble<G>(a, L, ok, seen, tring, wring, recs, counts, pair, lane);
     }
@@ -560,6 +513,8 @@ __device__ __forceinline__ void conn_group(const DecodeArgs& a, uint32_t g, uint
 template <int G>
 __global__ void __launch_bounds__(G * 64) conn_kernel(DecodeArgs a) {
     extern __shared__ __align__(128) uint8_t smem[];
+    __shared__ uint4 mtf_masks[16];
+    if (threadIdx.x < 16u) mtf_masks[threadIdx.x] = mtf_mask_row(threadIdx.x);
     const uint32_t pair = threadIdx.x >> 6;
     const bool parser = ((threadIdx.x >> 5) & 1u) == 0u;
     const int lane = threadIdx.x & 31;
@@ -568,7 +523,7 @@ __global__ void __launch_bounds__(G * 64) conn_kernel(DecodeArgs a) {
     const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
     const uint32_t f = blockIdx.x * G + pair;
     if (f >= n_groups) return;  // both warps of the pair
-    conn_group<G>(a, group_at(f, n_groups), pair, parser, lane, smem + pair * conn_pair_bytes());
+    conn_group<G>(a, group_at(f, n_groups), pair, parser, lane, smem + pair * conn_pair_bytes(), mtf_masks);
 }
 
 // ---------------------------------------------------------------------------
@@ -944,6 +899,8 @@ __global__ void __launch_bounds__(128, kMinBlocks) flow_kernel(DecodeArgs a, uin
     extern __shared__ __align__(128) uint8_t smem[];
     __shared__ uint32_t s_claim[2];
     __shared__ uint32_t s_group;
+    __shared__ uint4 mtf_masks[16];
+    if (threadIdx.x < 16u) mtf_masks[threadIdx.x] = mtf_mask_row(threadIdx.x);
     const uint32_t warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const bool failed = *reinterpret_cast<volatile unsigned long long*>(&a.status->err) != 0ull;
@@ -966,7 +923,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) flow_kernel(DecodeArgs a, uin
             }
             if (f >= n_groups) break;
             const uint32_t g = group_at(f, n_groups);
-            conn_group<2>(a, g, pair, parser, lane, base);
+            conn_group<2>(a, g, pair, parser, lane, base, mtf_masks);
             __threadfence();  // this thread's outputs, before the list entry
             claim_bar(pair);  // both warps are done with the group
             if (!parser && lane == 0) st_release_u32(done_entry(a, atomicAdd(&a.status->done_tail, 1u)), g + 1u);
