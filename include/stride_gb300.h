@@ -65,6 +65,14 @@ typedef struct {
                             or the group kernel: persistent 2 or 3), 3 with
                             the two-kernel shapes (persistent 0 or 1), 0 for
                             an empty stream                                   */
+    float g_min[3];      /* header g_min, g_range: a position's normalised   */
+    float g_range[3];    /* value is g_min + q / (2^g_bits - 1) * g_range     */
+    uint32_t shared_bytes;      /* stride_info only, after a decode: dynamic
+                                   shared memory per CTA of the decode's main
+                                   kernel (fused, group or vertex kernel)     */
+    uint32_t persistent_blocks; /* ... and its CTAs; the reference's
+                                   _shared_bytes / _persistent_blocks
+                                   (utils/paradelta_v5_cuda.py:656-683)      */
 } stride_info_t;
 
 /* Launch shape of the decode kernel (the autotuner's search space). */
@@ -194,6 +202,15 @@ int stride_decode_timed(stride_handle* h, void* stream, uint32_t* d_idx, float* 
 /* Launch shape for this handle's decodes (defaults are used until set). */
 int stride_set_config(stride_handle* h, const stride_launch_cfg* cfg);
 
+/* No counterpart in the reference.  SM clocks each device wait of this
+ * handle's decodes may spin -- a bulk copy's mbarrier, the fused kernel's
+ * wait for a finished connectivity group -- before the decode gives up with
+ * STRIDE_ERR_TIMEOUT (default 2^31, about a second; 0 gives up at the first
+ * unsuccessful check).  The waits are bounded either way; a small limit
+ * lets a test see the timeout path report its status while the context
+ * stays usable for the next decode. */
+int stride_set_wait_limit(stride_handle* h, uint64_t clocks);
+
 void stride_close(stride_handle* h);
 
 /* ---- decode without device allocation ------------------------------------
@@ -208,9 +225,14 @@ void stride_close(stride_handle* h);
  * streams of about 10 million triangles; larger ones are rejected with
  * STRIDE_ERR_NOMEM before any device work).  Calls nothing that allocates.
  * Synchronous: returns after the decode finished on `stream`, with its
- * status.  The first call on a device looks up the array's device address;
- * make that first call before any stream capture.  All calls share the
- * array: decodes that overlap on the GPU race and must be serialised. */
+ * status.  The first call on a device looks up the array's device address,
+ * and that is where the runtime loads this library's device code on the
+ * device and reserves the array (it can fail there with STRIDE_ERR_CUDA if
+ * the device is out of memory): make that first call at start-up, before
+ * any stream capture and before the frame loop.  A device reset
+ * (cudaDeviceReset) releases the array; the next call on that device
+ * reserves it again like a first call.  All calls share the array:
+ * decodes that overlap on the GPU race and must be serialised. */
 int stride_decode_static(const uint8_t* data, size_t len, void* stream, uint32_t* d_idx, float* d_pos);
 
 /* ---- many meshes, one launch ---------------------------------------------

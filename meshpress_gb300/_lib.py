@@ -45,7 +45,9 @@ class StrideInfo(ctypes.Structure):
     _fields_ = [("n_meshlets", ctypes.c_uint32), ("g_bits", ctypes.c_uint32 * 3),
                 ("n_v", ctypes.c_uint64), ("n_t", ctypes.c_uint64), ("nbytes", ctypes.c_uint64),
                 ("center", ctypes.c_float * 3), ("scale", ctypes.c_float),
-                ("pred_n", ctypes.c_int32 * 9), ("pred_k", ctypes.c_int32 * 3), ("kernels", ctypes.c_uint32)]
+                ("pred_n", ctypes.c_int32 * 9), ("pred_k", ctypes.c_int32 * 3), ("kernels", ctypes.c_uint32),
+                ("g_min", ctypes.c_float * 3), ("g_range", ctypes.c_float * 3),
+                ("shared_bytes", ctypes.c_uint32), ("persistent_blocks", ctypes.c_uint32)]
 
 
 class LaunchCfg(ctypes.Structure):
@@ -104,6 +106,7 @@ SIGNATURES = [
     ("stride_meshlet_bounds", _I, [_P, _P, _P, _P]),
     ("stride_cull_meshlets", _I, [_P, ctypes.c_uint32, _P, _P, _P, _P]),
     ("stride_set_config", _I, [_P, ctypes.POINTER(LaunchCfg)]),
+    ("stride_set_wait_limit", _I, [_P, _U64]),
     ("stride_close", None, [_P]),
     ("stride_decode_static", _I, [_P, _SZ, _P, _P, _P]),
     ("stride_batch_create", _I, [_P, _P, _U32, ctypes.POINTER(_P)]),

@@ -18,6 +18,8 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <new>
+#include <stdexcept>
 #include <vector>
 
 #include "stride_common.cuh"
@@ -443,7 +445,21 @@ struct P5Host {
     uint64_t refs = 0;
 };
 
+static int p5_host_parse_sized(const uint8_t* data, size_t len, P5Host& H);
+
+// The host parse with its host allocations' failures turned into an error
+// code (no exception may cross the C ABI).
 static int p5_host_parse(const uint8_t* data, size_t len, P5Host& H) {
+    try {
+        return p5_host_parse_sized(data, len, H);
+    } catch (const std::bad_alloc&) {
+        return fail(STRIDE_ERR_NOMEM, "host memory for the PLDT v5 tables");
+    } catch (const std::length_error&) {
+        return fail(STRIDE_ERR_NOMEM, "host memory for the PLDT v5 tables");
+    }
+}
+
+static int p5_host_parse_sized(const uint8_t* data, size_t len, P5Host& H) {
     pldt5_info_t& info = H.info;
     HostBits r{data, 8ull * len, 0, false};
     if (8ull * len < kP5HeaderBits) return fail(STRIDE_ERR_TRUNCATED, "PLDT v5 header past the end");
@@ -471,7 +487,10 @@ static int p5_host_parse(const uint8_t* data, size_t len, P5Host& H) {
     // boundary table (parse_globals_v5, :538-560), positions in float64 like
     // the CPU decoder (:322-336)
     const uint64_t nb = info.n_boundary;
-    if (nb > 8ull * len) return fail(STRIDE_ERR_TRUNCATED, "boundary table past the end");
+    // every row after the first takes at least one bit per axis (a Rice
+    // codeword's terminator): the header's count is bounded by the bits
+    // left before anything is sized from it
+    if (nb > (8ull * len - r.pos) / 3ull + 1ull) return fail(STRIDE_ERR_TRUNCATED, "boundary table past the end");
     std::vector<double>& rows0 = H.rows0;
     rows0.assign(3 * nb, 0.0);
     {
@@ -531,8 +550,8 @@ static int p5_host_parse(const uint8_t* data, size_t len, P5Host& H) {
         rows += n_int;
         tris += n_tris;
         refs += n_bnd;
-        if (rows > 0xFFFFFFFFull || tris > 0x55555555ull)
-            return fail(STRIDE_ERR_UNSUPPORTED, "more than 2^32 rows or 2^32 indices");
+        if (rows > 0xFFFFFFFFull || tris > 0x55555555ull || refs > 0xFFFFFFFFull)
+            return fail(STRIDE_ERR_UNSUPPORTED, "more than 2^32 rows, indices or boundary references");
     }
     info.n_v = rows;
     info.n_t = tris;

@@ -181,6 +181,8 @@ struct stride_handle {
     cudaEvent_t done = nullptr;
     bool launched = false;
     LaunchCfg cfg;
+    long long wait_clocks = 1ll << 31;  // DecodeArgs::wait_clocks of this handle's decodes
+    uint32_t launch_smem = 0, launch_grid = 0;  // the last decode's main kernel
     // stride_decode_host: copy streams and the events they wait on
     cudaStream_t copy[2] = {nullptr, nullptr};
     cudaEvent_t conn_done = nullptr, vert_done = nullptr, copied[2] = {nullptr, nullptr};
@@ -317,6 +319,8 @@ static void fill_info(const MeshParams& p, size_t len, int persistent, stride_in
     for (int i = 0; i < 3; i++) {
         info->g_bits[i] = p.g_bits[i];
         info->center[i] = static_cast<float>(p.dq[i].center);
+        info->g_min[i] = static_cast<float>(p.dq[i].gmin);
+        info->g_range[i] = static_cast<float>(p.dq[i].grange);
         info->pred_k[i] = p.pred_k[i];
     }
     for (int i = 0; i < 9; i++) info->pred_n[i] = p.pred_n[i];
@@ -393,11 +397,14 @@ int stride_reload(stride_handle* h, const uint8_t* data, size_t len, void* strea
 int stride_info(const stride_handle* h, stride_info_t* info) {
     if (!h || !info) return fail(STRIDE_ERR_ARG, "null argument");
     fill_info(h->params, h->len, h->cfg.persistent, info);
+    info->shared_bytes = h->launch_smem;
+    info->persistent_blocks = h->launch_grid;
     return STRIDE_OK;
 }
 
 static DecodeArgs handle_args(stride_handle* h, uint32_t* d_idx, float* d_pos, int32_t* d_codes) {
     DecodeArgs a;
+    a.wait_clocks = h->wait_clocks;
     a.arena = h->d_blob;
     a.meshes = h->d_params;
     a.meshlet_mesh = nullptr;
@@ -429,6 +436,7 @@ int stride_decode_timed(stride_handle* h, void* stream, uint32_t* d_idx, float* 
     void* evp[4] = {ev[0], ev[1], ev[2], ev[3]};
     int rc = enqueue_decode(handle_args(h, d_idx, d_pos, nullptr), h->cfg, stream, evp);
     if (rc == STRIDE_OK) {
+        last_launch(&h->launch_smem, &h->launch_grid);
         cudaEventRecord(h->done, static_cast<cudaStream_t>(stream));
         h->launched = true;
         cudaError_t e = cudaEventSynchronize(ev[3]);
@@ -452,6 +460,7 @@ int stride_decode(stride_handle* h, void* stream, uint32_t* d_idx, float* d_pos,
         return fail(STRIDE_ERR_ARG, "index output must be 16-byte aligned, positions and codes 4-byte aligned");
     const int rc = enqueue_decode(handle_args(h, d_idx, d_pos, d_codes), h->cfg, stream);
     if (rc) return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    last_launch(&h->launch_smem, &h->launch_grid);
     cudaError_t e = cudaEventRecord(h->done, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
     h->launched = true;
@@ -577,6 +586,12 @@ int stride_decode_host(stride_handle* h, void* stream, uint32_t* h_idx, float* h
     if (e == cudaSuccess) e = cudaEventRecord(h->done, s);
     if (e != cudaSuccess) return cuda_fail(e, "stride_decode_host copy");
     return stride_status(h, 1, nullptr);
+}
+
+int stride_set_wait_limit(stride_handle* h, uint64_t clocks) {
+    if (!h) return fail(STRIDE_ERR_ARG, "null handle");
+    h->wait_clocks = static_cast<long long>(clocks > (1ull << 62) ? (1ull << 62) : clocks);
+    return STRIDE_OK;
 }
 
 int stride_set_config(stride_handle* h, const stride_launch_cfg* c) {

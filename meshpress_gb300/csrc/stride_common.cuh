@@ -133,6 +133,10 @@ struct DecodeArgs {
     const uint32_t* lut_meshes;      // device: indices of those meshes
     uint32_t n_lut_meshes;
     uint32_t lut_max;                // largest table set (floats) of one mesh
+    // SM clocks a device wait (a bulk copy's mbarrier, the fused kernel's
+    // completion list) spins before it gives up with STRIDE_ERR_TIMEOUT
+    // (about a second by default; 0 gives up at the first unsuccessful check)
+    long long wait_clocks = 1ll << 31;
 };
 
 // Host: assigns table offsets (has_lut, lut_off) to the meshes that get
@@ -179,6 +183,13 @@ int enqueue_cull(const float* bounds, uint32_t n, const Planes& planes, uint32_t
 // relative to it.
 int enqueue_side_table(const MeshletDesc* descs, uint32_t n, unsigned long long* resid_bit, uint16_t* sub_offs,
                        void* stream);
+
+// Geometry of the decode's main kernel (the fused, group or vertex kernel)
+// as last launched by this host thread: dynamic shared memory per CTA and
+// CTAs in the grid (the reference class exposes the same two numbers as
+// _shared_bytes and _persistent_blocks, utils/paradelta_v5_cuda.py:656-683).
+void note_launch(uint32_t smem_bytes, uint32_t grid);
+void last_launch(uint32_t* smem_bytes, uint32_t* grid);
 
 // The group kernel (stride_group.cu): launch for `a` on `stream`, and its
 // shared memory per CTA.

@@ -180,11 +180,27 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
     return ok != 0u;
 }
 
-// Bounded wait (about a second of SM clocks); false on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
+// Non-blocking check of the phase.
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t phase) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(phase)
+        : "memory");
+    return ok != 0u;
+}
+
+// Bounded wait (`limit` SM clocks, DecodeArgs::wait_clocks); false on
+// timeout.  The first check does not block, so a limit of 0 gives up as
+// soon as the phase is found incomplete.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, long long limit) {
+    if (mbar_test_wait(bar, phase)) return true;
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, phase)) {
-        if (clock64() - t0 > (1ll << 31)) return false;
+        if (clock64() - t0 > limit) return false;
     }
     return true;
 }

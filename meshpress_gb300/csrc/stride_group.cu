@@ -749,6 +749,7 @@ cudaError_t launch_group_t(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream
     if (grid > cap) grid = cap;
     if (grid == 0) return cudaSuccess;
     group_kernel<kWide><<<grid, 32u * warps, smem, s>>>(a, warps);
+    note_launch(static_cast<uint32_t>(smem), grid);
     return cudaGetLastError();
 }
 

@@ -775,10 +775,10 @@ __device__ __forceinline__ bool vert_group(const DecodeArgs& a, uint32_t g, uint
                 if (act && ssz)
                     bulk_copy(reinterpret_cast<uint8_t*>(stage) + dst_off, a.arena + src16, ssz, bar);
             }
-            const bool timed_out = !mbar_wait(bar, phase);
+            const bool timed_out = !mbar_wait(bar, phase, a.wait_clocks);
             if (__syncthreads_or(timed_out)) {
                 if (threadIdx.x == 0) report(a.status, kErrTimeout, L.m);
-                mbar_wait(bar, phase);  // let the copies land before the CTA exits
+                mbar_wait(bar, phase, 1ll << 31);  // let the copies land before the CTA exits
                 return false;
             }
             phase ^= 1u;
@@ -863,7 +863,7 @@ __device__ __forceinline__ void claim_bar(uint32_t pair) {
 }
 
 // The next group of the vertex phase: the next completion-list entry,
-// waited for (bounded, about a second of SM clocks).  n_groups when the list
+// waited for (bounded: DecodeArgs::wait_clocks, about a second by default).  n_groups when the list
 // is used up, the decode has failed, or the wait ran out (reported).
 __device__ uint32_t next_done_group(const DecodeArgs& a, uint32_t n_groups) {
     const uint32_t i = atomicAdd(&a.status->work_vert, 1u);
@@ -874,7 +874,7 @@ __device__ uint32_t next_done_group(const DecodeArgs& a, uint32_t n_groups) {
         const uint32_t v = ld_acquire_u32(e);
         if (v != 0u) return v - 1u < n_groups ? v - 1u : n_groups;
         if (*reinterpret_cast<volatile unsigned long long*>(&a.status->err) != 0ull) return n_groups;
-        if (clock64() - t0 > (1ll << 31)) {
+        if (clock64() - t0 > a.wait_clocks) {
             report(a.status, kErrTimeout, 32u * i);
             return n_groups;
         }
@@ -1031,6 +1031,7 @@ cudaError_t launch_vert(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t 
     const uint32_t grid = grid_for(vert_kernel<kWide>, 96, smem, cfg, n_groups, 1, occ);
     if (grid == 0) return cudaSuccess;
     vert_kernel<kWide><<<grid, 96, smem, s>>>(a, cfg.stage_bytes, cfg.code_bytes, cfg.persistent);
+    note_launch(static_cast<uint32_t>(smem), grid);
     return cudaGetLastError();
 }
 
@@ -1054,6 +1055,7 @@ cudaError_t launch_flow(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t 
     const uint32_t grid = grid_for(flow_kernel<kWide, kMinBlocks>, 128, smem, cfg, n_groups, 1, occ);
     if (grid == 0) return cudaSuccess;
     flow_kernel<kWide, kMinBlocks><<<grid, 128, smem, s>>>(a, cfg.stage_bytes, cfg.code_bytes);
+    note_launch(static_cast<uint32_t>(smem), grid);
     return cudaGetLastError();
 }
 
@@ -1084,6 +1086,20 @@ cudaError_t launch_pair(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t 
 }
 
 }  // namespace
+
+namespace {
+thread_local uint32_t t_launch_smem = 0, t_launch_grid = 0;
+}  // namespace
+
+void note_launch(uint32_t smem_bytes, uint32_t grid) {
+    t_launch_smem = smem_bytes;
+    t_launch_grid = grid;
+}
+
+void last_launch(uint32_t* smem_bytes, uint32_t* grid) {
+    *smem_bytes = t_launch_smem;
+    *grid = t_launch_grid;
+}
 
 size_t conn_smem_bytes(const LaunchCfg& cfg) {
     return static_cast<size_t>(conn_pairs(cfg.warps_per_cta)) * conn_pair_bytes();

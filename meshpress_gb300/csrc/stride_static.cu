@@ -38,13 +38,25 @@ uint8_t* g_static_addr[64] = {nullptr};
 // Device address of the array on the current device.  The host-side symbol
 // is only a stand-in for the device object, so the address must come from
 // cudaGetSymbolAddress with the device current; it is looked up once per
-// device and cached.
+// device and cached.  That first lookup is also where the runtime loads the
+// library's device code on the device (lazy module loading) and so reserves
+// the array's memory.  A cached address is checked on every call: after a
+// cudaDeviceReset the device's context -- and the array with it -- is
+// gone, and the address is looked up again in the new context.
 int static_scratch(uint8_t** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
     if (dev < 0 || dev >= 64) return fail(STRIDE_ERR_ARG, "device ordinal %d out of range", dev);
     std::lock_guard<std::mutex> lock(g_static_mu);
+    if (g_static_addr[dev]) {
+        cudaPointerAttributes at;
+        if (cudaPointerGetAttributes(&at, g_static_addr[dev]) != cudaSuccess || at.type != cudaMemoryTypeDevice ||
+            at.device != dev) {
+            cudaGetLastError();           // clear the query's error, if any
+            g_static_addr[dev] = nullptr;  // the context was reset: look the address up again
+        }
+    }
     if (!g_static_addr[dev]) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_static_scratch);

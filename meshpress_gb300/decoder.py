@@ -37,9 +37,14 @@ def _stream_handle(stream=None) -> int:
 class ParaDeltaV5GpuDecoder:
     """GPU decoder for one STRIDE (DPR4 v3) stream.
 
-    Attributes kept from the reference: ``n_meshlets``, ``n_v_total``,
-    ``n_t_total``, ``meshlets_per_block`` (accepted for compatibility; the
-    reference kernel ignores it too, utils/paradelta_v5_cuda.py:259-260).
+    Attributes kept from the reference (utils/paradelta_v5_cuda.py:597-684,
+    read by scripts/bench_stride_decode_sweep.py:53-79): ``n_meshlets``,
+    ``n_v_total``, ``n_t_total``, ``meshlets_per_block`` (accepted for
+    compatibility; the reference kernel ignores it too, :259-260), ``d_buf``
+    (the stream on the device, uint8), ``d_verts_norm`` (normalised
+    positions of the last ``decode(normalised=True)``), ``d_tris``,
+    ``_shared_bytes`` and ``_persistent_blocks`` (shared memory per CTA and
+    CTAs of the last decode's main kernel).
     """
 
     def __new__(cls, data: bytes = b"", meshlets_per_block: int = 1):
@@ -70,7 +75,34 @@ class ParaDeltaV5GpuDecoder:
         self.g_bits = tuple(int(b) for b in info.g_bits)
         self.d_verts = None
         self.d_tris = None
+        self.d_verts_norm = None
+        self._d_buf = None
         self._device = torch.cuda.current_device()
+
+    # -- reference attributes --------------------------------------------------
+    @property
+    def d_buf(self):
+        """The encoded stream on the device (torch.uint8), made on first use."""
+        if self._d_buf is None:
+            torch = _torch()
+            self._d_buf = torch.frombuffer(bytearray(self._data), dtype=torch.uint8).to(f"cuda:{self._device}")
+        return self._d_buf
+
+    def _launch_info(self):
+        info = _lib.StrideInfo()
+        _lib.check(self._lib.stride_info(self._h, ctypes.byref(info)), "stride_info")
+        return info
+
+    @property
+    def _shared_bytes(self) -> int:
+        """Dynamic shared memory per CTA of the last decode's main kernel
+        (0 before the first decode)."""
+        return int(self._launch_info().shared_bytes)
+
+    @property
+    def _persistent_blocks(self) -> int:
+        """CTAs of the last decode's main kernel (0 before the first decode)."""
+        return int(self._launch_info().persistent_blocks)
 
     # -- launch configuration ------------------------------------------------
     def set_launch_config(self, cfg: _lib.LaunchCfg):
@@ -155,13 +187,33 @@ class ParaDeltaV5GpuDecoder:
         self.decode_into(tris, verts, stream=stream, check=check)
         return tris, verts
 
-    def decode(self, *, stream=None, check: bool = True):
+    def decode(self, *, stream=None, check: bool = True, normalised: bool = False):
         """Reference order: -> (positions (n_v, 3) float32, triangles (n_t, 3))
-        as CUDA tensors (the reference returns normalised positions and int32
-        triangles, :712; this decoder returns world-space positions and
-        uint32 triangles)."""
-        tris, verts = self.decode_to_device(stream=stream, check=check)
-        return verts, tris
+        as CUDA tensors.  By default world-space positions and uint32
+        triangles; ``normalised=True`` returns what the reference's decode()
+        returns (:686-712): positions before ``* scale + center`` --
+        float32(g_min + q / (2^g_bits - 1) * g_range), the float64 expression
+        of decode_dup (encoder/paradelta_v5_dup.py:607-616) -- kept in
+        ``d_verts_norm``, and the triangles as int32."""
+        if not normalised:
+            tris, verts = self.decode_to_device(stream=stream, check=check)
+            return verts, tris
+        torch = _torch()
+        tris, verts = self._outputs()
+        codes = torch.empty((self.n_v_total, 3), dtype=torch.int32, device=verts.device)
+        self.decode_into(tris, verts, codes=codes, stream=stream, check=check)
+        s = stream if stream is not None else torch.cuda.current_stream()
+        with torch.cuda.stream(s):
+            vn = torch.empty((self.n_v_total, 3), dtype=torch.float64, device=verts.device)
+            for d in range(3):
+                gmin, grange, bits = float(self.info.g_min[d]), float(self.info.g_range[d]), int(self.g_bits[d])
+                if bits == 0:
+                    vn[:, d] = gmin
+                else:
+                    # one operation per step, in decode_dup's order, each rounded in float64
+                    vn[:, d] = (codes[:, d].double() / float((1 << bits) - 1)) * grange + gmin
+            self.d_verts_norm = vn.float()
+        return self.d_verts_norm, tris.view(torch.int32)
 
     def decode_to_host(self, out=None, *, stream=None):
         """-> (positions np.float32 (n_v, 3), triangles np.uint32 (n_t, 3)),

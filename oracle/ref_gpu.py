@@ -32,7 +32,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_DIR = os.path.join(HERE, "_ref")
 CUBIN = os.path.join(REF_DIR, "stride_dup_decode.cubin")
 ENTRY = os.path.join(REF_DIR, "stride_dup_decode.entry")
-REF_SRC = "/root/reference/bench_cpp/stride_dup_decode_bench.cu"
+REFERENCE = os.environ.get("MESHPRESS_REFERENCE", "/root/reference")  # the reference checkout
+REF_SRC = os.path.join(REFERENCE, "bench_cpp", "stride_dup_decode_bench.cu")
 
 
 def build(force: bool = False) -> bool:

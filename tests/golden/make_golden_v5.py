@@ -33,7 +33,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
-REFERENCE = "/root/reference"
+REFERENCE = os.environ.get("MESHPRESS_REFERENCE", "/root/reference")  # the reference checkout
 
 sys.path.insert(0, REPO)
 from meshpress_gb300 import synth  # noqa: E402

@@ -56,7 +56,8 @@ def test_encoder_rejects_bad_input():
         encoder.encode(V, T, predictor="nope")
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/encoder"), reason="reference checkout not present")
+@pytest.mark.skipif(not os.path.isdir(os.path.join(os.environ.get("MESHPRESS_REFERENCE", "/root/reference"), "encoder")),
+                    reason="reference checkout not present")
 def test_reference_decoder_accepts_project_encoder_output():
     """The reference's own decode_dup reads the project encoder's bytes and
     returns what the oracle returns."""

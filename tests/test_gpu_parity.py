@@ -287,3 +287,33 @@ def test_device_side_table_matches_oracle(torch_cuda, name):
     assert np.array_equal(resid.cpu().numpy().astype(np.uint64), st["resid_bit"])
     assert np.array_equal(subs.cpu().numpy().view(np.uint16), st["sub_offs"])
     dec.close()
+
+
+def test_reference_attributes_and_normalised_decode(torch_cuda):
+    """decode(normalised=True) returns what the reference's decode() returns
+    (utils/paradelta_v5_cuda.py:686-712): normalised float32 positions --
+    decode_dup's float64 g_min + q / mx * g_range, rounded once -- and int32
+    triangles; the attributes the reference's sweep script reads exist."""
+    from meshpress_gb300 import ParaDeltaV5GpuDecoder
+    torch = torch_cuda
+    g = _golden.load("grid129_b12")
+    data = g["data"]
+    dec = ParaDeltaV5GpuDecoder(data)
+    vn, tris = dec.decode(normalised=True)
+    torch.cuda.synchronize()
+    assert vn.dtype == torch.float32 and tris.dtype == torch.int32 and dec.d_verts_norm is vn
+    _, oidx, ocodes = oracle.decode(data, with_codes=True)
+    h = oracle.parse_header(data)
+    ref = np.empty(ocodes.shape, np.float64)
+    for d in range(3):
+        mx = (1 << int(h.g_bits[d])) - 1
+        ref[:, d] = float(h.g_min[d]) if mx == 0 else float(h.g_min[d]) + ocodes[:, d].astype(np.float64) / mx * float(h.g_range[d])
+    assert np.array_equal(vn.cpu().numpy().view(np.uint32), ref.astype(np.float32).view(np.uint32))
+    assert np.array_equal(tris.cpu().numpy().astype(np.int64), oidx)
+    # world space, as decode_to_host returns it, is unchanged by the mode
+    opos, _ = oracle.decode(data)
+    verts, _ = dec.decode()
+    assert np.array_equal(verts.cpu().numpy().view(np.uint32), opos.view(np.uint32))
+    assert bytes(dec.d_buf.cpu().numpy()) == data
+    assert dec._shared_bytes > 0 and dec._persistent_blocks > 0
+    dec.close()

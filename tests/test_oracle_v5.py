@@ -120,3 +120,18 @@ def test_host_inspect_rejects():
     bad[table + 4:table + 8] = bad[table:table + 4]
     with pytest.raises(_lib.StrideFormatError):
         _lib.inspect_pldt5(bytes(bad))
+
+
+def test_host_inspect_rejects_a_boundary_count_the_bytes_cannot_hold():
+    """A header claiming 2^31 boundary rows in a short stream is rejected
+    before the host parse sizes any table from it (each row after the first
+    takes at least three bits)."""
+    from meshpress_gb300 import _lib
+    data, _, _, _ = _load("v5_grid33_mv64")
+    bad = bytearray(data)
+    bad[61:65] = (0x7FFFFFFF).to_bytes(4, "big")  # n_boundary, after magic .. n_t (488 bits)
+    with pytest.raises(_lib.StrideFormatError) as err:
+        _lib.inspect_pldt5(bytes(bad))
+    assert err.value.code == _lib.STRIDE_ERR_TRUNCATED
+    h = oracle.parse_header_v5(data)
+    assert int.from_bytes(data[61:65], "big") == h.n_boundary  # the field the test overwrote

@@ -1,8 +1,9 @@
 """Multi-process host logic of bench.py on CPU (gloo, world size 2).
 
-The decode path does not shard across GPUs: every rank decodes its own
-replica (or its own share of a batch's meshes) and the job's step time is the
-slowest rank's.  These tests run that host logic as two gloo ranks.
+The single-mesh workloads run one replica per rank; the batch workload
+gives each rank its own share of the meshes (no exchange).  The job's step
+time is the slowest rank's.  These tests run that host logic as two gloo
+ranks.
 """
 import json
 import os
@@ -37,10 +38,11 @@ def _worker(rank, world, port, q):
         worst = bench.reduce_max(mine)
         bench.barrier()
         value = bench.replica_value(1000, w, worst / 1e3)
-        shard = bench.shard_range(10, r, w)
+        # the batch workload's path: each rank decodes its share of the meshes
+        shard = bench.shard_batch(list(range(10)), r, w)
         got = [None] * w
         dist.all_gather_object(got, list(shard))
-        q.put((rank, r, w, worst, value, got))
+        q.put((rank, r, w, worst, value, got, bench.sharded_value(10, worst / 1e3)))
     finally:
         if dist.is_initialized():
             dist.destroy_process_group()
@@ -57,13 +59,15 @@ def test_two_ranks_max_and_aggregate():
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
-    for rank, r, w, worst, value, got in res:
+    for rank, r, w, worst, value, got, sharded in res:
         assert r == rank and w == world
         assert worst == 2.0  # max over ranks, seen by every rank
         assert value == pytest.approx(1000 * world / 2e-3)
-        # the shares cover every mesh exactly once
+        # the shares cover every mesh exactly once; the job's rate is every
+        # mesh over the slowest rank's time
         flat = sorted(i for s in got for i in s)
         assert flat == list(range(10))
+        assert sharded == pytest.approx(10 / 2e-3)
 
 
 def test_shard_range_edges():
@@ -98,3 +102,20 @@ def test_reference_arm_line_on_small_grid():
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
     assert line["cpu_baseline"]["value"] == line["value"] > 0
     assert line["config"]["triangles"] == 2 * 64 * 64
+
+
+def test_reference_arm_loads_no_product_library():
+    """The reference arm reads the workload's stream from a file (made by a
+    child process when missing) and times the CPU decoder: no library of
+    this repository's product (encoder or GPU decoder) is loaded into it."""
+    env = dict(os.environ)
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        env.pop(k, None)
+    code = ("import sys; sys.path.insert(0, %r); import bench; "
+            "bench.main(['--impl', 'reference', '--steps', '1', '--warmup', '1', '--grid', '33']); "
+            "print('MAPS', 'libstride_encode' in open('/proc/self/maps').read(), "
+            "'libstride_gb300' in open('/proc/self/maps').read())" % REPO)
+    out = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    maps = [ln for ln in out.stdout.splitlines() if ln.startswith("MAPS")]
+    assert maps == ["MAPS False False"]
