@@ -57,6 +57,9 @@ def parse_args(argv=None):
     ap.add_argument("--bits", type=int, default=12)
     ap.add_argument("--grid", type=int, default=2049)
     ap.add_argument("--tune", type=int, default=1, help="autotune the launch shape before timing")
+    ap.add_argument("--shape", default=None,
+                    help="launch shape warps_per_cta,persistent[,stage_bytes,code_bytes] instead of autotuning "
+                         "(single-mesh workloads)")
     ap.add_argument("--batch-meshes", type=int, default=4096)
     ap.add_argument("--rates", default="50,100,200,500,1000,2000", help="serve: Poisson arrival rates (requests/s)")
     ap.add_argument("--serve-host-rate", type=float, default=500.0,
@@ -64,6 +67,9 @@ def parse_args(argv=None):
     ap.add_argument("--serve-seconds", type=float, default=3.0, help="serve: arrivals per rate span this long")
     ap.add_argument("--serve-pool", type=int, default=48, help="serve: distinct encoded blobs drawn from")
     ap.add_argument("--serve-budget-gb", type=int, default=40)
+    ap.add_argument("--serve-burst", default="64,512",
+                    help="serve: saturating passes that queue this many requests at once, then let the server "
+                         "run them ('' = none)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--write-stream", default=None, help=argparse.SUPPRESS)  # encode a workload's stream to a file
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -214,7 +220,7 @@ def measured_peak():
     return 6800.0, "fallback 6.8 TB/s"
 
 
-def kernel_split(kern, fused: bool, stream_bytes: int, n_v: int, n_t: int, persistent: int = 3):
+def kernel_split(kern, fused: bool, stream_bytes: int, n_v: int, n_t: int, persistent: int = 2):
     """Names of the decode's kernels, the dominant one and its algorithmic
     bytes, from the per-kernel times (scan, connectivity, vertex; a one-kernel
     decode's time in the second slot: the group kernel, persistent 3, or the
@@ -409,9 +415,18 @@ def run_single(args):
     stream = torch.cuda.current_stream()
     sh = ctypes.c_void_p(int(stream.cuda_stream))
 
-    # launch shape: autotune over a one-mesh batch, apply to the handle
+    # launch shape: as given, or autotuned over a one-mesh batch; applied to the handle
     launch = None
-    if args.tune:
+    if args.shape:
+        v = [int(x) for x in args.shape.split(",")]
+        c = _lib.LaunchCfg()
+        c.warps_per_cta, c.persistent = v[0], v[1]
+        c.ctas_per_sm = 0
+        c.stage_bytes = v[2] if len(v) > 2 else 16 * 1024
+        c.code_bytes = v[3] if len(v) > 3 else 12 * 1024
+        dec.set_launch_config(c)
+        launch = c.as_dict()
+    elif args.tune:
         from meshpress_gb300.batch import BatchDecoder
         b = BatchDecoder([data])
         best, best_ms = b.autotune(iters=3)
@@ -473,7 +488,7 @@ def run_single(args):
     peak, peak_src = measured_peak()
     k = np.array(kern_ms).mean(axis=0)
     names, dom, dom_bytes = kernel_split(k, int(dec.info.kernels) == 2, len(data), n_v, n_t,
-                                         int(launch["persistent"]) if launch else 3)
+                                         int(launch["persistent"]) if launch else 2)
     achieved = dom_bytes / (k[dom] / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
                 "frac": round(achieved / peak, 4), "traffic": ncu_traffic(names[dom], cfg["workload"]),
@@ -702,8 +717,11 @@ def run_batch(args):
 
 
 def run_serve(args):
-    """Poisson arrivals into the continuous-batching server; one line per
-    arrival rate with p50/p99 latency and aggregate throughput."""
+    """Poisson arrivals into the continuous-batching server, then closed-loop
+    passes that keep a fixed number of requests outstanding (the saturating
+    rate); one line per pass with p50/p99 latency, aggregate throughput,
+    requests per launch and the arena's high-water mark.  Every response is
+    compared with the same mesh decoded alone."""
     import threading
     import torch
     from meshpress_gb300 import ParaDeltaV5GpuDecoder
@@ -736,74 +754,125 @@ def run_serve(args):
         for rid in [warm.submit(x) for x in blobs[:4]]:
             assert warm.wait(rid).ok
             warm.release(rid)
-    runs = [(r, False) for r in rates] + ([(args.serve_host_rate, True)] if args.serve_host_rate > 0 else [])
+    runs = [("rate", r, False) for r in rates]
+    runs += [("rate", args.serve_host_rate, True)] if args.serve_host_rate > 0 else []
+    runs += [("burst", int(q), False) for q in args.serve_burst.split(",") if q.strip()]
     alone_host = None
-    for rate, to_host in runs:
-        n_req = max(20, int(rate * args.serve_seconds))
-        gaps = rng.exponential(1.0 / rate, n_req)
+    for mode, knob, to_host in runs:
+        if mode == "rate":
+            n_req = max(20, int(knob * args.serve_seconds))
+            gaps = rng.exponential(1.0 / knob, n_req)
+        else:  # bursts of `knob` requests, as many in all as the 2000 rps pass
+            n_req = max(1, int(2000 * args.serve_seconds) // knob) * knob
+            gaps = None
         picks = rng.integers(0, len(blobs), n_req)
         if to_host and alone_host is None:
             alone_host = [(t.cpu().numpy(), v.cpu().numpy()) for t, v in alone]
         srv = DecodeServer(args.serve_budget_gb << 30, n_streams=3, max_batch=256, copy_to_host=to_host)
         ids = [None] * n_req
-        lat, ok, failed = [], [0, 0], {}
-        first_submit = [None]
-        last_done = [0.0]
+        ok, failed = [0, 0], {}
+        times = np.zeros((n_req, 3))  # server clock (us): submit, admit, done
+        # device results are compared on the device and read back in chunks
+        # (one synchronisation per chunk), then released
+        pending = []
 
-        def feed():
-            t_next = time.perf_counter()
-            for i in range(n_req):
-                t_next += gaps[i]
-                dt = t_next - time.perf_counter()
-                if dt > 0:
-                    time.sleep(dt)
-                ids[i] = srv.submit(blobs[picks[i]])
+        def settle():
+            if not pending:
+                return
+            flags = torch.stack([f for _, f in pending]).cpu().tolist()
+            for (i, _), bad in zip(pending, flags):
+                ok[1 if bad else 0] += 1
+                srv.release(ids[i])
+            pending.clear()
 
-        th = threading.Thread(target=feed)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        th.start()
-        for i in range(n_req):
-            while ids[i] is None:
-                time.sleep(0.0002)
+        def collect(i):
             r = srv.wait(ids[i])
             if not r.ok:
                 failed[r.status] = failed.get(r.status, 0) + 1
+                srv.release(ids[i])
             elif to_host:
                 at, av = alone_host[picks[i]]
                 good = np.array_equal(r.host_tris.view(np.int32), at) and \
                     np.array_equal(r.host_verts.view(np.int32), av)
                 ok[0 if good else 1] += 1
+                srv.release(ids[i])
             else:
-                good = torch.equal(r.tris.view(torch.int32), alone[picks[i]][0]) and \
-                    torch.equal(r.verts.view(torch.int32), alone[picks[i]][1])
-                ok[0 if good else 1] += 1
-            lat.append(r.latency_ms)
-            if first_submit[0] is None:
-                first_submit[0] = r.t_submit_us
-            last_done[0] = max(last_done[0], r.t_done_us)
-            srv.release(ids[i])
-        th.join()
+                at, av = alone[picks[i]]
+                bad = torch.ne(r.tris.view(torch.int32), at).any() | torch.ne(r.verts.view(torch.int32), av).any()
+                pending.append((i, bad))
+                if len(pending) >= 32:
+                    settle()
+            times[i] = (r.t_submit_us, r.t_admit_us, r.t_done_us)
+
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        if mode == "rate":
+            def feed():
+                t_next = time.perf_counter()
+                for i in range(n_req):
+                    t_next += gaps[i]
+                    dt = t_next - time.perf_counter()
+                    if dt > 0:
+                        time.sleep(dt)
+                    ids[i] = srv.submit(blobs[picks[i]])
+
+            th = threading.Thread(target=feed)
+            th.start()
+            for i in range(n_req):
+                while ids[i] is None:
+                    time.sleep(0.0002)
+                collect(i)
+            th.join()
+        else:
+            # the server holds each burst's requests until all are queued, so
+            # it forms its launches from a full queue (the client's own
+            # per-request cost -- payload copies, checks -- stays outside the
+            # server's busy time measured below)
+            busy_us = 0.0
+            for b0 in range(0, n_req, knob):
+                srv.hold(True)
+                for i in range(b0, b0 + knob):
+                    ids[i] = srv.submit(blobs[picks[i]])
+                srv.hold(False)
+                for i in range(b0, b0 + knob):
+                    collect(i)
+                seg = times[b0:b0 + knob]
+                busy_us += seg[:, 2].max() - seg[:, 1].min()
+        settle()
         wall = time.perf_counter() - t0
         st = srv.stats()
         srv.close()
-        span_s = (last_done[0] - first_submit[0]) / 1e6
+        if mode == "rate":
+            span_s = (times[:, 2].max() - times[:, 0].min()) / 1e6
+            lat = (times[:, 2] - times[:, 0]) / 1e3
+        else:
+            span_s = busy_us / 1e6
+            lat = (times[:, 2] - times[:, 1]) / 1e3
         total_t = int(sum(tris[j] for j in picks))
         if rank == 0:
+            if mode == "rate":
+                name = f"serve_poisson_{int(knob)}rps" + ("_to_host" if to_host else "")
+                load = {"rate_rps": knob}
+            else:
+                name = f"serve_burst{knob}"
+                load = {"burst": knob, "arrivals": "bursts: the server holds each burst of requests until all "
+                                                   "are queued; throughput over the server's busy time (first "
+                                                   "admission to last completion of each burst)"}
             line = {
                 "metric": "served decode latency p50/p99 and throughput", "value": round(total_t / span_s / 1e6, 3),
                 "unit": "M tris/s", "n_gpus": world, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "int32+f32 (exact f64 expression)",
                 "data": "synthetic (seeded mixed meshes)",
-                "config": {"workload": f"serve_poisson_{int(rate)}rps" + ("_to_host" if to_host else ""),
-                           "rate_rps": rate, "requests": n_req,
+                "config": {"workload": name, **load, "requests": n_req,
                            "pool": len(blobs), "pool_triangles": int(sum(tris)),
                            "sizes": "log-uniform [5K, 2M] triangles from the many-mesh generator (seed 5)",
                            "hbm_budget_gb": args.serve_budget_gb, "streams": 3, "max_batch": 256},
                 "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3),
                                "p99": round(float(np.percentile(lat, 99)), 3),
                                "max": round(float(np.max(lat)), 3),
-                               "to": "outputs in pinned host memory" if to_host else "outputs resident on the device"},
+                               "from": "submit" if mode == "rate" else "admission",
+                               "to": "outputs in pinned host memory" if to_host
+                               else "outputs resident on the device"},
                 "achieved_rps": round(n_req / span_s, 1), "launches": st["launches"],
                 "mean_requests_per_launch": round(n_req / max(1, st["launches"]), 2),
                 "arena_peak_gb": round(st["arena_peak_bytes"] / 2 ** 30, 3),

@@ -194,15 +194,16 @@ __device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t phase) {
 }
 
 // Bounded wait (`limit` SM clocks, DecodeArgs::wait_clocks); false on
-// timeout.  The first check does not block, so a limit of 0 gives up as
-// soon as the phase is found incomplete.
+// timeout.  The first check does not block and the clock is read before
+// every (blocking) try, so a limit of 0 gives up as soon as the phase is
+// found incomplete.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase, long long limit) {
     if (mbar_test_wait(bar, phase)) return true;
     const long long t0 = clock64();
-    while (!mbar_try_wait(bar, phase)) {
+    for (;;) {
         if (clock64() - t0 > limit) return false;
+        if (mbar_try_wait(bar, phase)) return true;
     }
-    return true;
 }
 
 // ---------------------------------------------------------------------------

@@ -18,6 +18,13 @@ with the C oracle (so_side_table), and launches the kernel the way the
 reference harness does (stride_dup_decode_bench.cu:662-685): a persistent
 grid of min(n_meshlets, 16 x SMs) blocks of 128 threads, its work counter
 zeroed before every launch.
+
+The reference's PLDT v5 GPU harness, bench_cpp/stride_decode_bench.cu
+(kernel paradelta_v5_fused_decode, :171; a verbatim copy of the CuPy
+decoder's kernel in utils/paradelta_v5_cuda.py), is built the same way and
+run by RefPldt5Kernel from the SBLB tables (sblb_blob) as the harness's
+launch() does (:553-579): one 32-thread block per meshlet slot, a grid of
+min(n_meshlets, 16 x SMs), per_warp_bytes of dynamic shared memory.
 """
 from __future__ import annotations
 
@@ -34,30 +41,49 @@ CUBIN = os.path.join(REF_DIR, "stride_dup_decode.cubin")
 ENTRY = os.path.join(REF_DIR, "stride_dup_decode.entry")
 REFERENCE = os.environ.get("MESHPRESS_REFERENCE", "/root/reference")  # the reference checkout
 REF_SRC = os.path.join(REFERENCE, "bench_cpp", "stride_dup_decode_bench.cu")
+P5_CUBIN = os.path.join(REF_DIR, "stride_decode_v5.cubin")
+P5_ENTRY = os.path.join(REF_DIR, "stride_decode_v5.entry")
+P5_SRC = os.path.join(REFERENCE, "bench_cpp", "stride_decode_bench.cu")
+
+
+def _compile(src: str, cubin: str, entry: str, pattern: str) -> None:
+    """nvcc -cubin of one reference source, unmodified; the mangled names of
+    the kernel entries matching `pattern` (from the ptxas report) go to `entry`."""
+    os.makedirs(REF_DIR, exist_ok=True)
+    r = subprocess.run(["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
+                        "-std=c++17", "-Xptxas", "-v", src, "-o", cubin + ".tmp"],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"reference kernel build failed:\n{r.stderr}")
+    names = sorted(set(re.findall(r"Compiling entry function '([^']*%s[^']*)'" % pattern, r.stdout + r.stderr)))
+    if not names:
+        raise RuntimeError("reference kernel entry name not found in the ptxas report")
+    os.replace(cubin + ".tmp", cubin)
+    with open(entry, "w") as f:
+        f.write("\n".join(names) + "\n")
+
+
+def _stale(src: str, cubin: str, entry: str) -> bool:
+    return not os.path.exists(cubin) or not os.path.exists(entry) or os.path.getmtime(cubin) < os.path.getmtime(src)
 
 
 def build(force: bool = False) -> bool:
-    """Compile the reference kernel to a sm_103a cubin when the reference
-    tree is present; True when a cubin exists."""
-    if os.path.exists(REF_SRC) and (force or not os.path.exists(CUBIN) or not os.path.exists(ENTRY)
-                                    or os.path.getmtime(CUBIN) < os.path.getmtime(REF_SRC)):
-        os.makedirs(REF_DIR, exist_ok=True)
-        r = subprocess.run(["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a", "-O3",
-                            "-std=c++17", "-Xptxas", "-v", REF_SRC, "-o", CUBIN + ".tmp"],
-                           capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError(f"reference kernel build failed:\n{r.stderr}")
-        m = re.search(r"Compiling entry function '([^']*stride_dup_decode_kernel[^']*)'", r.stdout + r.stderr)
-        if not m:
-            raise RuntimeError("reference kernel entry name not found in the ptxas report")
-        os.replace(CUBIN + ".tmp", CUBIN)
-        with open(ENTRY, "w") as f:
-            f.write(m.group(1) + "\n")
+    """Compile the reference kernels (DPR4 #5 and PLDT v5 #8) to sm_103a
+    cubins when the reference tree is present; True when the DPR4 cubin
+    exists."""
+    if os.path.exists(REF_SRC) and (force or _stale(REF_SRC, CUBIN, ENTRY)):
+        _compile(REF_SRC, CUBIN, ENTRY, "stride_dup_decode_kernel")
+    if os.path.exists(P5_SRC) and (force or _stale(P5_SRC, P5_CUBIN, P5_ENTRY)):
+        _compile(P5_SRC, P5_CUBIN, P5_ENTRY, "paradelta_v5_fused_decode")
     return os.path.exists(CUBIN) and os.path.exists(ENTRY)
 
 
 def available() -> bool:
     return os.path.exists(CUBIN) and os.path.exists(ENTRY)
+
+
+def available_v5() -> bool:
+    return os.path.exists(P5_CUBIN) and os.path.exists(P5_ENTRY)
 
 
 def dprb_blob(data: bytes) -> bytes:
@@ -239,3 +265,144 @@ class RefKernel:
         if self._mod:
             _driver().cuModuleUnload(self._mod)
             self._mod = ctypes.c_void_p()
+
+
+def parse_sblb(blob: bytes) -> dict:
+    """The SBLB v1 file back into the harness's buffers (read_blob,
+    bench_cpp/stride_decode_bench.cu:455-486)."""
+    import struct
+    f = struct.unpack_from("<IIIIIIIIffffIIII", blob, 0)
+    if f[0] != 0x424C4253 or f[1] != 1:
+        raise ValueError("not an SBLB v1 file")
+    keys = ("magic", "version", "code_width", "n_meshlets", "n_boundary", "n_v_total", "n_t_total", "buf_size",
+            "lin3_w0", "lin3_w1", "lin3_w2", "delta", "per_warp_bytes", "meshlets_per_block")
+    h = dict(zip(keys, f))
+    M, nb, o = h["n_meshlets"], h["n_boundary"], 64
+    out = {"hdr": h}
+
+    def take(name, dtype, count):
+        nonlocal o
+        a = np.frombuffer(blob, dtype, count, o)
+        o += a.nbytes
+        out[name] = a
+
+    take("buf", np.uint8, h["buf_size"])
+    take("off_bits", "<u8", M)
+    for k in ("n_bnd", "n_int", "n_tris", "n_strips"):
+        take(k, "<i4", M)
+    take("tris_off", "<i4", M + 1)
+    take("int_cursor", "<i4", M)
+    take("bnd_pos", "<f4", 3 * nb)
+    if o != len(blob):
+        raise ValueError("SBLB file size does not match its header")
+    return out
+
+
+def v5_kernel_smem(n_bnd, n_int, n_tris, code_bytes: int) -> int:
+    """Bytes of dynamic shared memory the PLDT v5 kernel's per-meshlet layout
+    (stride_decode_bench.cu:212-222) reaches for the largest meshlet: float4
+    rows and an int l2g entry for every local vertex, the 256-bit seen map,
+    the interior codes, four short emit arrays, the byte triangles."""
+    n_local = np.asarray(n_bnd, np.int64) + np.asarray(n_int, np.int64)
+    end = n_local * 20 + 32 + np.asarray(n_int, np.int64) * (3 * code_bytes + 8) + np.asarray(n_tris, np.int64) * 3
+    return int(end.max()) if len(end) else 0
+
+
+class RefPldt5Kernel:
+    """The reference PLDT v5 kernel prepared from an SBLB file on the current
+    torch device, launched as the harness's launch() does.  Two guards the
+    harness does not have, so that the launch stays in bounds:
+    the stream gets 64 zero bytes of padding (the kernel's bit reader loads
+    five bytes from its position), and the dynamic shared memory is raised to
+    the kernel's real per-meshlet layout when the SBLB header's
+    per_warp_bytes -- the CuPy decoder's sizing, which counts l2g for the
+    boundary vertices only (utils/paradelta_v5_cuda.py:658-665) while the
+    kernel reserves it for every local vertex (:292-293) -- is smaller.
+    Meshlets of more than 256 local vertices are refused (the seen map has
+    256 bits)."""
+
+    def __init__(self, blob: bytes):
+        import torch
+        if not available_v5():
+            raise RuntimeError("reference PLDT v5 kernel not built (oracle/_ref)")
+        B = parse_sblb(blob)
+        h = B["hdr"]
+        self.hdr = h
+        n_local = B["n_bnd"].astype(np.int64) + B["n_int"]
+        if len(n_local) and int(n_local.max()) > 256:
+            raise ValueError("a meshlet has more than 256 local vertices")
+        code_bytes = 4 if h["code_width"] else 2
+        need = (v5_kernel_smem(B["n_bnd"], B["n_int"], B["n_tris"], code_bytes) + 15) & ~15
+        self.smem_header = int(h["per_warp_bytes"])
+        self.smem = max(self.smem_header, need)
+        if self.smem > 227 * 1024:
+            raise ValueError("per-meshlet shared memory above the 227 KB limit")
+        dev = torch.device("cuda", torch.cuda.current_device())
+        buf = np.zeros(len(B["buf"]) + 64, np.uint8)
+        buf[:len(B["buf"])] = B["buf"]
+
+        def dput(a):
+            return torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).copy()).to(dev)
+
+        self.d = {"buf": dput(buf), "off": dput(B["off_bits"]), "n_bnd": dput(B["n_bnd"]),
+                  "n_int": dput(B["n_int"]), "n_tris": dput(B["n_tris"]), "n_strips": dput(B["n_strips"]),
+                  "tris_off": dput(B["tris_off"]), "int_cur": dput(B["int_cursor"]),
+                  "bnd_pos": dput(B["bnd_pos"] if len(B["bnd_pos"]) else np.zeros(3, np.float32)),
+                  "counter": torch.zeros(4, dtype=torch.uint8, device=dev)}
+        self.n_v, self.n_t, self.n_meshlets = int(h["n_v_total"]), int(h["n_t_total"]), int(h["n_meshlets"])
+        self.verts = torch.zeros((max(1, self.n_v), 3), dtype=torch.float32, device=dev)
+        self.tris = torch.zeros((max(1, self.n_t), 3), dtype=torch.int32, device=dev)
+        drv = _driver()
+        self._mod = ctypes.c_void_p()
+        self._fn = ctypes.c_void_p()
+        with open(P5_CUBIN, "rb") as f:
+            image = f.read()
+        self._image = ctypes.create_string_buffer(image, len(image))
+        _ck(drv.cuModuleLoadData(ctypes.byref(self._mod), ctypes.cast(self._image, ctypes.c_void_p)),
+            "cuModuleLoadData")
+        names = open(P5_ENTRY).read().split()
+        # the <short> instantiation for 16-bit codes, <int> for 32-bit (:566, :575)
+        want = "IiE" if h["code_width"] else "IsE"
+        name = next((n for n in names if want in n), None)
+        if name is None:
+            raise RuntimeError("PLDT v5 kernel instantiation not found in the cubin's entries")
+        _ck(drv.cuModuleGetFunction(ctypes.byref(self._fn), self._mod, name.encode()), "cuModuleGetFunction")
+        if self.smem > 48 * 1024:
+            drv.cuFuncSetAttribute.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+            _ck(drv.cuFuncSetAttribute(self._fn, 8, self.smem), "cuFuncSetAttribute")  # max dynamic smem
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        self.grid = min(self.n_meshlets, 16 * sms)
+        P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+        I, F = ctypes.c_int, ctypes.c_float  # noqa: E741
+        self._vals = [P(self.d["buf"]), P(self.d["off"]), P(self.d["n_bnd"]), P(self.d["n_int"]),
+                      P(self.d["n_tris"]), P(self.d["n_strips"]), P(self.d["tris_off"]), I(h["n_boundary"]),
+                      P(self.d["int_cur"]), P(self.d["bnd_pos"]), I(h["n_boundary"]),
+                      F(h["lin3_w0"]), F(h["lin3_w1"]), F(h["lin3_w2"]), F(h["delta"]),
+                      P(self.verts), P(self.tris), I(self.n_meshlets), I(h["per_warp_bytes"]),
+                      I(h["meshlets_per_block"]), P(self.d["counter"])]
+        self._params = (ctypes.c_void_p * len(self._vals))(
+            *[ctypes.cast(ctypes.pointer(v), ctypes.c_void_p) for v in self._vals])
+
+    def launch(self, stream) -> None:
+        """One decode on `stream`: zero the work counter, launch (:553-579)."""
+        if self.n_meshlets == 0:
+            return
+        with __import__("torch").cuda.stream(stream):
+            self.d["counter"].zero_()
+        _ck(_driver().cuLaunchKernel(self._fn, self.grid, 1, 1, 32, 1, 1, self.smem,
+                                     ctypes.c_void_p(int(stream.cuda_stream)),
+                                     ctypes.cast(self._params, ctypes.c_void_p), None),
+            "cuLaunchKernel")
+
+    def close(self):
+        if self._mod:
+            _driver().cuModuleUnload(self._mod)
+            self._mod = ctypes.c_void_p()
+
+
+def world_rows_v5(v_norm: np.ndarray, data: bytes) -> np.ndarray:
+    """Normalised rows as world coordinates in float32, as the CuPy decoder's
+    decode_to_host does (utils/paradelta_v5_cuda.py:714-718)."""
+    from . import oracle as orc
+    h = orc.parse_header_v5(data)
+    return v_norm.astype(np.float32) * np.float32(h.scale) + np.asarray(list(h.center), np.float32)

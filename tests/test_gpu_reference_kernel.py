@@ -1,8 +1,12 @@
-"""The reference's own CUDA decoder (bench_cpp/stride_dup_decode_bench.cu)
-on this GPU, next to this decoder: same DPR4 streams, side table derived
-from the bytes.  Its triangles must equal decode_dup's; its positions are
-not bit-exact by design (fp32 dequantisation), which this test measures.
-The throughput comparison is printed as one JSON line (run with -s)."""
+"""The reference's own CUDA decoders on this GPU, next to this repository's.
+
+DPR4: bench_cpp/stride_dup_decode_bench.cu on the same DPR4 streams, its
+side table derived from the bytes; its triangles must equal decode_dup's,
+its positions are not bit-exact by design (fp32 dequantisation).  PLDT v5:
+bench_cpp/stride_decode_bench.cu:171 fed from the SBLB file, against
+decode_paradelta_v5.  The timing record of both kernels on the 2049 x 2049
+heightfield is written by oracle/time_reference_gpu.py; here it runs on a
+small grid."""
 import json
 
 import numpy as np
@@ -53,49 +57,44 @@ def test_reference_kernel_on_reference_encoded_streams(torch_cuda, name):
     k.close()
 
 
-def test_reference_kernel_throughput_vs_ours(torch_cuda):
+def test_reference_timing_record_on_a_small_grid(torch_cuda):
+    """The timing script that writes the committed record of both reference
+    GPU kernels beside this repository's decoders, on a 257 x 257 grid."""
+    if not ref_gpu.available_v5():
+        pytest.skip("reference PLDT v5 kernel not built")
+    from oracle import time_reference_gpu
+    rec = time_reference_gpu.run(grid=257, reps=3, sample_clocks=False)
+    json.dumps(rec)
+    assert rec["triangles"] == 2 * 256 * 256
+    for fmt in ("dpr4", "pldt5"):
+        ref, ours = rec[fmt]["reference_kernel"], rec[fmt]["this_decoder"]
+        assert ref["triangles_exact"] and ours["triangles_exact"]
+        assert ours["positions_bit_exact_frac"] == 1.0
+        assert ref["ms_mean"] > 0 and ours["ms_mean"] > 0
+        assert ref["positions_max_abs_err"] < 1e-2
+
+
+V5_FIXTURES = ["v5_grid33_b12", "v5_grid65_world", "v5_ico5_b14", "v5_noise129_mv128", "v5_torus_b10",
+               "v5_tri1_b12", "v5_noise33_b16"]
+
+
+@pytest.mark.parametrize("name", V5_FIXTURES)
+def test_reference_pldt5_kernel_on_reference_encoded_streams(torch_cuda, name):
+    """The reference PLDT v5 kernel (bench_cpp/stride_decode_bench.cu:171)
+    run from the SBLB file of a reference-encoded stream: its triangles equal
+    decode_paradelta_v5's; its positions (float32 prediction) come close."""
+    if not ref_gpu.available_v5():
+        pytest.skip("reference PLDT v5 kernel not built")
     torch = torch_cuda
-    import bench
-    from meshpress_gb300 import ParaDeltaV5GpuDecoder
-    data, cfg = bench.heightfield_stream(2049, 12)
-    k = _run_ref(torch, data)
-    opos, oidx = oracle.decode_mt(data, 0)
-    tris = k.tris.cpu().numpy().view(np.uint32).astype(np.int64)
-    assert np.array_equal(tris, oidx)
-    pos = k.verts.cpu().numpy()
-    exact = float(np.mean(pos.view(np.uint32) == opos.view(np.uint32)))
-    maxerr = float(np.max(np.abs(pos - opos)))
-    dec = ParaDeltaV5GpuDecoder(data)
-    t_ours, v_ours = dec.decode_to_device()
+    data = _golden.load(name)["data"]
+    k = ref_gpu.RefPldt5Kernel(ref_gpu.sblb_blob(data))
     s = torch.cuda.Stream()
-    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-
-    def timed(fn, n=10, warm=3):
-        ts = []
-        for i in range(n + warm):
-            with torch.cuda.stream(s):
-                flush.fill_(i & 255)
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record(s)
-                fn()
-                e1.record(s)
-            s.synchronize()
-            if i >= warm:
-                ts.append(e0.elapsed_time(e1))
-        return float(np.mean(ts))
-
-    ms_ref = timed(lambda: k.launch(s))
-    ms_ours = timed(lambda: dec.decode_into(t_ours, v_ours, stream=s))
-    n_t = int(oidx.shape[0])
-    line = {"workload": "heightfield_2049x2049_12bit", "triangles": n_t,
-            "reference_kernel": {"ms": round(ms_ref, 4), "M_tris_s": round(n_t / ms_ref / 1e3, 1),
-                                 "triangles_exact": True, "positions_bit_exact_frac": round(exact, 4),
-                                 "positions_max_abs_err": maxerr,
-                                 "note": "stride_dup_decode_kernel, unmodified, side table from the bytes"},
-            "this_decoder": {"ms": round(ms_ours, 4), "M_tris_s": round(n_t / ms_ours / 1e3, 1),
-                             "bit_exact": True},
-            "l2": "flushed before every decode"}
-    print("REFERENCE_KERNEL " + json.dumps(line))
-    assert ms_ours > 0 and ms_ref > 0
+    k.launch(s)
+    s.synchronize()
+    opos, oidx = oracle.decode_v5(data)
+    tris = k.tris.cpu().numpy()[:k.n_t].view(np.uint32).astype(np.int64)
+    assert np.array_equal(tris, oidx)
+    pos = ref_gpu.world_rows_v5(k.verts.cpu().numpy()[:k.n_v], data)
+    ext = float(np.max(np.ptp(opos, axis=0))) if len(opos) else 1.0
+    assert np.max(np.abs(pos - opos)) <= 1e-3 * max(ext, 1.0)  # float32 prediction: close, not exact
     k.close()
-    dec.close()

@@ -160,3 +160,29 @@ def test_queue_limit_and_errors(torch_cuda, pool):
         assert len(rids) >= 1
         with pytest.raises(_lib.StrideFormatError):
             srv.release(10 ** 9)  # unknown request
+
+
+def test_bench_serve_passes(torch_cuda):
+    """The bench's serve workload on a small pool: one Poisson pass and one
+    burst pass, every response exact, the burst batching more than one
+    request per launch."""
+    import json
+    import os
+    import subprocess
+    import sys
+    repo = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ)
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        env.pop(k, None)
+    out = subprocess.run([sys.executable, os.path.join(repo, "bench.py"), "--workload", "serve", "--rates", "200",
+                          "--serve-seconds", "0.5", "--serve-pool", "6", "--serve-burst", "64",
+                          "--serve-host-rate", "0", "--serve-budget-gb", "4"],
+                         env=env, capture_output=True, text=True, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [json.loads(x) for x in out.stdout.splitlines() if x.startswith("{")]
+    assert [x["config"]["workload"] for x in lines] == ["serve_poisson_200rps", "serve_burst64"]
+    for x in lines:
+        assert x["mismatched_responses"] == 0 and x["failed_responses"] == {}
+        assert x["exact_responses"] == x["config"]["requests"]
+        assert x["pool_bit_exact_vs_oracle"]
+    assert lines[1]["mean_requests_per_launch"] > 2.0
