@@ -656,6 +656,15 @@ struct MtfFifo {
         const uint32_t t = (x & 0x7F7F7F7Fu) + 0x7F7F7F7Fu;
         return ~(t | x) & m;
     }
+    // v among the 16 bytes (valid entries or filler): an exact test, no depth
+    __device__ __forceinline__ bool holds(uint32_t v) const {
+        const uint32_t vv = __byte_perm(v, 0u, 0u);
+        const uint32_t k = 0x01010101u, h = 0x80808080u;
+        const uint32_t x0 = f0 ^ vv, x1 = f1 ^ vv, x2 = f2 ^ vv, x3 = f3 ^ vv;
+        // a zero byte of x sets its top bit in (x - k) & ~x (borrows never
+        // reach past the first zero byte)
+        return ((((x0 - k) & ~x0) | ((x1 - k) & ~x1) | ((x2 - k) & ~x2) | ((x3 - k) & ~x3)) & h) != 0u;
+    }
     // depth of v among the valid entries, or 16
     __device__ __forceinline__ uint32_t find(uint32_t v) const {
         const uint32_t vv = __byte_perm(v, 0u, 0u);

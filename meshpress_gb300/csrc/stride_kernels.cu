@@ -81,6 +81,16 @@ __device__ __forceinline__ void pair_bar(uint32_t pair, uint32_t slot) {
     }
 }
 
+// Named barrier of a pair's two warps for taking and finishing groups
+// (immediate ids 9 and 10, past the record barriers 1..8).
+__device__ __forceinline__ void claim_bar(uint32_t pair) {
+    if (pair == 0u) {
+        bar_sync_imm<9>();
+    } else {
+        bar_sync_imm<10>();
+    }
+}
+
 // ---------------------------------------------------------------------------
 // 1. scan kernel
 // ---------------------------------------------------------------------------
@@ -273,14 +283,22 @@ __host__ __device__ inline uint32_t vert_cta_bytes(uint32_t stage_bytes, uint32_
 
 // Connectivity as a producer/consumer pair of warps per group of 32
 // meshlets.  The parser warp runs the serial part of every lane's token
-// chain -- bit cursor, strip headers, token widths, the 16-entry FIFO -- and
-// writes one 32-bit record per lane and iteration into a two-chunk ring in
-// shared memory; the assembler warp replays the records: strip state,
-// triangles, first occurrences (walk), output rings.  The two chains run on
-// different warps, so each is about half as long as the fused one.
+// chain -- bit cursor, strip headers, token widths, the 16-entry FIFO in
+// registers (_read_vert, encoder/paradelta_codec.py:330-340) -- and writes
+// one 32-bit record per lane and iteration into a two-chunk ring in shared
+// memory; the assembler warp replays the records: strip state, triangles,
+// first occurrences (walk), output rings.  The two chains run on different
+// warps, so each is about half as long as the fused one.
 //
-// Record: bits 0..7 vertex, bit 8 valid, bit 9 edge code, bits 10..11 token
-// position in its strip (0..2 the three roots, 3 a strip-body token).
+// Validity is checked lazily, as running extremes compared once at the end:
+// the parser's FIFO indices, local ids, cursor and strips, the assembler's
+// triangle count.  Until then a corrupt lane runs on harmlessly: every id
+// the parser passes on is clamped below n_local, and the assembler's
+// flushes never write past the meshlet's triangles or walk entries.
+//
+// Record: bits 0..7 vertex, bit 8 live (clear: no token), bit 9 edge code,
+// bits 10..11 token position in its strip (0..2 the three roots, 3 a
+// strip-body token).
 constexpr uint32_t kChunk = kChunkWords;  // iterations per ring chunk
 constexpr uint32_t kChunkDone = 1u << 31;  // count word: the parser has finished
 
@@ -295,13 +313,22 @@ __device__ __forceinline__ uint32_t bar_empty(uint32_t c) { return 2u + c; }
 // one refill are waited for at the next, so each has a full record chunk
 // of time to land; a refill overwrites the chunk two behind, which the
 // window has passed (its last words are in registers).
-template <int G>
-__device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, uint32_t* __restrict__ ring,
+//
+// The FIFO is a move-to-front register whose unused bytes hold 0xFF.  In
+// the fast pass (kExact false) a raw token's id is taken as new to the FIFO
+// -- an encoder writes a FIFO index for an id it still holds -- and an id
+// that is there after all (or equals the 0xFF filler) is only detected,
+// which makes the lane suspect; a group with a suspect lane runs again with
+// kExact, where a raw id is searched for and moved from where it is.
+// Returns the suspect flag (always false with kExact).
+template <int G, bool kExact>
+__device__ bool conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, uint32_t* __restrict__ ring,
                            uint32_t* __restrict__ recs, uint32_t* __restrict__ counts, uint32_t pair, int lane,
                            const uint4* __restrict__ mtf_masks) {
     const uint32_t n_local = L.d.counts0 & 0xFFFFu;
-    const uint32_t n_tris = L.d.counts0 >> 16;
-    const uint32_t ib = max(1u, 32u - __clz(n_local));
+    const uint32_t ib = max(1u, 32u - __clz(n_local));  // _idx_bits_for (paradelta_codec.py:124-125)
+    const uint32_t rsh = 32u - ib, ib1 = 1u + ib;
+    const uint32_t vmax = n_local ? n_local - 1u : 0u;
     const uint32_t end = L.d.end_bit;
     const unsigned long long s0 = (L.blob_off + (L.d.start_bit >> 3)) & ~15ull;
     const unsigned long long e16 = (L.blob_off + ((end + 7u) >> 3) + 15ull) & ~15ull;
@@ -318,15 +345,18 @@ __device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
     win.pos = win.w0 = win.w1 = win.w2 = 0u;
     if (act) win.seek(L.d.start_bit + 48u);
     uint32_t strips_left = L.d.n_strips;
-    uint32_t tok_left = 0u, tok_idx = 0u, tris = 0u;
+    uint32_t tok_left = 0u, tx = 0u;
+    uint32_t ridmax = 0u;  // largest raw id + 1 (0: none)
+    int32_t smin = 0;      // smallest depth a FIFO token named (negative: past the entries)
+    bool suspect = false;
     MtfFifo fifo;
-    bool bad = false;
-    bool live = act && strips_left > 0u;  // false for good once the lane's strips are read (or it failed)
+    fifo.f0 = fifo.f1 = fifo.f2 = fifo.f3 = 0xFFFFFFFFu;
+    bool live = act && strips_left > 0u;  // false for good once the lane's strips are read
     // A strip of length len takes len + 2 tokens and adds len triangles (one
-    // for len 0), and a lane stops once its triangles would pass n_tris, so
-    // n_tris + 2 n_strips iterations finish (or fail) every lane: the warp
-    // runs the largest of those counts instead of voting every iteration.
-    const uint32_t iters = __reduce_max_sync(kFull, act ? n_tris + 2u * L.d.n_strips : 0u);
+    // for len 0), so n_tris + 2 n_strips iterations read every strip of a
+    // valid lane: the warp runs the largest of those counts instead of
+    // voting every iteration.  A lane still live after them is corrupt.
+    const uint32_t iters = __reduce_max_sync(kFull, act ? (L.d.counts0 >> 16) + 2u * L.d.n_strips : 0u);
     uint32_t it = 0u;
     uint32_t k = 0u;  // chunk
     for (;;) {
@@ -339,49 +369,53 @@ __device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
 #pragma unroll 4
         for (uint32_t i = 0; i < n; i++) {
             // No branch per token, so consecutive tokens' chains can overlap:
-            // a lane that has finished (or failed) keeps running the body on
-            // whatever bits follow, but its window no longer moves and its
-            // records are empty.
-            // A 32-bit window holds a strip header (16 bits) plus the next
-            // token (at most 1 + 9 bits), or an edge code plus a token.
+            // a lane that has finished keeps running the body on whatever
+            // bits follow, but its window and FIFO no longer move and its
+            // records are empty.  A 32-bit window holds a strip header (16
+            // bits) plus the next token (at most 1 + 9 bits), or an edge code
+            // plus a token.
             const uint32_t x0 = win.peek();
-            uint32_t used = 0u;
-            const bool hdr = tok_left == 0u;  // strip header (paradelta_v5_dup.py:519)
-            const uint32_t len = x0 >> 16;
-            const uint32_t sbody = len > 1u ? len - 1u : 0u;
-            tok_left = hdr ? 3u + sbody : tok_left;
-            tok_idx = hdr ? 0u : tok_idx;
+            const bool hdr = tok_left == 0u;                 // strip header (paradelta_v5_dup.py:519)
+            const uint32_t sb = max(x0 >> 16, 1u) - 1u;       // body tokens of the strip
+            tok_left = hdr ? sb + 3u : tok_left;
             strips_left -= hdr ? 1u : 0u;
-            tris += (hdr & live) ? 1u + sbody : 0u;  // the count the lane is checked against
-            used += hdr ? 16u : 0u;
+            const uint32_t tix = hdr ? 0u : tx;
             uint32_t x = hdr ? (x0 << 16) : x0;
-            const bool body = tok_idx >= 3u;
+            uint32_t used = hdr ? 16u : 0u;
+            const bool body = tix == 3u;
             const uint32_t ec = x >> 31;  // edge code of a strip-body token (:528)
             x = body ? (x << 1) : x;
             used += body ? 1u : 0u;
-            const bool raw = (x >> 31) != 0u;
-            const uint32_t rid = (x << 1) >> (32u - ib);
-            const uint32_t fi = (x << 1) >> 27;
-            used += raw ? 1u + ib : 6u;
-            // decode_dup raises IndexError on both (FIFO index, local id)
-            const bool invalid = (raw ? rid >= n_local : fi >= fifo.len) | (tris > n_tris);
-            // the FIFO as a move-to-front register: a FIFO token's entry at
-            // depth len-1-fi, a raw id's at the depth find() gives, or none
-            // (a new id enters, the oldest leaving a full FIFO)
-            const uint32_t sd = (fifo.len - 1u - fi) & 15u;
-            const uint32_t v = raw ? (rid & 0xFFu) : fifo.at(sd);
-            const uint32_t at = raw ? fifo.find(v) : sd;
-            const bool fresh = at == 16u;
-            fifo.mtf_masked(v, mtf_masks[fresh ? min(fifo.len, 15u) : at]);
-            fifo.len += (fresh & (fifo.len < 16u)) ? 1u : 0u;
-            const uint32_t rec = (invalid | !live) ? 0u
-                                                   : (v | 0x100u | ((body ? ec : 0u) << 9) | (min(tok_idx, 3u) << 10));
-            tok_idx++;
+            const bool raw = static_cast<int32_t>(x) < 0;
+            const uint32_t y = x << 1;
+            const uint32_t rid = y >> rsh;
+            const uint32_t fi = y >> 27;
+            used += raw ? ib1 : 6u;
+            // decode_dup raises IndexError on a FIFO index past the entries
+            // and on a local id past n_local: kept as a running min / max
+            const int32_t sd = static_cast<int32_t>(fifo.len) - 1 - static_cast<int32_t>(fi);
+            const bool rl = raw & live;
+            smin = min(smin, (raw | !live) ? 0 : sd);
+            ridmax = max(ridmax, rl ? rid + 1u : 0u);
+            const uint32_t s = static_cast<uint32_t>(sd) & 15u;  // depth of a FIFO token's entry
+            const uint32_t v = raw ? (rid & 0xFFu) : fifo.at(s);
+            bool fresh = raw;  // a raw id not in the FIFO
+            uint32_t p;
+            if constexpr (kExact) {
+                const uint32_t at = raw ? fifo.find(v) : 16u;
+                fresh = raw & (at == 16u);
+                p = raw ? (fresh ? min(fifo.len, 15u) : at) : s;
+            } else {
+                suspect = suspect | (rl & fifo.holds(v));
+                p = raw ? min(fifo.len, 15u) : s;
+            }
+            fifo.mtf_masked(v, mtf_masks[live ? p : 16u]);  // row 16 is zero: no change
+            fifo.len += (live & fresh & (fifo.len < 16u)) ? 1u : 0u;
+            rc[i * 32u] = live ? (min(v, vmax) | 0x100u | ((body ? ec : 0u) << 9) | (tix << 10)) : 0u;
             tok_left--;
+            tx = min(tix + 1u, 3u);
             win.advance(live ? used : 0u);
-            bad = bad | (live & (invalid | (win.pos > end)));
-            live = live & !bad & ((tok_left | strips_left) != 0u);
-            rc[i * 32u] = rec;
+            live = live & ((tok_left | strips_left) != 0u);
         }
         it += n;
         const bool done = it >= iters;
@@ -398,17 +432,21 @@ __device__ void conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
         cp_async_commit();
     }
     cp_async_wait_all();  // no copy may land after the CTA's shared memory is gone
-    bad = bad | live;  // cannot happen: the count bounds every lane
     // take the assembler's remaining chunk releases: the ring and the
     // barriers are clean
     for (uint32_t j = k >= 2u ? k - 2u : 0u; j < k; j++) pair_bar<G, false>(pair, bar_empty(j & 1u));
     if (act) {
-        if (bad || tris != n_tris) {
+        // every strip read, ids and FIFO indices in range, inside the meshlet;
+        // a suspect lane's FIFO (and so its checks) may be off: its group
+        // runs again exactly
+        const bool bad = live || smin < 0 || ridmax > n_local || win.pos > end;
+        if (bad && !suspect) {
             report(a.status, kErrCorrupt, L.m);
-        } else {
+        } else if (!bad) {
             a.descs[L.m].anchor_bit = win.pos;
         }
     }
+    return act && suspect;
 }
 
 // Assembler warp.
@@ -419,6 +457,8 @@ __device__ void conn_assemble(const DecodeArgs& a, const GroupLane& L, bool act,
                               int lane) {
 #pragma unroll
     for (int i = 0; i < 8; i++) seen[i * 32 + lane] = 0u;
+    const uint32_t n_local = L.d.counts0 & 0xFFFFu;
+    const uint32_t n_tris = L.d.counts0 >> 16;
     uint32_t* walk_out = a.walk_scratch + L.wp_base;
     // triangle indices are relative to the mesh's first vertex
     const uint32_t vloc = act ? static_cast<uint32_t>(L.v_base - L.P->v_offset) : 0u;
@@ -465,9 +505,9 @@ __device__ void conn_assemble(const DecodeArgs& a, const GroupLane& L, bool act,
             }
             if (--flush_in == 0u) {  // warp-uniform
                 flush_in = kFlushEvery;
-                if (act) {
-                    flush_tris(a.idx, L.t_base, tr, tf, tcnt, vloc, false);
-                    flush_walk(walk_out, wr, wf, wcnt, false);
+                if (act) {  // never past the meshlet's triangles or walk entries
+                    flush_tris(a.idx, L.t_base, tr, tf, min(tcnt, n_tris), vloc, false);
+                    flush_walk(walk_out, wr, wf, min(wcnt, n_local), false);
                 }
             }
         }
@@ -475,17 +515,22 @@ __device__ void conn_assemble(const DecodeArgs& a, const GroupLane& L, bool act,
         if (cw & kChunkDone) break;
     }
     if (act) {
-        flush_tris(a.idx, L.t_base, tr, tf, tcnt, vloc, true);
-        flush_walk(walk_out, wr, wf, wcnt, true);
-        a.descs[L.m].walk = kind0 | (wcnt << 16);
+        flush_tris(a.idx, L.t_base, tr, tf, min(tcnt, n_tris), vloc, true);
+        flush_walk(walk_out, wr, wf, min(wcnt, n_local), true);
+        // the triangle count does not depend on the FIFO: no suspect here
+        if (tcnt != n_tris) report(a.status, kErrCorrupt, L.m);
+        a.descs[L.m].walk = kind0 | (min(wcnt, n_local) << 16);
     }
 }
 
 // Connectivity of group g by one warp pair (its shared memory at `base`):
-// every lane streams its own meshlet, so no meshlet is too large.
+// every lane streams its own meshlet, so no meshlet is too large.  The fast
+// pass first; if a lane of it is suspect, both warps run the group again
+// with the exact FIFO (outputs and records are rewritten).  `redo` is the
+// pair's word in shared memory.
 template <int G>
 __device__ __forceinline__ void conn_group(const DecodeArgs& a, uint32_t g, uint32_t pair, bool parser, int lane,
-                                           uint8_t* base, const uint4* mtf_masks) {
+                                           uint8_t* base, const uint4* mtf_masks, volatile uint32_t* redo) {
     uint32_t* rings = reinterpret_cast<uint32_t*>(base);
     uint32_t* recs = rings + 32u * kLaneRingWords;
     uint32_t* counts = recs + 2u * kChunk * 32u;
@@ -501,7 +546,19 @@ __device__ __forceinline__ void conn_group(const DecodeArgs& a, uint32_t g, uint
     }
     if (!__any_sync(kFull, ok)) return;  // both warps see the same lanes
     if (parser) {
-        conn_parse<G>(a, L, ok, rings + lane * kLaneRingWords, recs, counts, pair, lane, mtf_masks);
+        const bool s = conn_parse<G, false>(a, L, ok, rings + lane * kLaneRingWords, recs, counts, pair, lane,
+                                            mtf_masks);
+        const bool any = __any_sync(kFull, s);
+        if (lane == 0) *redo = any ? 1u : 0u;
+    } else {
+        conn_assemble<G>(a, L, ok, seen, tring, wring, recs, counts, pair, lane);
+    }
+    claim_bar(pair);  // the pass is over; the redo word is written
+    const bool again = *redo != 0u;
+    claim_bar(pair);  // both warps have read it
+    if (!again) return;
+    if (parser) {
+        conn_parse<G, true>(a, L, ok, rings + lane * kLaneRingWords, recs, counts, pair, lane, mtf_masks);
     } else {
         conn_assemble<G>(a, L, ok, seen, tring, wring, recs, counts, pair, lane);
     }
@@ -513,8 +570,9 @@ __device__ __forceinline__ void conn_group(const DecodeArgs& a, uint32_t g, uint
 template <int G>
 __global__ void __launch_bounds__(G * 64) conn_kernel(DecodeArgs a) {
     extern __shared__ __align__(128) uint8_t smem[];
-    __shared__ uint4 mtf_masks[16];
-    if (threadIdx.x < 16u) mtf_masks[threadIdx.x] = mtf_mask_row(threadIdx.x);
+    __shared__ uint4 mtf_masks[17];
+    __shared__ uint32_t s_redo[2];
+    if (threadIdx.x < 17u) mtf_masks[threadIdx.x] = threadIdx.x < 16u ? mtf_mask_row(threadIdx.x) : make_uint4(0u, 0u, 0u, 0u);
     const uint32_t pair = threadIdx.x >> 6;
     const bool parser = ((threadIdx.x >> 5) & 1u) == 0u;
     const int lane = threadIdx.x & 31;
@@ -523,7 +581,8 @@ __global__ void __launch_bounds__(G * 64) conn_kernel(DecodeArgs a) {
     const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
     const uint32_t f = blockIdx.x * G + pair;
     if (f >= n_groups) return;  // both warps of the pair
-    conn_group<G>(a, group_at(f, n_groups), pair, parser, lane, smem + pair * conn_pair_bytes(), mtf_masks);
+    conn_group<G>(a, group_at(f, n_groups), pair, parser, lane, smem + pair * conn_pair_bytes(), mtf_masks,
+                  s_redo + pair);
 }
 
 // ---------------------------------------------------------------------------
@@ -852,15 +911,6 @@ __device__ __forceinline__ void st_release_u32(uint32_t* p, uint32_t v) {
 // to group + 1 when the group's connectivity is written.
 __device__ __forceinline__ uint32_t* done_entry(const DecodeArgs& a, uint32_t i) { return &a.descs[32u * i].pad[0]; }
 
-// Named barrier of a pair's two warps for taking and finishing groups
-// (immediate ids 9 and 10, past the record barriers 1..8).
-__device__ __forceinline__ void claim_bar(uint32_t pair) {
-    if (pair == 0u) {
-        bar_sync_imm<9>();
-    } else {
-        bar_sync_imm<10>();
-    }
-}
 
 // The next group of the vertex phase: the next completion-list entry,
 // waited for (bounded: DecodeArgs::wait_clocks, about a second by default).  n_groups when the list
@@ -899,8 +949,9 @@ __global__ void __launch_bounds__(128, kMinBlocks) flow_kernel(DecodeArgs a, uin
     extern __shared__ __align__(128) uint8_t smem[];
     __shared__ uint32_t s_claim[2];
     __shared__ uint32_t s_group;
-    __shared__ uint4 mtf_masks[16];
-    if (threadIdx.x < 16u) mtf_masks[threadIdx.x] = mtf_mask_row(threadIdx.x);
+    __shared__ uint4 mtf_masks[17];
+    __shared__ uint32_t s_redo[2];
+    if (threadIdx.x < 17u) mtf_masks[threadIdx.x] = threadIdx.x < 16u ? mtf_mask_row(threadIdx.x) : make_uint4(0u, 0u, 0u, 0u);
     const uint32_t warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const bool failed = *reinterpret_cast<volatile unsigned long long*>(&a.status->err) != 0ull;
@@ -923,7 +974,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) flow_kernel(DecodeArgs a, uin
             }
             if (f >= n_groups) break;
             const uint32_t g = group_at(f, n_groups);
-            conn_group<2>(a, g, pair, parser, lane, base, mtf_masks);
+            conn_group<2>(a, g, pair, parser, lane, base, mtf_masks, s_redo + pair);
             __threadfence();  // this thread's outputs, before the list entry
             claim_bar(pair);  // both warps are done with the group
             if (!parser && lane == 0) st_release_u32(done_entry(a, atomicAdd(&a.status->done_tail, 1u)), g + 1u);
