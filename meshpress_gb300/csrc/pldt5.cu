@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "stride_common.cuh"
+#include "stride_device.cuh"
 #include "stride_gb300.h"
 #include "stride_internal.h"
 
@@ -58,18 +59,39 @@ __device__ __forceinline__ void p5_report(Status* st, int code, uint32_t m) {
 }
 
 // MSB-first reads from global memory (through L2, as every global read of
-// the library); a read never passes `limit`.
+// the library) through a three-word register window: a read costs a funnel
+// shift, and the word load that refills the window is issued a word ahead
+// of its use.  The stream is read as big-endian 32-bit words (its device
+// copy is 256-byte aligned and followed by 64 zero bytes, so the window
+// never reads past the padding); a read never passes `limit`.
 struct P5Bits {
-    const uint8_t* buf;
-    unsigned long long pos, limit;
+    const uint32_t* w;
+    unsigned long long pos, limit, wi;  // wi: word index of w0
+    uint32_t w0, w1, w2;
     bool bad;
-    // the 64 bits from pos (the stream is followed by zero padding)
-    __device__ __forceinline__ unsigned long long peek64() const {
-        const unsigned long long b = pos >> 3;
-        unsigned long long v = 0ull;
-#pragma unroll
-        for (int i = 0; i < 8; i++) v = (v << 8) | __ldcg(buf + b + i);
-        return v << (pos & 7ull);
+    __device__ __forceinline__ static uint32_t ld(const uint32_t* w, unsigned long long i) {
+        return bswap32(__ldcg(w + i));
+    }
+    __device__ __forceinline__ void seek(unsigned long long p) {
+        pos = p;
+        wi = p >> 5;
+        w0 = ld(w, wi);
+        w1 = ld(w, wi + 1ull);
+        w2 = ld(w, wi + 2ull);
+    }
+    __device__ __forceinline__ uint32_t peek() const {
+        return __funnelshift_l(w1, w0, static_cast<uint32_t>(pos & 31ull));
+    }
+    // n <= 32: crosses at most one word boundary
+    __device__ __forceinline__ void skip(uint32_t n) {
+        pos += n;
+        const unsigned long long ni = pos >> 5;
+        if (ni != wi) {
+            wi = ni;
+            w0 = w1;
+            w1 = w2;
+            w2 = ld(w, wi + 2ull);
+        }
     }
     __device__ __forceinline__ uint32_t bits(int n) {  // n <= 32
         if (n <= 0) return 0u;
@@ -77,8 +99,8 @@ struct P5Bits {
             bad = true;
             return 0u;
         }
-        const uint32_t v = static_cast<uint32_t>(peek64() >> (64 - n));
-        pos += static_cast<unsigned>(n);
+        const uint32_t v = peek() >> (32 - n);
+        skip(static_cast<uint32_t>(n));
         return v;
     }
     // zeros before the next one bit, and the one bit (BitReader unary prefix;
@@ -90,16 +112,16 @@ struct P5Bits {
                 bad = true;
                 return 0u;
             }
-            const uint32_t x = static_cast<uint32_t>(peek64() >> 32);
+            const uint32_t x = peek();
             if (x) {
                 const uint32_t z = static_cast<uint32_t>(__clz(x));
                 q += z;
-                pos += z + 1u;
+                skip(z + 1u);
                 if (pos > limit) bad = true;
                 return q;
             }
             q += 32u;
-            pos += 32u;
+            skip(32u);
         }
     }
     // Rice(k) (BitReader.read_rice); q < 2^32 and k <= 24 fit 64 bits
@@ -123,67 +145,76 @@ struct P5Bits {
     }
 };
 
+// n <= 32 bits at an arbitrary position (fixed-width codes), 0 past `limit`
+__device__ __forceinline__ uint32_t p5_bits_at(const uint32_t* w, unsigned long long pos, int n,
+                                               unsigned long long limit, bool& bad) {
+    if (n <= 0) return 0u;
+    if (pos + static_cast<unsigned>(n) > limit) {
+        bad = true;
+        return 0u;
+    }
+    const unsigned long long i = pos >> 5;
+    const uint32_t x = __funnelshift_l(P5Bits::ld(w, i + 1ull), P5Bits::ld(w, i), static_cast<uint32_t>(pos & 31ull));
+    return x >> (32 - n);
+}
+
 __device__ __forceinline__ long long unzig(unsigned long long u) {
     return static_cast<long long>((u >> 1) ^ (0ull - (u & 1ull)));
 }
 
-// One residual code of axis d: tag 0 fixed width (random access), 1 Rice, 2
-// Exp-Golomb (paradelta_v5.py:405-424).
+// One axis' residual substream: tag 0 fixed width (random access), 1 Rice,
+// 2 Exp-Golomb (paradelta_v5.py:405-424); tags 1 and 2 read through their
+// own window.
 struct P5Axis {
     int tag, k, bw;
     long long mn;
-    unsigned long long cur;  // next code (tags 1, 2) or the first code (tag 0)
+    unsigned long long base;  // first code (tag 0)
+    P5Bits r;                 // the next code (tags 1, 2)
 };
 
-__device__ __forceinline__ long long p5_code(P5Bits& b, P5Axis& ax, uint32_t i) {
-    if (ax.tag == 0) {
-        b.pos = ax.cur + static_cast<unsigned long long>(i) * static_cast<unsigned>(ax.bw);
-        return ax.mn + static_cast<long long>(b.bits(ax.bw));
-    }
-    b.pos = ax.cur;
-    const unsigned long long u = ax.tag == 1 ? b.rice(ax.k) : b.eg(ax.k);
-    ax.cur = b.pos;
+__device__ __forceinline__ long long p5_code(P5Axis& ax, uint32_t i, bool& bad) {
+    if (ax.tag == 0)
+        return ax.mn + static_cast<long long>(p5_bits_at(ax.r.w, ax.base + static_cast<unsigned long long>(i) *
+                                                                             static_cast<unsigned>(ax.bw),
+                                                         ax.bw, ax.r.limit, bad));
+    const unsigned long long u = ax.tag == 1 ? ax.r.rice(ax.k) : ax.r.eg(ax.k);
+    bad = bad || ax.r.bad;
     return unzig(u);
 }
 
-// FIFO of the 16 most recently used local ids, oldest first (_read_vert,
-// encoder/paradelta_codec.py:330-340).
-struct P5Fifo {
-    int v[16];
-    int len;
-    __device__ __forceinline__ void use(int x) {
-        int at = -1;
-        for (int i = 0; i < len; i++)
-            if (v[i] == x) at = i;
-        if (at < 0 && len == 16) at = 0;  // evict the oldest
-        if (at >= 0) {
-            for (int i = at; i + 1 < len; i++) v[i] = v[i + 1];
-            len--;
-        }
-        v[len++] = x;
-    }
-};
-
-__device__ __forceinline__ int p5_vert(P5Bits& b, P5Fifo& f, int idx_bits, bool& bad) {
-    int x;
+// One token's local id through the FIFO of the 16 most recently used ids
+// (_read_vert, encoder/paradelta_codec.py:330-340): a move-to-front register
+// (depth 0 the newest, so the FIFO index fi, 0 the oldest, is depth
+// len - 1 - fi), an id found in it moved to the front, a new one pushed
+// (the oldest leaving a full FIFO).
+__device__ __forceinline__ int p5_vert(P5Bits& b, MtfFifo& f, int idx_bits, const uint4* masks, bool& bad) {
+    uint32_t x, at;
     if (b.bits(1) == 0u) {
-        const int fi = static_cast<int>(b.bits(5));
+        const uint32_t fi = b.bits(5);
         if (fi >= f.len) {
             bad = true;
             return 0;
         }
-        x = f.v[fi];
+        at = f.len - 1u - fi;
+        x = f.at(at);
     } else {
-        x = static_cast<int>(b.bits(idx_bits));
+        x = b.bits(idx_bits);
+        at = x < 256u ? f.find(x) : 16u;
     }
-    f.use(x);
-    return x;
+    const bool fresh = at == 16u;
+    f.mtf_masked(x & 0xFFu, masks[fresh ? min(f.len, 15u) : at]);
+    f.len += (fresh && f.len < 16u) ? 1u : 0u;
+    return static_cast<int>(x);
 }
 
 // Lane l < per_warp of warp w decodes meshlet w * per_warp + l: the lanes of
 // a warp take different branches on almost every token, so a stream with
 // few meshlets gets one per warp, spread over the SMs.
 __global__ void __launch_bounds__(128) p5_decode_kernel(P5Args a, uint32_t per_warp) {
+    __shared__ uint4 masks[16];
+    __shared__ uint32_t seen_all[8 * 128];  // each thread's first-reach bits: word i at [i * 128 + thread]
+    if (threadIdx.x < 16u) masks[threadIdx.x] = mtf_mask_row(threadIdx.x);
+    __syncthreads();
     const uint32_t lane = threadIdx.x & 31u;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (lane >= per_warp) return;
@@ -191,7 +222,12 @@ __global__ void __launch_bounds__(128) p5_decode_kernel(P5Args a, uint32_t per_w
     if (m >= a.n_meshlets) return;
     const unsigned long long s0 = a.start[m], s1 = a.start[m + 1];
     const bool last = m + 1 == a.n_meshlets;
-    P5Bits b{a.blob, s0, a.nbits, false};
+    const uint32_t* words = reinterpret_cast<const uint32_t*>(a.blob);
+    P5Bits b;
+    b.w = words;
+    b.limit = a.nbits;
+    b.bad = false;
+    b.seek(s0);
     bool bad = false;
     const int n_bnd = static_cast<int>(b.bits(16));
     const int n_int = static_cast<int>(b.bits(16));
@@ -222,20 +258,22 @@ __global__ void __launch_bounds__(128) p5_decode_kernel(P5Args a, uint32_t per_w
         }
     }
     auto row_of = [&](int l) -> unsigned long long {
-        return l < n_bnd ? a.refs[rb + l] : row0 + static_cast<unsigned>(l - n_bnd);
+        return l < n_bnd ? __ldcg(a.refs + rb + l) : row0 + static_cast<unsigned>(l - n_bnd);
     };
     // connectivity and first-reach order (:371-400)
-    uint32_t seen[8];
+    uint32_t* seen = seen_all + threadIdx.x;
 #pragma unroll
-    for (int i = 0; i < 8; i++) seen[i] = 0u;
-    for (int l = 0; l < n_bnd; l++) seen[l >> 5] |= 1u << (l & 31);
+    for (int i = 0; i < 8; i++) seen[i * 128] = 0u;
+    for (int l = 0; l < n_bnd; l++) seen[(l >> 5) * 128] |= 1u << (l & 31);
     int idx_bits = 1;
     while ((1 << idx_bits) <= n_local) idx_bits++;  // max(1, ceil(log2(n_local + 1)))
-    P5Fifo f;
-    f.len = 0;
+    MtfFifo f;
     int n_t = 0, n_emit = 0;
     auto reach = [&](int v, uint32_t entry) {
-        if (v >= n_bnd && !((seen[v >> 5] >> (v & 31)) & 1u)) {
+        uint32_t* sp = seen + (v >> 5) * 128;
+        const uint32_t sw = *sp;
+        const uint32_t bit = 1u << (v & 31);
+        if (v >= n_bnd && !(sw & bit)) {
             if (n_emit >= n_int) {
                 bad = true;
             } else {
@@ -243,7 +281,7 @@ __global__ void __launch_bounds__(128) p5_decode_kernel(P5Args a, uint32_t per_w
                 n_emit++;
             }
         }
-        seen[v >> 5] |= 1u << (v & 31);
+        *sp = sw | bit;
     };
     auto put_tri = [&](int x, int y, int z) {
         if (n_t >= n_tris) {
@@ -259,7 +297,7 @@ __global__ void __launch_bounds__(128) p5_decode_kernel(P5Args a, uint32_t per_w
         const int strip_len = static_cast<int>(b.bits(16));
         int v[3];
         for (int j = 0; j < 3; j++) {
-            v[j] = p5_vert(b, f, idx_bits, bad);
+            v[j] = p5_vert(b, f, idx_bits, masks, bad);
             bad = bad || v[j] >= n_local;
         }
         if (bad || b.bad) break;
@@ -268,7 +306,7 @@ __global__ void __launch_bounds__(128) p5_decode_kernel(P5Args a, uint32_t per_w
         int p0 = v[0], p1 = v[1], p2 = v[2];
         for (int t = 0; t + 1 < strip_len && !bad && !b.bad; t++) {
             const uint32_t edge = b.bits(1);
-            const int nv = p5_vert(b, f, idx_bits, bad);
+            const int nv = p5_vert(b, f, idx_bits, masks, bad);
             if (nv >= n_local) bad = true;
             if (bad || b.bad) break;
             int x, y, c;
@@ -292,18 +330,23 @@ __global__ void __launch_bounds__(128) p5_decode_kernel(P5Args a, uint32_t per_w
             ax[d].k = 0;
             ax[d].bw = 0;
             ax[d].mn = 0;
+            ax[d].base = 0ull;
+            ax[d].r.w = words;
+            ax[d].r.limit = a.nbits;
+            ax[d].r.bad = false;
             if (ax[d].tag == 0) {
                 const uint32_t mn_u = b.bits(16);
                 ax[d].mn = (mn_u & 0x8000u) ? static_cast<long long>(mn_u) - 0x10000 : mn_u;
                 ax[d].bw = static_cast<int>(b.bits(8));
                 bad = bad || ax[d].bw > kP5MaxWidth;
-                ax[d].cur = b.pos;
-                b.pos += static_cast<unsigned long long>(n_int) * static_cast<unsigned>(ax[d].bw);
-                bad = bad || b.pos > b.limit;
+                ax[d].base = b.pos;
+                const unsigned long long e = b.pos + static_cast<unsigned long long>(n_int) * static_cast<unsigned>(ax[d].bw);
+                bad = bad || e > b.limit;
+                if (!bad) b.seek(e);
             } else if (ax[d].tag == 1 || ax[d].tag == 2) {
                 ax[d].k = static_cast<int>(b.bits(8));
                 bad = bad || ax[d].k > kP5MaxK;
-                ax[d].cur = b.pos;
+                ax[d].r.seek(b.pos);
                 for (int i = 0; i < n_int && !bad && !b.bad; i++) (void)(ax[d].tag == 1 ? b.rice(ax[d].k) : b.eg(ax[d].k));
             } else {
                 bad = true;  // ValueError("bad tag")
@@ -336,18 +379,22 @@ __global__ void __launch_bounds__(128) p5_decode_kernel(P5Args a, uint32_t per_w
         const int rc = static_cast<int>(e >> 24);
         const bool para = ra != v;  // roots are stored as (v, v, v, v)
         const unsigned long long out = 3ull * row_of(v);
+        const unsigned long long oa = para ? 3ull * row_of(ra) : 0ull;
+        const unsigned long long ob = para ? 3ull * row_of(rbv) : 0ull;
+        const unsigned long long oc = para ? 3ull * row_of(rc) : 0ull;
         for (int d = 0; d < 3; d++) {
-            const long long code = p5_code(b, ax[d], static_cast<uint32_t>(i));
+            const long long code = p5_code(ax[d], static_cast<uint32_t>(i), bad);
             double pred = fb[d];
             if (para) {
-                const double t0 = __dmul_rn(a.w0, a.rows[3ull * row_of(ra) + d]);
-                const double t1 = __dmul_rn(a.w1, a.rows[3ull * row_of(rbv) + d]);
-                const double t2 = __dmul_rn(a.w2, a.rows[3ull * row_of(rc) + d]);
+                const double t0 = __dmul_rn(a.w0, a.rows[oa + d]);
+                const double t1 = __dmul_rn(a.w1, a.rows[ob + d]);
+                const double t2 = __dmul_rn(a.w2, a.rows[oc + d]);
                 pred = __dadd_rn(__dadd_rn(t0, t1), t2);
             }
             a.rows[out + d] = __dadd_rn(pred, __dmul_rn(static_cast<double>(code), a.delta));
         }
     }
+    if (bad) p5_report(a.status, kErrCorrupt, m);  // cannot happen: the substreams were read once already
 }
 
 // rows -> f32(row * scale + center)
