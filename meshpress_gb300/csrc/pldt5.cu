@@ -172,229 +172,245 @@ struct P5Axis {
     P5Bits r;                 // the next code (tags 1, 2)
 };
 
-__device__ __forceinline__ long long p5_code(P5Axis& ax, uint32_t i, bool& bad) {
-    if (ax.tag == 0)
-        return ax.mn + static_cast<long long>(p5_bits_at(ax.r.w, ax.base + static_cast<unsigned long long>(i) *
-                                                                             static_cast<unsigned>(ax.bw),
-                                                         ax.bw, ax.r.limit, bad));
-    const unsigned long long u = ax.tag == 1 ? ax.r.rice(ax.k) : ax.r.eg(ax.k);
-    bad = bad || ax.r.bad;
-    return unzig(u);
+
+// One codeword of a Rice (eg false) or Exp-Golomb substream through its
+// window: a straight-line read when prefix, terminator and value fit the
+// 32-bit window, the general reader otherwise (rare; a branch taken by
+// single lanes).  u is the codeword's value.
+__device__ __forceinline__ unsigned long long p5_codeword(P5Bits& r, bool eg, int k) {
+    const uint32_t x = r.peek();
+    const uint32_t z = static_cast<uint32_t>(__clz(x));
+    const uint32_t nb = (eg ? z : 0u) + static_cast<uint32_t>(k);
+    const uint32_t len = z + 1u + nb;
+    if (len > 32u || r.pos + len > r.limit) return eg ? r.eg(k) : r.rice(k);
+    const uint32_t t = __funnelshift_lc(0u, x, z + 1u);      // bits after the terminator
+    const uint32_t val = nb ? (t >> (32u - nb)) : 0u;        // the top nb of them
+    const unsigned long long base = eg ? ((1ull << z) - 1ull) : static_cast<unsigned long long>(z);
+    r.skip(len);
+    return (base << k) + val;
 }
 
-// One token's local id through the FIFO of the 16 most recently used ids
-// (_read_vert, encoder/paradelta_codec.py:330-340): a move-to-front register
-// (depth 0 the newest, so the FIFO index fi, 0 the oldest, is depth
-// len - 1 - fi), an id found in it moved to the front, a new one pushed
-// (the oldest leaving a full FIFO).
-__device__ __forceinline__ int p5_vert(P5Bits& b, MtfFifo& f, int idx_bits, const uint4* masks, bool& bad) {
-    uint32_t x, at;
-    if (b.bits(1) == 0u) {
-        const uint32_t fi = b.bits(5);
-        if (fi >= f.len) {
-            bad = true;
-            return 0;
-        }
-        at = f.len - 1u - fi;
-        x = f.at(at);
-    } else {
-        x = b.bits(idx_bits);
-        at = x < 256u ? f.find(x) : 16u;
-    }
-    const bool fresh = at == 16u;
-    f.mtf_masked(x & 0xFFu, masks[fresh ? min(f.len, 15u) : at]);
-    f.len += (fresh && f.len < 16u) ? 1u : 0u;
-    return static_cast<int>(x);
-}
+constexpr int kP5Threads = 64;     // meshlets (lanes) per block
+constexpr int kP5RefCache = 128;   // a lane's first boundary references kept in shared memory
 
-// Lane l < per_warp of warp w decodes meshlet w * per_warp + l: the lanes of
-// a warp take different branches on almost every token, so a stream with
-// few meshlets gets one per warp, spread over the SMs.
-__global__ void __launch_bounds__(128) p5_decode_kernel(P5Args a, uint32_t per_warp) {
-    __shared__ uint4 masks[16];
-    __shared__ uint32_t seen_all[8 * 128];  // each thread's first-reach bits: word i at [i * 128 + thread]
-    if (threadIdx.x < 16u) masks[threadIdx.x] = mtf_mask_row(threadIdx.x);
+// One lane per meshlet, 32 meshlets per warp, every phase a loop that the
+// whole warp runs to its longest lane's count (no branch per token: the
+// lanes stay together), as in the DPR4 kernels:
+//  1. the meshlet header and its boundary references (:350-361), the first
+//     kP5RefCache of them into shared memory;
+//  2. connectivity, one token per iteration (strip header, roots, strip
+//     bodies; the FIFO as a move-to-front register), triangles written as
+//     rows, first-reach order of the interior vertices (:371-400);
+//  3. the three residual substreams' starts (:403-424);
+//  4. the float64 reconstruction in walk order (:426-445).
+// Validity is checked lazily: running extremes and counts compared once per
+// meshlet, ids clamped below n_local and writes bounded by the header's
+// counts until then, so a corrupt lane runs on harmlessly and is reported.
+__global__ void __launch_bounds__(kP5Threads) p5_decode_kernel(P5Args a) {
+    __shared__ uint4 masks[17];
+    __shared__ uint32_t seen_all[8 * kP5Threads];           // word i of lane t at [i * kP5Threads + t]
+    __shared__ uint32_t ref_all[kP5RefCache * kP5Threads];  // reference l of lane t at [l * kP5Threads + t]
+    if (threadIdx.x < 17u) masks[threadIdx.x] = threadIdx.x < 16u ? mtf_mask_row(threadIdx.x) : make_uint4(0u, 0u, 0u, 0u);
     __syncthreads();
-    const uint32_t lane = threadIdx.x & 31u;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (lane >= per_warp) return;
-    const uint32_t m = warp * per_warp + lane;
-    if (m >= a.n_meshlets) return;
-    const unsigned long long s0 = a.start[m], s1 = a.start[m + 1];
-    const bool last = m + 1 == a.n_meshlets;
+    const uint32_t m = blockIdx.x * kP5Threads + threadIdx.x;
+    bool act = m < a.n_meshlets;
+    const uint32_t mm = act ? m : 0u;
+    const unsigned long long s0 = a.start[mm], s1 = a.start[mm + 1u];
+    const bool last = mm + 1u == a.n_meshlets;
     const uint32_t* words = reinterpret_cast<const uint32_t*>(a.blob);
     P5Bits b;
     b.w = words;
     b.limit = a.nbits;
     b.bad = false;
-    b.seek(s0);
-    bool bad = false;
-    const int n_bnd = static_cast<int>(b.bits(16));
-    const int n_int = static_cast<int>(b.bits(16));
-    const int n_tris = static_cast<int>(b.bits(16));
-    const int n_strips = static_cast<int>(b.bits(16));
-    const int n_local = n_bnd + n_int;
-    if (n_local > kP5MaxLocal) {
+    b.seek(act ? s0 : 0ull);
+    uint32_t n_bnd = b.bits(16), n_int = b.bits(16), n_tris = b.bits(16), n_strips = b.bits(16);
+    uint32_t n_local = n_bnd + n_int;
+    bool bad = b.bad;
+    if (act && n_local > static_cast<uint32_t>(kP5MaxLocal)) {
         p5_report(a.status, kErrUnsupported, m);
-        return;
+        act = false;
     }
-    const uint32_t rb = a.ref_base[m];
-    const uint32_t row0 = a.row_base[m];
-    uint32_t* tri = a.idx + 3ull * a.tri_base[m];
-    // boundary references (:350-361); the decoder reads them as rows of the
-    // boundary table (a stream whose references point past it is rejected)
-    if (n_bnd > 0) {
+    bad = bad || n_strips > n_tris;  // every strip emits a triangle
+    if (!act || bad) n_bnd = n_int = n_tris = n_strips = n_local = 0u;
+    const uint32_t rb = act ? a.ref_base[m] : 0u;
+    const uint32_t row0 = act ? a.row_base[m] : 0u;
+    uint32_t* tri = a.idx + 3ull * (act ? a.tri_base[m] : 0u);
+    uint32_t* refc = ref_all + threadIdx.x;
+    // 1. boundary references; the decoder reads them as rows of the boundary
+    // table (a stream whose references point past it is rejected)
+    if (n_bnd > 0u) {
         unsigned long long prev = b.bits(32);
-        a.refs[rb] = static_cast<uint32_t>(prev);
         bad = bad || prev >= a.n_boundary;
-        if (n_bnd > 1) {
-            const int k = static_cast<int>(b.bits(8));
-            bad = bad || k > kP5MaxK;
-            for (int i = 1; i < n_bnd && !bad && !b.bad; i++) {
-                prev = prev + b.rice(k) + 1ull;
-                bad = bad || prev >= a.n_boundary;
-                a.refs[rb + i] = static_cast<uint32_t>(prev);
-            }
+        a.refs[rb] = static_cast<uint32_t>(prev);
+        refc[0] = static_cast<uint32_t>(prev);
+        const int k = n_bnd > 1u ? static_cast<int>(b.bits(8)) : 0;
+        bad = bad || k > kP5MaxK;
+        for (uint32_t i = 1; i < n_bnd && !bad; i++) {
+            prev = prev + p5_codeword(b, false, k) + 1ull;
+            bad = bad || b.bad || prev >= a.n_boundary;
+            a.refs[rb + i] = static_cast<uint32_t>(prev);
+            if (i < static_cast<uint32_t>(kP5RefCache)) refc[i * kP5Threads] = static_cast<uint32_t>(prev);
         }
     }
-    auto row_of = [&](int l) -> unsigned long long {
-        return l < n_bnd ? __ldcg(a.refs + rb + l) : row0 + static_cast<unsigned>(l - n_bnd);
+    auto row_of = [&](uint32_t l) -> uint32_t {
+        if (l >= n_bnd) return row0 + (l - n_bnd);
+        return l < static_cast<uint32_t>(kP5RefCache) ? refc[l * kP5Threads] : __ldcg(a.refs + rb + l);
     };
-    // connectivity and first-reach order (:371-400)
+    // 2. connectivity
     uint32_t* seen = seen_all + threadIdx.x;
 #pragma unroll
-    for (int i = 0; i < 8; i++) seen[i * 128] = 0u;
-    for (int l = 0; l < n_bnd; l++) seen[(l >> 5) * 128] |= 1u << (l & 31);
-    int idx_bits = 1;
-    while ((1 << idx_bits) <= n_local) idx_bits++;  // max(1, ceil(log2(n_local + 1)))
+    for (int i = 0; i < 8; i++) {
+        const uint32_t lo = 32u * i;
+        seen[i * kP5Threads] = n_bnd >= lo + 32u ? 0xFFFFFFFFu : (n_bnd > lo ? (1u << (n_bnd - lo)) - 1u : 0u);
+    }
+    const uint32_t idx_bits = max(1u, 32u - __clz(n_local));  // max(1, ceil(log2(n_local + 1)))
+    const uint32_t rsh = 32u - idx_bits, vmax = n_local ? n_local - 1u : 0u;
     MtfFifo f;
-    int n_t = 0, n_emit = 0;
-    auto reach = [&](int v, uint32_t entry) {
-        uint32_t* sp = seen + (v >> 5) * 128;
-        const uint32_t sw = *sp;
-        const uint32_t bit = 1u << (v & 31);
-        if (v >= n_bnd && !(sw & bit)) {
-            if (n_emit >= n_int) {
-                bad = true;
-            } else {
-                a.walk[row0 + n_emit] = entry;
+    uint32_t sl = n_strips, tl = 0u, tx = 0u, P = 0u, n_t = 0u, n_emit = 0u, ridmax = 0u;
+    int32_t smin = 0;
+    bool live = act && !bad && sl > 0u;
+    const uint32_t iters = __reduce_max_sync(0xFFFFFFFFu, live ? n_tris + 2u * n_strips : 0u);
+    for (uint32_t it = 0; it < iters; it++) {
+        const uint32_t x0 = b.peek();
+        const bool hdr = tl == 0u;                     // strip header (:376)
+        const uint32_t sb = max(x0 >> 16, 1u) - 1u;   // body tokens of the strip
+        tl = hdr ? sb + 3u : tl;
+        sl -= hdr ? 1u : 0u;
+        const uint32_t tix = hdr ? 0u : tx;
+        uint32_t x = hdr ? (x0 << 16) : x0;
+        uint32_t used = hdr ? 16u : 0u;
+        const bool body = tix == 3u;
+        const uint32_t ec = x >> 31;  // edge bit of a strip-body token
+        x = body ? (x << 1) : x;
+        used += body ? 1u : 0u;
+        const bool raw = static_cast<int32_t>(x) < 0;  // _read_vert's flag
+        const uint32_t y = x << 1;
+        const uint32_t rid = y >> rsh;
+        const uint32_t fi = y >> 27;
+        used += raw ? 1u + idx_bits : 6u;
+        // IndexError on a FIFO index past the entries or an id past n_local
+        const int32_t sd = static_cast<int32_t>(f.len) - 1 - static_cast<int32_t>(fi);
+        smin = min(smin, (raw | !live) ? 0 : sd);
+        ridmax = max(ridmax, (raw & live) ? rid + 1u : 0u);
+        const uint32_t sdep = static_cast<uint32_t>(sd) & 15u;
+        const uint32_t v = raw ? (rid & 0xFFu) : f.at(sdep);
+        const uint32_t at = raw ? f.find(v) : sdep;
+        const bool fresh = at == 16u;
+        f.mtf_masked(v, masks[live ? (fresh ? min(f.len, 15u) : at) : 16u]);  // row 16: no change
+        f.len += (live & fresh & (f.len < 16u)) ? 1u : 0u;
+        if (live) {
+            const uint32_t u = min(v, vmax);
+            // edge 0 -> (p1, p2 | p0), 1 -> (p0, p2 | p1) (:386-391); a root
+            // token puts u at its position
+            const uint32_t sel = body ? (ec ? 0x7420u : 0x7421u) : (0x7210u + ((4u - tix) << (4u * tix)));
+            const uint32_t cref = ec ? ((P >> 8) & 0xFFu) : (P & 0xFFu);
+            const uint32_t Pn = __byte_perm(P, u, sel);
+            if ((body | (tix == 2u)) && n_t < n_tris) {
+                tri[3u * n_t] = row_of(Pn & 0xFFu);
+                tri[3u * n_t + 1u] = row_of((Pn >> 8) & 0xFFu);
+                tri[3u * n_t + 2u] = row_of((Pn >> 16) & 0xFFu);
+            }
+            n_t += (body | (tix == 2u)) ? 1u : 0u;
+            // first reach of an interior vertex (boundary bits are preset)
+            uint32_t* sp = seen + (u >> 5) * kP5Threads;
+            const uint32_t sw = *sp;
+            const uint32_t bit = 1u << (u & 31u);
+            if ((sw & bit) == 0u) {
+                *sp = sw | bit;
+                if (n_emit < n_int)
+                    a.walk[row0 + n_emit] = body ? (u | ((Pn & 0xFFFFu) << 8) | (cref << 24)) : u * 0x01010101u;
                 n_emit++;
             }
+            P = Pn;
         }
-        *sp = sw | bit;
-    };
-    auto put_tri = [&](int x, int y, int z) {
-        if (n_t >= n_tris) {
-            bad = true;
-            return;
-        }
-        tri[3 * n_t] = static_cast<uint32_t>(row_of(x));
-        tri[3 * n_t + 1] = static_cast<uint32_t>(row_of(y));
-        tri[3 * n_t + 2] = static_cast<uint32_t>(row_of(z));
-        n_t++;
-    };
-    for (int s = 0; s < n_strips && !bad && !b.bad; s++) {
-        const int strip_len = static_cast<int>(b.bits(16));
-        int v[3];
-        for (int j = 0; j < 3; j++) {
-            v[j] = p5_vert(b, f, idx_bits, masks, bad);
-            bad = bad || v[j] >= n_local;
-        }
-        if (bad || b.bad) break;
-        put_tri(v[0], v[1], v[2]);
-        for (int j = 0; j < 3; j++) reach(v[j], static_cast<uint32_t>(v[j]) * 0x01010101u);
-        int p0 = v[0], p1 = v[1], p2 = v[2];
-        for (int t = 0; t + 1 < strip_len && !bad && !b.bad; t++) {
-            const uint32_t edge = b.bits(1);
-            const int nv = p5_vert(b, f, idx_bits, masks, bad);
-            if (nv >= n_local) bad = true;
-            if (bad || b.bad) break;
-            int x, y, c;
-            if (edge == 0u) {
-                x = p1; y = p2; c = p0;
-            } else {
-                x = p0; y = p2; c = p1;
-            }
-            put_tri(x, y, nv);
-            reach(nv, static_cast<uint32_t>(nv) | static_cast<uint32_t>(x) << 8 | static_cast<uint32_t>(y) << 16 |
-                          static_cast<uint32_t>(c) << 24);
-            p0 = x; p1 = y; p2 = nv;
-        }
+        tl--;
+        tx = min(tix + 1u, 3u);
+        b.skip(live ? used : 0u);
+        live = live & ((tl | sl) != 0u) & (b.pos <= b.limit);
     }
-    bad = bad || b.bad || n_t != n_tris;  // the header's count must match the strips
-    // residual substreams (:403-424): find each axis' start
+    bad = bad || live || b.pos > b.limit || smin < 0 || ridmax > n_local || n_t != n_tris || n_emit > n_int;
+    // 3. residual substreams: tag, then fixed width (tag 0: minimum and width,
+    // random access) or Rice / Exp-Golomb (tags 1, 2: k); each axis' start
     P5Axis ax[3];
-    if (!bad && n_int > 0) {
-        for (int d = 0; d < 3 && !bad; d++) {
-            ax[d].tag = static_cast<int>(b.bits(8));
-            ax[d].k = 0;
-            ax[d].bw = 0;
-            ax[d].mn = 0;
-            ax[d].base = 0ull;
-            ax[d].r.w = words;
-            ax[d].r.limit = a.nbits;
-            ax[d].r.bad = false;
-            if (ax[d].tag == 0) {
-                const uint32_t mn_u = b.bits(16);
-                ax[d].mn = (mn_u & 0x8000u) ? static_cast<long long>(mn_u) - 0x10000 : mn_u;
-                ax[d].bw = static_cast<int>(b.bits(8));
-                bad = bad || ax[d].bw > kP5MaxWidth;
-                ax[d].base = b.pos;
-                const unsigned long long e = b.pos + static_cast<unsigned long long>(n_int) * static_cast<unsigned>(ax[d].bw);
-                bad = bad || e > b.limit;
-                if (!bad) b.seek(e);
-            } else if (ax[d].tag == 1 || ax[d].tag == 2) {
-                ax[d].k = static_cast<int>(b.bits(8));
-                bad = bad || ax[d].k > kP5MaxK;
-                ax[d].r.seek(b.pos);
-                for (int i = 0; i < n_int && !bad && !b.bad; i++) (void)(ax[d].tag == 1 ? b.rice(ax[d].k) : b.eg(ax[d].k));
-            } else {
-                bad = true;  // ValueError("bad tag")
-            }
-            bad = bad || b.bad;
+    const bool vx = act && !bad && n_int > 0u;
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+        ax[d].tag = vx ? static_cast<int>(b.bits(8)) : 1;
+        ax[d].k = 0;
+        ax[d].bw = 0;
+        ax[d].mn = 0;
+        ax[d].base = 0ull;
+        ax[d].r.w = words;
+        ax[d].r.limit = a.nbits;
+        ax[d].r.bad = false;
+        if (ax[d].tag == 0) {
+            const uint32_t mn_u = b.bits(16);
+            ax[d].mn = (mn_u & 0x8000u) ? static_cast<long long>(mn_u) - 0x10000 : mn_u;
+            ax[d].bw = static_cast<int>(b.bits(8));
+            bad = bad || ax[d].bw > kP5MaxWidth;
+            ax[d].base = b.pos;
+            const unsigned long long e = b.pos + static_cast<unsigned long long>(n_int) * static_cast<unsigned>(ax[d].bw);
+            bad = bad || e > b.limit;
+            if (vx && !bad) b.seek(e);
+        } else if (ax[d].tag == 1 || ax[d].tag == 2) {
+            ax[d].k = vx ? static_cast<int>(b.bits(8)) : 0;
+            bad = bad || ax[d].k > kP5MaxK;
+            ax[d].r.seek(vx ? b.pos : 0ull);
+        } else {
+            bad = true;  // ValueError("bad tag")
         }
+        // the substream's codewords, skipped (every lane of the warp takes
+        // part in the count)
+        const bool skipping = vx && !bad && (ax[d].tag == 1 || ax[d].tag == 2);
+        const uint32_t n = __reduce_max_sync(0xFFFFFFFFu, skipping ? n_int : 0u);
+        for (uint32_t i = 0; i < n; i++)
+            if (skipping && i < n_int) (void)p5_codeword(b, ax[d].tag == 2, ax[d].k);
+        bad = bad || b.bad;
     }
     // meshlets lie back to back, as the CPU decoder reads them
-    bad = bad || (last ? b.pos > a.nbits : b.pos != s1);
-    if (bad) {
-        p5_report(a.status, kErrCorrupt, m);
-        return;
+    if (act) {
+        bad = bad || (last ? b.pos > a.nbits : b.pos != s1);
+        if (bad) p5_report(a.status, kErrCorrupt, m);
     }
-    if (n_int == 0) return;
-    // reconstruction in float64, in the reference's operation order, no
+    // 4. reconstruction in float64, in the reference's operation order, no
     // contraction (:426-445)
+    const bool rec = act && !bad && n_int > 0u;
     double fb[3] = {0.0, 0.0, 0.0};
-    if (n_bnd > 0) {
+    if (rec && n_bnd > 0u) {
         for (int d = 0; d < 3; d++) {
-            double s = a.rows[3ull * a.refs[rb] + d];
-            for (int i = 1; i < n_bnd; i++) s = __dadd_rn(s, a.rows[3ull * a.refs[rb + i] + d]);
+            double s = a.rows[3ull * row_of(0u) + d];
+            for (uint32_t i = 1; i < n_bnd; i++) s = __dadd_rn(s, a.rows[3ull * row_of(i) + d]);
             fb[d] = __ddiv_rn(s, static_cast<double>(n_bnd));
         }
     }
-    for (int i = 0; i < n_emit; i++) {
-        const uint32_t e = a.walk[row0 + i];
-        const int v = static_cast<int>(e & 0xFFu);
-        const int ra = static_cast<int>((e >> 8) & 0xFFu);
-        const int rbv = static_cast<int>((e >> 16) & 0xFFu);
-        const int rc = static_cast<int>(e >> 24);
+    const uint32_t ne = __reduce_max_sync(0xFFFFFFFFu, rec ? n_emit : 0u);
+    for (uint32_t i = 0; i < ne; i++) {
+        if (!rec || i >= n_emit) continue;
+        const uint32_t e = __ldcg(a.walk + row0 + i);
+        const uint32_t v = e & 0xFFu, ra = (e >> 8) & 0xFFu, rbv = (e >> 16) & 0xFFu, rc = e >> 24;
         const bool para = ra != v;  // roots are stored as (v, v, v, v)
         const unsigned long long out = 3ull * row_of(v);
-        const unsigned long long oa = para ? 3ull * row_of(ra) : 0ull;
-        const unsigned long long ob = para ? 3ull * row_of(rbv) : 0ull;
-        const unsigned long long oc = para ? 3ull * row_of(rc) : 0ull;
+        const unsigned long long oa = 3ull * row_of(ra), ob = 3ull * row_of(rbv), oc = 3ull * row_of(rc);
+#pragma unroll
         for (int d = 0; d < 3; d++) {
-            const long long code = p5_code(ax[d], static_cast<uint32_t>(i), bad);
+            long long code;
+            if (ax[d].tag == 0) {
+                code = ax[d].mn + static_cast<long long>(p5_bits_at(words, ax[d].base + static_cast<unsigned long long>(i) *
+                                                                               static_cast<unsigned>(ax[d].bw),
+                                                                    ax[d].bw, a.nbits, bad));
+            } else {
+                code = unzig(p5_codeword(ax[d].r, ax[d].tag == 2, ax[d].k));
+            }
             double pred = fb[d];
             if (para) {
-                const double t0 = __dmul_rn(a.w0, a.rows[oa + d]);
-                const double t1 = __dmul_rn(a.w1, a.rows[ob + d]);
-                const double t2 = __dmul_rn(a.w2, a.rows[oc + d]);
+                const double t0 = __dmul_rn(a.w0, __ldcg(a.rows + oa + d));
+                const double t1 = __dmul_rn(a.w1, __ldcg(a.rows + ob + d));
+                const double t2 = __dmul_rn(a.w2, __ldcg(a.rows + oc + d));
                 pred = __dadd_rn(__dadd_rn(t0, t1), t2);
             }
             a.rows[out + d] = __dadd_rn(pred, __dmul_rn(static_cast<double>(code), a.delta));
         }
     }
-    if (bad) p5_report(a.status, kErrCorrupt, m);  // cannot happen: the substreams were read once already
 }
 
 // rows -> f32(row * scale + center)
@@ -697,11 +713,8 @@ int pldt5_decode(pldt5_handle* h, void* stream, uint32_t* d_idx, float* d_pos) {
         a.w2 = h->w[2];
         a.delta = h->delta;
         a.status = h->d_status;
-        // about sixteen busy warps per SM, at most 32 meshlets per warp
-        const uint64_t target = 16ull * static_cast<uint64_t>(device_sm_count());
-        const uint32_t per_warp = static_cast<uint32_t>(std::min<uint64_t>(32, std::max<uint64_t>(1, (M + target - 1) / target)));
-        const uint64_t warps = (M + per_warp - 1) / per_warp;
-        p5_decode_kernel<<<static_cast<uint32_t>((warps + 3) / 4), 128, 0, s>>>(a, per_warp);
+        // one lane per meshlet (kP5Threads per block)
+        p5_decode_kernel<<<static_cast<uint32_t>((M + kP5Threads - 1) / kP5Threads), kP5Threads, 0, s>>>(a);
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "p5_decode_kernel");
     }
     if (rows) {
