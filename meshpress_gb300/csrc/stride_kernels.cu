@@ -171,6 +171,11 @@ __device__ __forceinline__ void lut_block(const DecodeArgs& a, uint32_t b, uint3
 // meshlet of rank i, so a group's lanes have about the same work.  Outputs
 // are placed per meshlet, so the order changes no result.
 __global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a, uint32_t nb, uint32_t lut_bx) {
+    // The fused kernel may be scheduled once every block of this launch has
+    // started (it waits for this grid's completion before it reads
+    // anything): its launch latency then overlaps this kernel, and it never
+    // holds an SM that a block of this launch still needs.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     if (blockIdx.x >= nb) {  // block-uniform
         lut_block(a, blockIdx.x - nb, lut_bx);
         return;
@@ -952,6 +957,10 @@ __global__ void __launch_bounds__(128, kMinBlocks) flow_kernel(DecodeArgs a, uin
     __shared__ uint4 mtf_masks[17];
     __shared__ uint32_t s_redo[2];
     if (threadIdx.x < 17u) mtf_masks[threadIdx.x] = threadIdx.x < 16u ? mtf_mask_row(threadIdx.x) : make_uint4(0u, 0u, 0u, 0u);
+    // launched as the scan's programmatic dependent: nothing the scan or the
+    // status reset writes is read before the scan grid has completed (a
+    // no-op after an ordinary launch)
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     const uint32_t warp = threadIdx.x >> 5;
     const int lane = threadIdx.x & 31;
     const bool failed = *reinterpret_cast<volatile unsigned long long*>(&a.status->err) != 0ull;
@@ -1093,7 +1102,7 @@ size_t flow_cta_bytes(const LaunchCfg& cfg) {
 }
 
 template <bool kWide, int kMinBlocks>
-cudaError_t launch_flow(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s) {
+cudaError_t launch_flow(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s, bool after_scan) {
     static size_t configured[64] = {0};
     static OccCache occ;
     const size_t smem = flow_cta_bytes(cfg);
@@ -1105,9 +1114,24 @@ cudaError_t launch_flow(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t 
     // group left go straight to it
     const uint32_t grid = grid_for(flow_kernel<kWide, kMinBlocks>, 128, smem, cfg, n_groups, 1, occ);
     if (grid == 0) return cudaSuccess;
-    flow_kernel<kWide, kMinBlocks><<<grid, 128, smem, s>>>(a, cfg.stage_bytes, cfg.code_bytes);
+    if (after_scan) {  // the scan kernel directly before it on the stream
+        cudaLaunchConfig_t lc = {};
+        lc.gridDim = dim3(grid);
+        lc.blockDim = dim3(128);
+        lc.dynamicSmemBytes = smem;
+        lc.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        lc.attrs = attr;
+        lc.numAttrs = 1;
+        e = cudaLaunchKernelEx(&lc, flow_kernel<kWide, kMinBlocks>, a, cfg.stage_bytes, cfg.code_bytes);
+    } else {
+        flow_kernel<kWide, kMinBlocks><<<grid, 128, smem, s>>>(a, cfg.stage_bytes, cfg.code_bytes);
+        e = cudaGetLastError();
+    }
     note_launch(static_cast<uint32_t>(smem), grid);
-    return cudaGetLastError();
+    return e;
 }
 
 // Groups from which the fused kernel is budgeted for five CTAs per SM.
@@ -1117,10 +1141,11 @@ cudaError_t launch_flow(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t 
 // 2,700 groups: 432 against 460 us; 4,096 mixed meshes: 3.84 against 4.19 ms).
 constexpr uint32_t kFlowFiveGroups = 1024u;
 
-cudaError_t launch_flow_any(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s) {
+cudaError_t launch_flow_any(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t s, bool after_scan) {
     const bool five = (a.total_meshlets + 31u) / 32u >= kFlowFiveGroups;
-    if (a.wide_codes) return five ? launch_flow<true, 5>(a, cfg, s) : launch_flow<true, 4>(a, cfg, s);
-    return five ? launch_flow<false, 5>(a, cfg, s) : launch_flow<false, 4>(a, cfg, s);
+    if (a.wide_codes)
+        return five ? launch_flow<true, 5>(a, cfg, s, after_scan) : launch_flow<true, 4>(a, cfg, s, after_scan);
+    return five ? launch_flow<false, 5>(a, cfg, s, after_scan) : launch_flow<false, 4>(a, cfg, s, after_scan);
 }
 
 // ev[k] is recorded when ev and ev[k] are non-null
@@ -1215,7 +1240,9 @@ int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void
             e = launch_group(a, cfg, s);
             record(ev, 2, s);
         } else if (cfg.persistent == 2) {  // one kernel: the connectivity/vertex split is not timed
-            e = launch_flow_any(a, cfg, s);
+            // without timing events between them, the fused kernel is the
+            // scan's programmatic dependent
+            e = launch_flow_any(a, cfg, s, ev == nullptr);
             record(ev, 2, s);
         } else {
             switch (cfg.warps_per_cta) {
