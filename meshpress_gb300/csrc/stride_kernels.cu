@@ -727,7 +727,7 @@ __device__ __forceinline__ void vert_axis(const DecodeArgs& a, const GroupLane& 
 // code counts) -- decode axis d of their meshlets, then the warp writes that
 // coordinate of every vertex.  The three warps skip independently: waiting
 // for one another's skips measured slower than repeating them.
-template <bool kShared, bool kWide>
+template <bool kShared, bool kWide, bool kPair>
 __device__ __forceinline__ void vert_round(const DecodeArgs& a, const GroupLane& L, uint32_t d, bool act,
                                            uint32_t rmask, const uint32_t* w, uint32_t rbase, uint8_t* planes,
                                            uint32_t code_off, int lane) {
@@ -765,7 +765,7 @@ __device__ __forceinline__ void vert_round(const DecodeArgs& a, const GroupLane&
     PlaneT<kWide>* plane = reinterpret_cast<PlaneT<kWide>*>(planes + code_off);
     if (act && !S.bad) vert_axis<kShared, kWide>(a, L, d, w, rbase, plane, S);
     __syncwarp();
-    emit_axis<kWide>(a, L, rmask, planes, code_off, d, lane);
+    emit_axis<kWide, kPair>(a, L, rmask, planes, code_off, d, lane);
     if (act) {
         // pz, the last substream, must end where the next meshlet starts (:507)
         const MeshParams* P = L.P;
@@ -779,7 +779,7 @@ __device__ __forceinline__ void vert_round(const DecodeArgs& a, const GroupLane&
 // fourth warp, d = 3, only joins the CTA's barriers and the stage pass); the
 // group's residual bits are staged once and read by all three axis warps.
 // False when a stage copy did not arrive in time (reported).
-template <bool kWide>
+template <bool kWide, bool kPair>
 __device__ __forceinline__ bool vert_group(const DecodeArgs& a, uint32_t g, uint32_t d, int lane, uint32_t* stage,
                                            uint8_t* planes, uint64_t* bar, uint32_t& phase, uint32_t vstage,
                                            uint32_t code_bytes) {
@@ -852,9 +852,9 @@ __device__ __forceinline__ bool vert_group(const DecodeArgs& a, uint32_t g, uint
                 __syncthreads();
             }
             const uint32_t rbase = static_cast<uint32_t>(L.blob_off * 8ull - src16 * 8ull + dst_off * 8ull);
-            if (d < 3u) vert_round<true, kWide>(a, L, d, act, rmask, stage, rbase, planes, code_off, lane);
+            if (d < 3u) vert_round<true, kWide, kPair>(a, L, d, act, rmask, stage, rbase, planes, code_off, lane);
         } else if (d < 3u) {
-            vert_round<false, kWide>(a, L, d, act, rmask,
+            vert_round<false, kWide, kPair>(a, L, d, act, rmask,
                                      reinterpret_cast<const uint32_t*>(a.arena + L.blob_off), 0u, planes,
                                      code_off, lane);
         }
@@ -888,7 +888,7 @@ __global__ void __launch_bounds__(96, 5) vert_kernel(DecodeArgs a, uint32_t stag
         f = s_group;
     }
     while (f < n_groups) {
-        if (!vert_group<kWide>(a, group_at(f, n_groups), d, lane, stage, planes, bar, phase, vstage, code_bytes))
+        if (!vert_group<kWide, true>(a, group_at(f, n_groups), d, lane, stage, planes, bar, phase, vstage, code_bytes))
             return;
         if (!persistent) break;
         __syncthreads();  // every thread has read s_group
@@ -1003,7 +1003,7 @@ __global__ void __launch_bounds__(128, kMinBlocks) flow_kernel(DecodeArgs a, uin
         __syncthreads();
         const uint32_t g = s_group;
         if (g >= n_groups) return;
-        if (!vert_group<kWide>(a, g, warp, lane, stage, planes, bar, phase, vstage, code_bytes)) return;
+        if (!vert_group<kWide, false>(a, g, warp, lane, stage, planes, bar, phase, vstage, code_bytes)) return;
         __syncthreads();  // every thread has read s_group
     }
 }
