@@ -240,33 +240,6 @@ __device__ __forceinline__ void ring_fetch(uint32_t* ring, const uint8_t* src, u
     }
 }
 
-// The BitWin cursor over a lane ring.
-struct RingWin {
-    const uint32_t* __restrict__ ring;
-    uint32_t rbase, pos, w0, w1, w2;
-    __device__ __forceinline__ uint32_t at(uint32_t i) const { return bswap32(ring[i & (kLaneRingWords - 1u)]); }
-    __device__ __forceinline__ void seek(uint32_t p) {
-        pos = p;
-        const uint32_t i = (p + rbase) >> 5;
-        w0 = at(i);
-        w1 = at(i + 1u);
-        w2 = at(i + 2u);
-    }
-    __device__ __forceinline__ uint32_t peek() const { return __funnelshift_l(w1, w0, (pos + rbase) & 31u); }
-    __device__ __forceinline__ void advance(uint32_t len) {
-        const uint32_t np = pos + len;
-        const uint32_t i = (np + rbase) >> 5;
-        const bool cross = i != ((pos + rbase) >> 5);
-        pos = np;
-        if (cross) {
-            w0 = w1;
-            w1 = w2;
-            w2 = at(i + 2u);
-        }
-    }
-    // rotated index of the next word the window will load
-    __device__ __forceinline__ uint32_t next_word() const { return ((pos + rbase) >> 5) + 3u; }
-};
 
 // Output rings.  Each lane collects its triangles (packed local ids) and its
 // walk entries in a 32-slot row of shared memory; every kFlushEvery token

@@ -301,11 +301,14 @@ __host__ __device__ inline uint32_t vert_cta_bytes(uint32_t stage_bytes, uint32_
 // the parser passes on is clamped below n_local, and the assembler's
 // flushes never write past the meshlet's triangles or walk entries.
 //
-// Record: bits 0..7 vertex, bit 8 live (clear: no token), bit 9 edge code,
-// bits 10..11 token position in its strip (0..2 the three roots, 3 a
-// strip-body token).
+// Record: bits 0..8 the local id (a raw token's as read, up to ib <= 9
+// bits; a FIFO token's from the FIFO), bit 9 raw, bit 10 the edge bit (a
+// strip-body token's edge code), bits 11..12 token position in its strip
+// (0..2 the three roots, 3 a strip-body token), bit 13 live (clear: no
+// token).
 constexpr uint32_t kChunk = kChunkWords;  // iterations per ring chunk
 constexpr uint32_t kChunkDone = 1u << 31;  // count word: the parser has finished
+constexpr uint32_t kRecRaw = 1u << 9, kRecLive = 1u << 13;
 
 // Pair barrier slots: chunk c full, chunk c empty.
 __device__ __forceinline__ uint32_t bar_full(uint32_t c) { return c; }
@@ -333,7 +336,6 @@ __device__ bool conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
     const uint32_t n_local = L.d.counts0 & 0xFFFFu;
     const uint32_t ib = max(1u, 32u - __clz(n_local));  // _idx_bits_for (paradelta_codec.py:124-125)
     const uint32_t rsh = 32u - ib, ib1 = 1u + ib;
-    const uint32_t vmax = n_local ? n_local - 1u : 0u;
     const uint32_t end = L.d.end_bit;
     const unsigned long long s0 = (L.blob_off + (L.d.start_bit >> 3)) & ~15ull;
     const unsigned long long e16 = (L.blob_off + ((end + 7u) >> 3) + 15ull) & ~15ull;
@@ -344,15 +346,18 @@ __device__ bool conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
     ring_fetch(ring, src, avail, rot, 1u);
     cp_async_wait_all();
     uint32_t req = 2u;  // chunks requested
-    RingWin win;  // the token cursor (win.pos)
-    win.ring = ring;
-    win.rbase = static_cast<uint32_t>(L.blob_off * 8ull - s0 * 8ull) + 32u * rot;
-    win.pos = win.w0 = win.w1 = win.w2 = 0u;
-    if (act) win.seek(L.d.start_bit + 48u);
+    // bit window: words wi, wi + 1, wi + 2 of the lane's data (in bit order)
+    // in w0, w1, w2; `off` bits of w0 consumed; ri = rotated ring index of
+    // wi + 2 (word j of the data sits at ring[(j + rot) & 63])
+    const uint32_t base0 = static_cast<uint32_t>((s0 - L.blob_off) * 8ull);  // stream bit of the data's bit 0
+    const uint32_t q0 = act ? L.d.start_bit + 48u - base0 : 0u;
+    uint32_t off = q0 & 31u;
+    uint32_t ri = (q0 >> 5) + 2u + rot;
+    auto rw = [ring](uint32_t r) { return bswap32(ring[r & (kLaneRingWords - 1u)]); };
+    uint32_t w0 = rw(ri - 2u), w1 = rw(ri - 1u), w2 = rw(ri);
     uint32_t strips_left = L.d.n_strips;
     uint32_t tok_left = 0u, tx = 0u;
-    uint32_t ridmax = 0u;  // largest raw id + 1 (0: none)
-    int32_t smin = 0;      // smallest depth a FIFO token named (negative: past the entries)
+    int32_t smin = 0;  // smallest depth a FIFO token named (negative: past the entries)
     bool suspect = false;
     MtfFifo fifo;
     fifo.f0 = fifo.f1 = fifo.f2 = fifo.f3 = 0xFFFFFFFFu;
@@ -376,10 +381,10 @@ __device__ bool conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
             // No branch per token, so consecutive tokens' chains can overlap:
             // a lane that has finished keeps running the body on whatever
             // bits follow, but its window and FIFO no longer move and its
-            // records are empty.  A 32-bit window holds a strip header (16
+            // records are not live.  A 32-bit window holds a strip header (16
             // bits) plus the next token (at most 1 + 9 bits), or an edge code
             // plus a token.
-            const uint32_t x0 = win.peek();
+            const uint32_t x0 = __funnelshift_l(w1, w0, off);
             const bool hdr = tok_left == 0u;                 // strip header (paradelta_v5_dup.py:519)
             const uint32_t sb = max(x0 >> 16, 1u) - 1u;       // body tokens of the strip
             tok_left = hdr ? sb + 3u : tok_left;
@@ -397,11 +402,9 @@ __device__ bool conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
             const uint32_t fi = y >> 27;
             used += raw ? ib1 : 6u;
             // decode_dup raises IndexError on a FIFO index past the entries
-            // and on a local id past n_local: kept as a running min / max
+            // (a running min here; the local ids are checked by the assembler)
             const int32_t sd = static_cast<int32_t>(fifo.len) - 1 - static_cast<int32_t>(fi);
-            const bool rl = raw & live;
             smin = min(smin, (raw | !live) ? 0 : sd);
-            ridmax = max(ridmax, rl ? rid + 1u : 0u);
             const uint32_t s = static_cast<uint32_t>(sd) & 15u;  // depth of a FIFO token's entry
             const uint32_t v = raw ? (rid & 0xFFu) : fifo.at(s);
             bool fresh = raw;  // a raw id not in the FIFO
@@ -411,15 +414,23 @@ __device__ bool conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
                 fresh = raw & (at == 16u);
                 p = raw ? (fresh ? min(fifo.len, 15u) : at) : s;
             } else {
-                suspect = suspect | (rl & fifo.holds(v));
+                suspect = suspect | (raw & live & fifo.holds(v));
                 p = raw ? min(fifo.len, 15u) : s;
             }
             fifo.mtf_masked(v, mtf_masks[live ? p : 16u]);  // row 16 is zero: no change
             fifo.len += (live & fresh & (fifo.len < 16u)) ? 1u : 0u;
-            rc[i * 32u] = live ? (min(v, vmax) | 0x100u | ((body ? ec : 0u) << 9) | (tix << 10)) : 0u;
+            rc[i * 32u] = (raw ? (rid | kRecRaw) : v) | (ec << 10) | (tix << 11) | (live ? kRecLive : 0u);
             tok_left--;
             tx = min(tix + 1u, 3u);
-            win.advance(live ? used : 0u);
+            // advance: at most one word boundary per token (used <= 26)
+            off += live ? used : 0u;
+            const bool cross = off >= 32u;
+            off &= 31u;
+            ri += cross ? 1u : 0u;
+            const uint32_t nw = rw(ri);
+            w0 = cross ? w1 : w0;
+            w1 = cross ? w2 : w1;
+            w2 = cross ? nw : w2;
             live = live & ((tok_left | strips_left) != 0u);
         }
         it += n;
@@ -428,9 +439,11 @@ __device__ bool conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
         pair_bar<G, true>(pair, bar_full(c));
         k++;
         if (done) break;
-        // refill (the previous refill has had a record chunk to land)
+        // refill (the previous refill has had a record chunk to land): one
+        // more chunk when fewer than 33 words lie ahead of the window's next
+        // load
         cp_async_wait_all();
-        if (live && kLaneChunkWords * req < win.next_word() - rot + 33u) {
+        if (live && kLaneChunkWords * req < ri - rot + 34u) {
             ring_fetch(ring, src, avail, rot, req);
             req++;
         }
@@ -441,14 +454,15 @@ __device__ bool conn_parse(const DecodeArgs& a, const GroupLane& L, bool act, ui
     // barriers are clean
     for (uint32_t j = k >= 2u ? k - 2u : 0u; j < k; j++) pair_bar<G, false>(pair, bar_empty(j & 1u));
     if (act) {
-        // every strip read, ids and FIFO indices in range, inside the meshlet;
-        // a suspect lane's FIFO (and so its checks) may be off: its group
-        // runs again exactly
-        const bool bad = live || smin < 0 || ridmax > n_local || win.pos > end;
+        const uint32_t pos = base0 + 32u * (ri - 2u - rot) + off;  // the stream bit after the last token
+        // every strip read, FIFO indices in range, inside the meshlet; a
+        // suspect lane's FIFO (and so its checks) may be off: its group runs
+        // again exactly
+        const bool bad = live || smin < 0 || pos > end;
         if (bad && !suspect) {
             report(a.status, kErrCorrupt, L.m);
         } else if (!bad) {
-            a.descs[L.m].anchor_bit = win.pos;
+            a.descs[L.m].anchor_bit = pos;
         }
     }
     return act && suspect;
@@ -474,6 +488,8 @@ __device__ void conn_assemble(const DecodeArgs& a, const GroupLane& L, bool act,
     uint32_t flush_in = kFlushEvery;
     uint32_t P = 0u;  // strip state p0 | p1 << 8 | p2 << 16
     uint32_t tcnt = 0u, wcnt = 0u, kind0 = 0u;
+    const uint32_t vmax = n_local ? n_local - 1u : 0u;
+    uint32_t ridmax = 0u;  // largest raw id + 1 (0: none)
     for (uint32_t k = 0u;; k++) {
         const uint32_t c = k & 1u;
         pair_bar<G, false>(pair, bar_full(c));
@@ -482,11 +498,15 @@ __device__ void conn_assemble(const DecodeArgs& a, const GroupLane& L, bool act,
         const uint32_t* rc = recs + c * kChunk * 32u + lane;
         for (uint32_t i = 0; i < n; i++) {
             const uint32_t rec = rc[i * 32u];
-            if (rec & 0x100u) {
-                const uint32_t v = rec & 0xFFu;
-                const uint32_t ec = (rec >> 9) & 1u;
-                const uint32_t ti = (rec >> 10) & 3u;
+            if (rec & kRecLive) {
+                const uint32_t id = rec & 0x1FFu;
+                // decode_dup raises IndexError on a local id past n_local: a
+                // running max; ids stay below n_local, whatever the stream says
+                ridmax = max(ridmax, (rec & kRecRaw) ? id + 1u : 0u);
+                const uint32_t v = min(id, vmax);
+                const uint32_t ti = (rec >> 11) & 3u;
                 const bool body = ti == 3u;
+                const uint32_t ec = body ? (rec >> 10) & 1u : 0u;
                 // edge code 0 -> (p1, p2 | p0), 1 -> (p0, p2 | p1) (:530-535);
                 // a root token puts v at its position
                 const uint32_t sel = body ? (ec ? 0x7420u : 0x7421u) : (0x7210u + ((4u - ti) << (4u * ti)));
@@ -522,8 +542,9 @@ __device__ void conn_assemble(const DecodeArgs& a, const GroupLane& L, bool act,
     if (act) {
         flush_tris(a.idx, L.t_base, tr, tf, min(tcnt, n_tris), vloc, true);
         flush_walk(walk_out, wr, wf, min(wcnt, n_local), true);
-        // the triangle count does not depend on the FIFO: no suspect here
-        if (tcnt != n_tris) report(a.status, kErrCorrupt, L.m);
+        // the triangle count and the raw ids do not depend on the FIFO: no
+        // suspect here
+        if (tcnt != n_tris || ridmax > n_local) report(a.status, kErrCorrupt, L.m);
         a.descs[L.m].walk = kind0 | (min(wcnt, n_local) << 16);
     }
 }
