@@ -87,6 +87,35 @@ def test_sblb_blob_layout():
 
 
 @pytest.mark.parametrize("name", V5_CASES)
+def test_sblb_read_back_and_kernel_shared_memory(name):
+    """The SBLB file parsed back the way the reference harness reads it
+    (read_blob), and the shared memory the reference PLDT v5 kernel's
+    per-meshlet layout reaches, which the launcher grants when the header's
+    size (the CuPy decoder's formula) is smaller."""
+    from oracle import ref_gpu
+    data, pos, idx, meta = _load(name)
+    B = ref_gpu.parse_sblb(ref_gpu.sblb_blob(data))
+    h = B["hdr"]
+    t = oracle.tables_v5(data)
+    assert h["n_meshlets"] == meta["n_meshlets"] and h["n_boundary"] == meta["n_boundary"]
+    assert h["n_v_total"] == len(pos) and h["n_t_total"] == len(idx)
+    assert bytes(B["buf"]) == data
+    for k in ("n_bnd", "n_int", "n_tris", "n_strips"):
+        assert np.array_equal(B[k], t[k])
+    cb = 4 if h["code_width"] else 2
+    need = ref_gpu.v5_kernel_smem(B["n_bnd"], B["n_int"], B["n_tris"], cb)
+    n_local = B["n_bnd"].astype(np.int64) + B["n_int"]
+    # the kernel's layout: float4 rows and an l2g entry per local vertex,
+    # the 256-bit seen map, interior codes, four short emit arrays, triangles
+    want = int((n_local * 20 + 32 + B["n_int"].astype(np.int64) * (3 * cb + 8)
+                + B["n_tris"].astype(np.int64) * 3).max()) if len(n_local) else 0
+    assert need == want
+    formula = ((int(n_local.max()) * 16 + int(B["n_bnd"].max()) * 4 + 32 + int(B["n_int"].max()) * 3 * cb
+                + int(B["n_int"].max()) * 8 + int(B["n_tris"].max()) * 3 + 15) & ~15) if len(n_local) else 32
+    assert h["per_warp_bytes"] == formula
+
+
+@pytest.mark.parametrize("name", V5_CASES)
 def test_host_inspect_matches_oracle(name):
     """pldt5_inspect (the library's host parse, no GPU): header fields and
     output sizes as the oracle decodes them."""
