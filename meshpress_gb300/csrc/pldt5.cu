@@ -373,24 +373,47 @@ __global__ void __launch_bounds__(kP5Threads) p5_decode_kernel(P5Args a) {
         if (bad) p5_report(a.status, kErrCorrupt, m);
     }
     // 4. reconstruction in float64, in the reference's operation order, no
-    // contraction (:426-445)
+    // contraction (:426-445).  A strip-body vertex is predicted from the
+    // previous triangle, whose interior vertices were reconstructed a step
+    // or two before: the last four interior rows stay in registers, so those
+    // references do not wait for a store to come back from L2.
     const bool rec = act && !bad && n_int > 0u;
     double fb[3] = {0.0, 0.0, 0.0};
     if (rec && n_bnd > 0u) {
         for (int d = 0; d < 3; d++) {
-            double s = a.rows[3ull * row_of(0u) + d];
-            for (uint32_t i = 1; i < n_bnd; i++) s = __dadd_rn(s, a.rows[3ull * row_of(i) + d]);
+            double s = __ldcg(a.rows + 3ull * row_of(0u) + d);
+#pragma unroll 4
+            for (uint32_t i = 1; i < n_bnd; i++) s = __dadd_rn(s, __ldcg(a.rows + 3ull * row_of(i) + d));
             fb[d] = __ddiv_rn(s, static_cast<double>(n_bnd));
         }
     }
+    uint32_t cid[4] = {0xFFFFu, 0xFFFFu, 0xFFFFu, 0xFFFFu};  // local ids of the cached rows (newest first)
+    double cx[4][3];
+#pragma unroll
+    for (int j = 0; j < 4; j++) cx[j][0] = cx[j][1] = cx[j][2] = 0.0;
+    // coordinate d of local vertex l: a cached row or the rows array
+    auto coord = [&](uint32_t l, unsigned long long o, int d) -> double {
+        double r = 0.0;
+        bool hit = false;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            const bool h = cid[j] == l;
+            r = h ? cx[j][d] : r;
+            hit = hit || h;
+        }
+        return hit ? r : __ldcg(a.rows + o + d);
+    };
     const uint32_t ne = __reduce_max_sync(0xFFFFFFFFu, rec ? n_emit : 0u);
+    uint32_t e_next = (rec && n_emit > 0u) ? __ldcg(a.walk + row0) : 0u;
     for (uint32_t i = 0; i < ne; i++) {
         if (!rec || i >= n_emit) continue;
-        const uint32_t e = __ldcg(a.walk + row0 + i);
+        const uint32_t e = e_next;
+        if (i + 1u < n_emit) e_next = __ldcg(a.walk + row0 + i + 1u);  // the next entry, a step ahead
         const uint32_t v = e & 0xFFu, ra = (e >> 8) & 0xFFu, rbv = (e >> 16) & 0xFFu, rc = e >> 24;
         const bool para = ra != v;  // roots are stored as (v, v, v, v)
         const unsigned long long out = 3ull * row_of(v);
         const unsigned long long oa = 3ull * row_of(ra), ob = 3ull * row_of(rbv), oc = 3ull * row_of(rc);
+        double nr[3];
 #pragma unroll
         for (int d = 0; d < 3; d++) {
             long long code;
@@ -403,13 +426,25 @@ __global__ void __launch_bounds__(kP5Threads) p5_decode_kernel(P5Args a) {
             }
             double pred = fb[d];
             if (para) {
-                const double t0 = __dmul_rn(a.w0, __ldcg(a.rows + oa + d));
-                const double t1 = __dmul_rn(a.w1, __ldcg(a.rows + ob + d));
-                const double t2 = __dmul_rn(a.w2, __ldcg(a.rows + oc + d));
+                const double t0 = __dmul_rn(a.w0, coord(ra, oa, d));
+                const double t1 = __dmul_rn(a.w1, coord(rbv, ob, d));
+                const double t2 = __dmul_rn(a.w2, coord(rc, oc, d));
                 pred = __dadd_rn(__dadd_rn(t0, t1), t2);
             }
-            a.rows[out + d] = __dadd_rn(pred, __dmul_rn(static_cast<double>(code), a.delta));
+            nr[d] = __dadd_rn(pred, __dmul_rn(static_cast<double>(code), a.delta));
+            a.rows[out + d] = nr[d];
         }
+#pragma unroll
+        for (int j = 3; j > 0; j--) {
+            cid[j] = cid[j - 1];
+            cx[j][0] = cx[j - 1][0];
+            cx[j][1] = cx[j - 1][1];
+            cx[j][2] = cx[j - 1][2];
+        }
+        cid[0] = v;
+        cx[0][0] = nr[0];
+        cx[0][1] = nr[1];
+        cx[0][2] = nr[2];
     }
 }
 
