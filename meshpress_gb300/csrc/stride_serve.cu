@@ -244,8 +244,13 @@ bool pinned_get(stride_server* s, size_t bytes, Pinned* out) {
         s->pinned_pool.erase(s->pinned_pool.begin() + best);
         return true;
     }
+    // sizes in powers of two from 1 MiB: pinning host memory takes
+    // milliseconds per tens of MiB and stalls every queued request, so the
+    // pool settles on a few size classes after a handful of allocations
+    // instead of growing by one odd size per launch
     Pinned p;
-    p.bytes = std::max<size_t>(bytes, 1 << 20);
+    p.bytes = size_t(1) << 20;
+    while (p.bytes < bytes) p.bytes <<= 1;
     if (cudaHostAlloc(reinterpret_cast<void**>(&p.ptr), p.bytes, cudaHostAllocDefault) != cudaSuccess) {
         cudaGetLastError();
         return false;
