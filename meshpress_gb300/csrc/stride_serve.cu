@@ -9,9 +9,11 @@
 //
 // A scheduler thread forms a launch from the queued requests in arrival
 // order (up to max_batch of them, as many as the arena admits), uploads
-// their payloads through a pinned staging buffer, and runs the same scan /
-// connectivity / vertex kernels as a batch over their concatenated meshlet
-// queue on one of n_streams non-blocking streams.  Up to n_streams launches
+// their payloads -- each copied into pinned memory by the thread that
+// submitted it (up to a pinned budget; past it through a pinned staging
+// buffer) -- and runs the same scan / connectivity / vertex kernels as a
+// batch over their concatenated meshlet queue on one of n_streams
+// non-blocking streams.  Up to n_streams launches
 // are in flight, so requests that arrive while others decode are admitted as
 // soon as a stream and arena space are free, and their copies and kernels
 // overlap the running launch on the device.  A host function placed on the
@@ -47,6 +49,10 @@ using namespace stride;
 namespace {
 
 constexpr uint64_t kAlign = 256;
+// Pinned host bytes the engine keeps for payloads of queued and running
+// requests; past it a payload waits in pageable memory and goes through a
+// launch's staging buffer.
+constexpr size_t kPinnedPayloadBudget = size_t(4) << 30;
 
 uint64_t up(uint64_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 
@@ -140,23 +146,25 @@ uint64_t out_bytes(uint64_t n_v, uint64_t n_t) { return up(12ull * n_t) + up(12u
 
 struct Launch;
 
+// Pinned host buffer, recycled through the engine's pool.
+struct Pinned {
+    uint8_t* ptr = nullptr;
+    size_t bytes = 0;
+};
+
 struct Request {
     uint64_t id = 0;
-    std::vector<uint8_t> data;
+    std::vector<uint8_t> data;  // the payload, unless it is in `pay`
+    size_t len = 0;             // payload bytes
     MeshParams p{};
     enum State { kQueued, kRunning, kDone } state = kQueued;
     int status = STRIDE_OK;
     uint64_t blob_off = 0;  // arena, while running
     bool has_blob = false;
     std::shared_ptr<Launch> launch;  // owner of the result buffers once done
+    Pinned pay;                      // the payload and kBlobPad zero bytes, pinned (when ptr is set)
     uint64_t t_rel = 0, v_rel = 0;   // offsets inside the launch's outputs
     double t_submit = 0, t_admit = 0, t_done = 0;
-};
-
-// Pinned host buffer, recycled through the engine's pool.
-struct Pinned {
-    uint8_t* ptr = nullptr;
-    size_t bytes = 0;
 };
 
 struct Launch {
@@ -198,6 +206,7 @@ struct stride_server {
     std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
     std::vector<Slot> slots;
     std::vector<Pinned> pinned_pool;
+    size_t pinned_payload = 0;            // pinned bytes held by queued and running payloads
     uint64_t next_id = 1, launches = 0, completed = 0, seq = 0;
     std::atomic<bool> stop{false};
     bool hold = false;                    // queue without dispatching (stride_server_hold)
@@ -273,8 +282,12 @@ void finish_request(stride_server* s, Request* r, int status) {
     r->status = status;
     r->state = Request::kDone;
     if (r->has_blob) {
-        s->arena.release(r->blob_off, blob_alloc_bytes(r->data.size()));
+        s->arena.release(r->blob_off, blob_alloc_bytes(r->len));
         r->has_blob = false;
+    }
+    if (r->pay.ptr) {  // its upload, if any, has completed: the launch retired
+        s->pinned_payload -= r->pay.bytes;
+        pinned_put(s, r->pay);
     }
     s->completed++;
 }
@@ -322,7 +335,7 @@ void retire(stride_server* s, Launch* l) {
                 finish_request(s, r, code);
             } else {
                 if (r->has_blob) {
-                    s->arena.release(r->blob_off, blob_alloc_bytes(r->data.size()));
+                    s->arena.release(r->blob_off, blob_alloc_bytes(r->len));
                     r->has_blob = false;
                 }
                 r->state = Request::kQueued;
@@ -352,14 +365,14 @@ bool dispatch(stride_server* s, int slot_i) {
         if (take.size() >= max_batch) break;
         if (static_cast<uint64_t>(tm) + r->p.n_meshlets > 0xFFFFFFF0ull) break;
         uint64_t off = 0;
-        if (!s->arena.alloc(blob_alloc_bytes(r->data.size()), &off)) break;
+        if (!s->arena.alloc(blob_alloc_bytes(r->len), &off)) break;
         // outputs + scratch for the launch with this request in it
         const uint64_t need = out_bytes(tv + r->p.n_v, tt + r->p.n_t) +
                               plan_scratch(static_cast<uint32_t>(take.size() + 1), tm + r->p.n_meshlets,
                                            tv + r->p.n_v, tl + lut_entries(r->p)).total;
         uint64_t probe = 0;
         if (!s->arena.alloc(need, &probe)) {
-            s->arena.release(off, blob_alloc_bytes(r->data.size()));
+            s->arena.release(off, blob_alloc_bytes(r->len));
             break;
         }
         s->arena.release(probe, need);
@@ -383,7 +396,7 @@ bool dispatch(stride_server* s, int slot_i) {
         if (l->has_out) s->arena.release(l->out_off, l->out_size);
         l->has_out = false;
         for (Request* r : take) {
-            s->arena.release(r->blob_off, blob_alloc_bytes(r->data.size()));
+            s->arena.release(r->blob_off, blob_alloc_bytes(r->len));
             r->has_blob = false;
         }
         return false;
@@ -424,7 +437,7 @@ bool dispatch(stride_server* s, int slot_i) {
     // stage: mesh table | meshlet->mesh map | table mesh list | payloads
     const size_t list_off = up(sizeof(MeshParams) * take.size()) + up(4ull * std::max<uint32_t>(1u, tm));
     size_t stage_bytes = list_off + up(4ull * take.size());
-    for (Request* r : take) stage_bytes += up(r->data.size());
+    for (Request* r : take) stage_bytes += r->pay.ptr ? 0u : up(r->len);
     if (slot.stage.bytes < stage_bytes) {
         pinned_put(s, slot.stage);  // idle: the slot's previous launch has retired
         if (!pinned_get(s, stage_bytes, &slot.stage)) {
@@ -454,10 +467,14 @@ bool dispatch(stride_server* s, int slot_i) {
         e = cudaMemcpyAsync(sc + sp.lut_list, hs + list_off, 4ull * n_lut, cudaMemcpyHostToDevice, st);
     for (Request* r : take) {
         if (e != cudaSuccess) break;
-        std::memcpy(hp, r->data.data(), r->data.size());
-        e = cudaMemcpyAsync(base + r->blob_off, hp, r->data.size(), cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaMemsetAsync(base + r->blob_off + r->data.size(), 0, kBlobPad, st);
-        hp += up(r->data.size());
+        if (r->pay.ptr) {  // payload and padding already pinned: one copy
+            e = cudaMemcpyAsync(base + r->blob_off, r->pay.ptr, r->len + kBlobPad, cudaMemcpyHostToDevice, st);
+            continue;
+        }
+        std::memcpy(hp, r->data.data(), r->len);
+        e = cudaMemcpyAsync(base + r->blob_off, hp, r->len, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(base + r->blob_off + r->len, 0, kBlobPad, st);
+        hp += up(r->len);
     }
     int rc = e == cudaSuccess ? STRIDE_OK : STRIDE_ERR_CUDA;
     if (rc == STRIDE_OK) {
@@ -605,11 +622,28 @@ int stride_server_submit(stride_server* s, const uint8_t* data, size_t len, uint
         return fail(STRIDE_ERR_NOMEM, "request needs %llu arena bytes alone; the HBM budget is %llu",
                     static_cast<unsigned long long>(footprint(r->p, len)),
                     static_cast<unsigned long long>(s->arena.size()));
-    r->data.assign(data, data + len);
+    r->len = len;
+    {  // the payload into pinned memory, copied on this thread, within the pinned budget
+        std::lock_guard<std::mutex> g(s->mu);
+        if (s->pinned_payload + len + kBlobPad <= kPinnedPayloadBudget && pinned_get(s, len + kBlobPad, &r->pay))
+            s->pinned_payload += r->pay.bytes;
+    }
+    if (r->pay.ptr) {
+        std::memcpy(r->pay.ptr, data, len);
+        std::memset(r->pay.ptr + len, 0, kBlobPad);
+    } else {
+        r->data.assign(data, data + len);
+    }
     {
         std::lock_guard<std::mutex> g(s->mu);
-        if (s->stop.load()) return fail(STRIDE_ERR_ARG, "server is shutting down");
-        if (s->queue.size() >= s->opts.max_queue) return fail(STRIDE_ERR_BUSY, "request queue full");
+        if (s->stop.load() || s->queue.size() >= s->opts.max_queue) {
+            if (r->pay.ptr) {
+                s->pinned_payload -= r->pay.bytes;
+                pinned_put(s, r->pay);
+            }
+            if (s->stop.load()) return fail(STRIDE_ERR_ARG, "server is shutting down");
+            return fail(STRIDE_ERR_BUSY, "request queue full");
+        }
         r->id = s->next_id++;
         r->t_submit = now_us(s->t0);
         *req_id = r->id;
@@ -702,11 +736,16 @@ void stride_server_destroy(stride_server* s) {
         cudaFreeHost(sl.h_status);
         if (sl.stage.ptr) cudaFreeHost(sl.stage.ptr);
     }
-    for (auto& kv : s->reqs)
+    for (auto& kv : s->reqs) {
         if (kv.second->launch && kv.second->launch->host.ptr) {
             cudaFreeHost(kv.second->launch->host.ptr);
             kv.second->launch->host = Pinned{};
         }
+        if (kv.second->pay.ptr) {
+            cudaFreeHost(kv.second->pay.ptr);
+            kv.second->pay = Pinned{};
+        }
+    }
     for (Pinned& p : s->pinned_pool) cudaFreeHost(p.ptr);
     cudaFree(s->d_arena);
     delete s;
