@@ -289,6 +289,9 @@ typedef struct {
     uint32_t n_streams;          /* launches in flight (0 = 2)                */
     uint32_t max_queue;          /* queued requests before submit is refused  */
     uint32_t copy_to_host;       /* 1 = also copy results to host buffers     */
+    uint32_t pad0;
+    uint64_t pinned_budget_bytes; /* pinned host bytes for payloads copied at submit
+                                   * (0 = 4 GiB); past it payloads are staged per launch */
 } stride_server_opts;
 
 typedef struct {
@@ -303,7 +306,8 @@ typedef struct {
 } stride_result;
 
 int stride_server_create(const stride_server_opts* opts, stride_server** out);
-/* Copies `data`; returns a request id. */
+/* Copies `data` (into pinned memory within the pinned budget, on the
+ * calling thread); returns a request id. */
 int stride_server_submit(stride_server* s, const uint8_t* data, size_t len, uint64_t* req_id);
 /* Waits up to timeout_ms (<0 = forever) for the request to finish. */
 int stride_server_wait(stride_server* s, uint64_t req_id, int timeout_ms, stride_result* out);

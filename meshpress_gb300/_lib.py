@@ -62,7 +62,8 @@ class LaunchCfg(ctypes.Structure):
 class ServerOpts(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_batch", ctypes.c_uint32),
                 ("n_streams", ctypes.c_uint32), ("max_queue", ctypes.c_uint32),
-                ("copy_to_host", ctypes.c_uint32)]
+                ("copy_to_host", ctypes.c_uint32), ("pad0", ctypes.c_uint32),
+                ("pinned_budget_bytes", ctypes.c_uint64)]
 
 
 class ServerResult(ctypes.Structure):

@@ -50,9 +50,10 @@ namespace {
 
 constexpr uint64_t kAlign = 256;
 // Pinned host bytes the engine keeps for payloads of queued and running
-// requests; past it a payload waits in pageable memory and goes through a
-// launch's staging buffer.
-constexpr size_t kPinnedPayloadBudget = size_t(4) << 30;
+// requests (stride_server_opts::pinned_budget_bytes, 0: this); past it a
+// payload waits in pageable memory and goes through a launch's staging
+// buffer.
+constexpr uint64_t kPinnedPayloadBudget = uint64_t(4) << 30;
 
 uint64_t up(uint64_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 
@@ -625,7 +626,8 @@ int stride_server_submit(stride_server* s, const uint8_t* data, size_t len, uint
     r->len = len;
     {  // the payload into pinned memory, copied on this thread, within the pinned budget
         std::lock_guard<std::mutex> g(s->mu);
-        if (s->pinned_payload + len + kBlobPad <= kPinnedPayloadBudget && pinned_get(s, len + kBlobPad, &r->pay))
+        const uint64_t budget = s->opts.pinned_budget_bytes ? s->opts.pinned_budget_bytes : kPinnedPayloadBudget;
+        if (s->pinned_payload + len + kBlobPad <= budget && pinned_get(s, len + kBlobPad, &r->pay))
             s->pinned_payload += r->pay.bytes;
     }
     if (r->pay.ptr) {

@@ -53,7 +53,7 @@ class ServedResult:
 
 class DecodeServer:
     def __init__(self, hbm_budget_bytes: int, *, max_batch: int = 256, n_streams: int = 2, max_queue: int = 0,
-                 copy_to_host: bool = False):
+                 copy_to_host: bool = False, pinned_budget_bytes: int = 0):
         import torch
         if not torch.cuda.is_available():
             raise RuntimeError("CUDA device not available: the STRIDE decoder runs on the GPU only")
@@ -61,7 +61,7 @@ class DecodeServer:
         self._lib = _lib.load()
         self._device = torch.cuda.current_device()
         opts = _lib.ServerOpts(int(hbm_budget_bytes), int(max_batch), int(n_streams), int(max_queue),
-                               int(bool(copy_to_host)))
+                               int(bool(copy_to_host)), 0, int(pinned_budget_bytes))
         h = ctypes.c_void_p()
         _lib.check(self._lib.stride_server_create(ctypes.byref(opts), ctypes.byref(h)), "stride_server_create")
         self._h = h

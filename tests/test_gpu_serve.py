@@ -48,7 +48,11 @@ def _same(torch, res, t, v):
     assert torch.equal(res.verts.view(torch.int32), v.view(torch.int32))
 
 
-def test_alone_equals_mix(torch_cuda, pool):
+@pytest.mark.parametrize("pinned_budget", [0, 3 << 20], ids=["payloads_pinned", "pinned_and_staged"])
+def test_alone_equals_mix(torch_cuda, pool, pinned_budget):
+    """Every response equals the alone-decode, whether its payload was
+    pinned at submit or staged by the scheduler (a 3 MiB pinned budget holds
+    about three payloads at a time, so launches mix both kinds)."""
     torch = torch_cuda
     from meshpress_gb300.serve import DecodeServer
     # alone: one request in the server at a time
@@ -60,7 +64,7 @@ def test_alone_equals_mix(torch_cuda, pool):
             srv.release(rid)
     # mix: three threads submit the pool twice over, interleaved; the first
     # half is queued behind a hold so that launches certainly share requests
-    with DecodeServer(512 << 20, n_streams=3, max_batch=6) as srv:
+    with DecodeServer(512 << 20, n_streams=3, max_batch=6, pinned_budget_bytes=pinned_budget) as srv:
         srv.hold(True)
         ids = {}
         lock = threading.Lock()
