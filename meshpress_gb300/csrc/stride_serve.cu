@@ -103,7 +103,6 @@ class Arena {
         }
     }
     uint64_t size() const { return size_; }
-    uint64_t used() const { return used_; }
     uint64_t peak() const { return peak_; }
 
   private:
