@@ -195,11 +195,14 @@ int stride_cull_meshlets(const float* d_bounds, uint32_t n, const float* planes,
  * stride_decode, with CUDA events recorded on `stream` between its
  * kernels; waits and writes their durations in milliseconds to
  * kernel_ms[0] (meshlet scan), kernel_ms[1] (connectivity) and
- * kernel_ms[2] (vertices + output).  With the fused kernel (persistent 2,
- * the default) kernel_ms[1] is the fused kernel and kernel_ms[2] is 0. */
+ * kernel_ms[2] (vertices + output).  With the fused kernel (persistent 2)
+ * kernel_ms[1] is the fused kernel and kernel_ms[2] is 0. */
 int stride_decode_timed(stride_handle* h, void* stream, uint32_t* d_idx, float* d_pos, float* kernel_ms);
 
-/* Launch shape for this handle's decodes (defaults are used until set). */
+/* Launch shape for this handle's decodes.  Until it is set the shape
+ * follows the mesh's size: the two kernels (persistent 1) for 128 to 1,023
+ * groups of 32 meshlets, the fused kernel (persistent 2) otherwise; a
+ * reload keeps a shape that was set. */
 int stride_set_config(stride_handle* h, const stride_launch_cfg* cfg);
 
 /* No counterpart in the reference.  SM clocks each device wait of this

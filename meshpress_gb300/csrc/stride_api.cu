@@ -181,6 +181,7 @@ struct stride_handle {
     cudaEvent_t done = nullptr;
     bool launched = false;
     LaunchCfg cfg;
+    bool cfg_set = false;               // stride_set_config called: keep cfg across reloads
     long long wait_clocks = 1ll << 31;  // DecodeArgs::wait_clocks of this handle's decodes
     uint32_t launch_smem = 0, launch_grid = 0;  // the last decode's main kernel
     // stride_decode_host: copy streams and the events they wait on
@@ -338,7 +339,7 @@ int stride_inspect(const uint8_t* data, size_t len, stride_info_t* info) {
     char why[256] = {0};
     const int rc = parse_header(data, len, &p, why, sizeof(why));
     if (rc) return fail(rc, "%s", why);
-    fill_info(p, len, LaunchCfg().persistent, info);
+    fill_info(p, len, default_config(p.n_meshlets).persistent, info);
     return STRIDE_OK;
 }
 
@@ -355,6 +356,7 @@ int stride_open(const uint8_t* data, size_t len, stride_handle** out) {
     cudaError_t e;
     rc = ensure_capacity(h, len, p);
     h->params = p;
+    h->cfg = default_config(p.n_meshlets);
     if (rc != STRIDE_OK) {
         free_buffers(h);
         delete h;
@@ -384,6 +386,7 @@ int stride_reload(stride_handle* h, const uint8_t* data, size_t len, void* strea
     if ((rc = ensure_capacity(h, len, p)) != STRIDE_OK) return rc;
     h->params = p;
     h->len = len;
+    if (!h->cfg_set) h->cfg = default_config(p.n_meshlets);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaError_t e;
     if ((e = cudaMemcpyAsync(h->d_blob, data, len, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
@@ -605,6 +608,7 @@ int stride_set_config(stride_handle* h, const stride_launch_cfg* c) {
     const bool wide = h->params.g_bits[0] > 16 || h->params.g_bits[1] > 16 || h->params.g_bits[2] > 16;
     if (check_config(cfg, wide)) return fail(STRIDE_ERR_ARG, "launch configuration not launchable");
     h->cfg = cfg;
+    h->cfg_set = true;
     return STRIDE_OK;
 }
 

@@ -150,6 +150,7 @@ int stride_batch_create(const uint8_t* const* blobs, const size_t* lens, uint32_
         delete b;
         return rc;
     }
+    b->cfg = default_config(b->total_meshlets);
     if (b->wide) b->cfg.code_bytes = std::max<uint32_t>(b->cfg.code_bytes, kMaxLocal * 4u);
     b->arena_bytes = arena_bytes;
     b->walk_cap = walk_scratch_words(b->total_v, b->total_meshlets);

@@ -163,6 +163,8 @@ int parse_header(const uint8_t* data, size_t len, MeshParams* p, char* why, size
 // kernel, after it, after the connectivity (or fused) kernel and after the
 // vertex kernel (right after the fused one).
 int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void* const* ev = nullptr);
+// The launch shape a decode of this many meshlets takes unless one is set.
+LaunchCfg default_config(uint32_t total_meshlets);
 
 // Meshlet-native outputs of a finished decode: each meshlet's first vertex
 // and triangle row (n + 1 entries, the last the totals); the bounds (min

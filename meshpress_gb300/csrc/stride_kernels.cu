@@ -1239,6 +1239,25 @@ int check_config(const LaunchCfg& cfg, bool wide) {
     return STRIDE_OK;
 }
 
+// Groups from which the default launch shape is the two-kernel one, below
+// kFlowFiveGroups.  Measured on one GB300 (step, L2 flushed, every output
+// bit-identical), fused against two kernels: 513^2 heightfield (83 groups)
+// 0.111 / 0.115 ms, level-8 icosphere (210) 0.137 / 0.121, 1025^2 (331)
+// 0.147 / 0.125, 1449^2 (666) 0.177 / 0.173, 2049^2 (1,347) 0.222 / 0.278,
+// 2897^2 (2,700) 0.407 / 0.475.  Between these bounds the vertex kernel's
+// three-warp CTAs (no idle warp, two meshlets per L2 round trip in the
+// output pass) outrun the fused kernel's vertex phase; above them the
+// fused kernel's overlap of the two phases wins, below them its single
+// launch.
+constexpr uint32_t kTwoKernelGroups = 128u;
+
+LaunchCfg default_config(uint32_t total_meshlets) {
+    LaunchCfg cfg;
+    const uint32_t groups = (total_meshlets + 31u) / 32u;
+    cfg.persistent = (groups >= kTwoKernelGroups && groups < kFlowFiveGroups) ? 1 : 2;
+    return cfg;
+}
+
 int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void* const* ev) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (check_config(cfg, a.wide_codes)) return STRIDE_ERR_ARG;

@@ -198,7 +198,6 @@ struct stride_server {
     std::chrono::steady_clock::time_point t0;
     uint8_t* d_arena = nullptr;
     Arena arena;
-    LaunchCfg cfg;
 
     std::mutex mu;                        // engine state
     std::condition_variable done_cv;      // request finished (waiters)
@@ -500,7 +499,7 @@ bool dispatch(stride_server* s, int slot_i) {
         a.wide_codes = false;
         for (const MeshParams& p : params)
             a.wide_codes = a.wide_codes || p.g_bits[0] > 16 || p.g_bits[1] > 16 || p.g_bits[2] > 16;
-        LaunchCfg cfg = s->cfg;
+        LaunchCfg cfg = default_config(tm);  // the launch's shape by its size
         if (a.wide_codes) cfg.code_bytes = std::max<uint32_t>(cfg.code_bytes, kMaxLocal * 4u);
         rc = enqueue_decode(a, cfg, st);
         if (rc == STRIDE_OK &&

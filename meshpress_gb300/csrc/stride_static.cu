@@ -150,6 +150,8 @@ extern "C" int stride_decode_static(const uint8_t* data, size_t len, void* strea
     a.lut_meshes = reinterpret_cast<const uint32_t*>(base + L.lut_list);
     a.n_lut_meshes = n_lut;
     a.lut_max = lut_max;
+    // always the fused shape: one set of kernels, loaded by the first call
+    // (a shape used for the first time later would load its kernels then)
     LaunchCfg cfg;
     if (a.wide_codes) cfg.code_bytes = kMaxLocal * 4u > cfg.code_bytes ? kMaxLocal * 4u : cfg.code_bytes;
     rc = enqueue_decode(a, cfg, stream);

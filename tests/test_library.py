@@ -74,11 +74,18 @@ def test_decoder_fails_loudly_without_library(monkeypatch):
 
 
 def test_kernel_count(built_libs):
-    """With the default launch shape a decode is two kernel launches: scan
-    (which also fills any per-code dequantisation tables), then the fused
-    connectivity + vertex kernel."""
+    """The default launch shape follows the meshlet count: below 128 groups
+    of 32 meshlets and from 1,024 on, two kernel launches (scan, which also
+    fills any per-code dequantisation tables, then the fused connectivity +
+    vertex kernel); in between three (scan, connectivity, vertices)."""
     for name in ("grid129_b12", "grid9_b12", "grid17_canon_b16", "tri1_b12"):
         assert _lib.inspect(_golden.load(name)["data"]).kernels == 2
+    from meshpress_gb300 import encoder, synth
+    V, T = synth.noise_heightfield(1025, seed=3)  # 331 groups
+    data = encoder.encode(V, T, precision_error=synth.bbox_bits_error(12), precision_mode="bbox_frac").data
+    info = _lib.inspect(data)
+    assert 128 * 32 <= info.n_meshlets < 1024 * 32
+    assert info.kernels == 3
 
 
 def test_global_reads_through_l2_only():
