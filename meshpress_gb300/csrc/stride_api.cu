@@ -158,6 +158,13 @@ unsigned long long plan_luts(MeshParams* p, uint32_t n, uint32_t* meshes, uint32
 
 }  // namespace stride
 
+// stride_decode_host: the connectivity of a mesh of at least kHostPartTris
+// triangles runs as kHostParts launches, and each part's triangles go to
+// the host when it ends (the host link, about 190 GB/s each way, is the
+// bound; a part's connectivity takes less time than its triangles' copy)
+constexpr int kHostParts = 4;
+constexpr uint64_t kHostPartTris = 3ull << 20;
+
 struct stride_handle {
     int device = 0;
     size_t len = 0, cap_bytes = 0;
@@ -187,13 +194,25 @@ struct stride_handle {
     // stride_decode_host: copy streams and the events they wait on
     cudaStream_t copy[2] = {nullptr, nullptr};
     cudaEvent_t conn_done = nullptr, vert_done = nullptr, copied[2] = {nullptr, nullptr};
+    // ... and for a decode whose connectivity runs in parts
+    cudaEvent_t scan_done = nullptr, prefix_in = nullptr, part_done[kHostParts] = {};
+    BlockPrefix* h_prefix = nullptr;  // pinned: the scan's block prefixes
+    uint32_t prefix_cap = 0;
 };
+
+static void for_copy_events(stride_handle* h, void (*f)(cudaEvent_t*, cudaError_t*), cudaError_t* e) {
+    for (cudaEvent_t* ev : {&h->conn_done, &h->vert_done, &h->copied[0], &h->copied[1], &h->scan_done, &h->prefix_in})
+        f(ev, e);
+    for (cudaEvent_t& ev : h->part_done) f(&ev, e);
+}
 
 static void free_copy_streams(stride_handle* h) {
     for (auto& c : h->copy)
         if (c) cudaStreamDestroy(c), c = nullptr;
-    for (cudaEvent_t* e : {&h->conn_done, &h->vert_done, &h->copied[0], &h->copied[1]})
-        if (*e) cudaEventDestroy(*e), *e = nullptr;
+    for_copy_events(h, [](cudaEvent_t* ev, cudaError_t*) { if (*ev) cudaEventDestroy(*ev), *ev = nullptr; }, nullptr);
+    cudaFreeHost(h->h_prefix);
+    h->h_prefix = nullptr;
+    h->prefix_cap = 0;
 }
 
 static cudaError_t make_copy_streams(stride_handle* h) {
@@ -201,8 +220,9 @@ static cudaError_t make_copy_streams(stride_handle* h) {
     cudaError_t e = cudaSuccess;
     for (auto& c : h->copy)
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking);
-    for (cudaEvent_t* ev : {&h->conn_done, &h->vert_done, &h->copied[0], &h->copied[1]})
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    for_copy_events(h, [](cudaEvent_t* ev, cudaError_t* err) {
+        if (*err == cudaSuccess) *err = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+    }, &e);
     if (e != cudaSuccess) free_copy_streams(h);
     return e;
 }
@@ -564,19 +584,69 @@ int stride_decode_host(stride_handle* h, void* stream, uint32_t* h_idx, float* h
     // The link is the bound here, so the decode takes the two-kernel shape,
     // whose connectivity ends first (the fused kernel's ends with it).
     cudaStream_t s = static_cast<cudaStream_t>(stream);
-    void* ev[4] = {nullptr, nullptr, h->conn_done, h->vert_done};
     LaunchCfg cfg = h->cfg;
     if (cfg.persistent == 2) cfg.persistent = 1;
-    int rc = enqueue_decode(handle_args(h, h->d_idx, h->d_pos, nullptr), cfg, stream, ev);
-    if (rc) return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
-    h->launched = true;
     const size_t ib = 12 * h->params.n_t, pb = 12 * h->params.n_v;
+    // Large meshes: the connectivity kernel runs in parts of whole windows
+    // and each part's triangles go to the host as soon as it ends, so the
+    // link starts after a quarter of the connectivity instead of all of it.
+    // The parts' first triangle rows come from the scan's block prefixes,
+    // read back while the first part runs.
+    const uint32_t n_groups = (h->params.n_meshlets + 31u) / 32u;
+    const uint32_t n_win = (n_groups + 7u) / 8u;
+    const bool parts = cfg.persistent < 2 && h->params.n_t >= kHostPartTris && n_win >= kHostParts;
+    size_t tri_at[kHostParts + 1] = {0};  // byte offsets of the parts' triangles
+    int n_parts = 1;
+    if (parts) {
+        uint32_t part_g[kHostParts + 1];
+        void* cd[kHostParts];
+        for (int p = 0; p < kHostParts; p++) {
+            part_g[p] = 8u * static_cast<uint32_t>(static_cast<uint64_t>(n_win) * p / kHostParts);
+            cd[p] = h->part_done[p];
+        }
+        part_g[kHostParts] = n_groups;
+        if (h->prefix_cap < n_win) {
+            cudaFreeHost(h->h_prefix);
+            h->h_prefix = nullptr;
+            h->prefix_cap = 0;
+            if ((e = cudaHostAlloc(&h->h_prefix, n_win * sizeof(BlockPrefix), cudaHostAllocDefault)) != cudaSuccess)
+                return cuda_fail(e, "cudaHostAlloc(prefix)");
+            h->prefix_cap = n_win;
+        }
+        int rc = enqueue_decode_parts(handle_args(h, h->d_idx, h->d_pos, nullptr), cfg, stream, part_g, kHostParts,
+                                      h->scan_done, cd, h->vert_done);
+        if (rc) return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+        h->launched = true;
+        if ((e = cudaStreamWaitEvent(h->copy[1], h->scan_done, 0)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(h->h_prefix, h->d_blk_prefix, n_win * sizeof(BlockPrefix), cudaMemcpyDeviceToHost,
+                                 h->copy[1])) != cudaSuccess ||
+            (e = cudaEventRecord(h->prefix_in, h->copy[1])) != cudaSuccess ||
+            (e = cudaEventSynchronize(h->prefix_in)) != cudaSuccess)
+            return cuda_fail(e, "stride_decode_host prefix");
+        // a corrupt stream's prefixes are clamped (its status reports it)
+        for (int p = 1; p < kHostParts; p++)
+            tri_at[p] = std::max(tri_at[p - 1], 12 * std::min<size_t>(h->h_prefix[part_g[p] / 8u].t, h->params.n_t));
+        tri_at[kHostParts] = ib;
+        n_parts = kHostParts;
+    } else {
+        void* ev[4] = {nullptr, nullptr, h->conn_done, h->vert_done};
+        int rc = enqueue_decode(handle_args(h, h->d_idx, h->d_pos, nullptr), cfg, stream, ev);
+        if (rc) return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+        h->launched = true;
+    }
     const size_t ih = (ib / 2) & ~size_t(15), ph = (pb / 2) & ~size_t(15);
     const size_t ioff[2] = {0, ih}, ilen[2] = {ih, ib - ih};
     const size_t poff[2] = {0, ph}, plen[2] = {ph, pb - ph};
+    // parts: every part's triangles in order on the first copy stream
+    for (int p = 0; parts && p < n_parts && e == cudaSuccess; p++) {
+        if ((e = cudaStreamWaitEvent(h->copy[0], h->part_done[p], 0)) == cudaSuccess && tri_at[p + 1] > tri_at[p])
+            e = cudaMemcpyAsync(reinterpret_cast<uint8_t*>(h_idx) + tri_at[p],
+                                reinterpret_cast<const uint8_t*>(h->d_idx) + tri_at[p], tri_at[p + 1] - tri_at[p],
+                                cudaMemcpyDeviceToHost, h->copy[0]);
+    }
     for (int k = 0; k < 2 && e == cudaSuccess; k++) {
         cudaStream_t c = h->copy[k];
-        if ((e = cudaStreamWaitEvent(c, h->conn_done, 0)) == cudaSuccess && ilen[k])
+        if (!parts && (e = cudaStreamWaitEvent(c, h->conn_done, 0)) == cudaSuccess && ilen[k])
             e = cudaMemcpyAsync(reinterpret_cast<uint8_t*>(h_idx) + ioff[k],
                                 reinterpret_cast<const uint8_t*>(h->d_idx) + ioff[k], ilen[k], cudaMemcpyDeviceToHost, c);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(c, h->vert_done, 0);

@@ -137,6 +137,10 @@ struct DecodeArgs {
     // completion list) spins before it gives up with STRIDE_ERR_TIMEOUT
     // (about a second by default; 0 gives up at the first unsuccessful check)
     long long wait_clocks = 1ll << 31;
+    // groups [conn_g0, conn_g1) of the connectivity kernel (two-kernel
+    // shape): whole 256-meshlet windows, i.e. multiples of eight; the
+    // defaults take every group
+    uint32_t conn_g0 = 0u, conn_g1 = 0xFFFFFFFFu;
 };
 
 // Host: assigns table offsets (has_lut, lut_off) to the meshes that get
@@ -163,6 +167,12 @@ int parse_header(const uint8_t* data, size_t len, MeshParams* p, char* why, size
 // kernel, after it, after the connectivity (or fused) kernel and after the
 // vertex kernel (right after the fused one).
 int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void* const* ev = nullptr);
+// The two-kernel decode with its connectivity in parts: the scan (then
+// `scan_done`), one connectivity launch per part of whole windows, part p
+// over groups [part_g[p], part_g[p + 1]) and followed by `conn_done[p]`,
+// then the vertex kernel over every group (then `vert_done`).
+int enqueue_decode_parts(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, const uint32_t* part_g,
+                         int n_parts, void* scan_done, void* const* conn_done, void* vert_done);
 // The launch shape a decode of this many meshlets takes unless one is set.
 LaunchCfg default_config(uint32_t total_meshlets);
 

@@ -604,10 +604,12 @@ __global__ void __launch_bounds__(G * 64) conn_kernel(DecodeArgs a) {
     const int lane = threadIdx.x & 31;
     const bool failed = *reinterpret_cast<volatile unsigned long long*>(&a.status->err) != 0ull;
     if (__syncthreads_or(failed)) return;
-    const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
+    // groups [g0, g1): whole windows, so the order below is a bijection of them
+    const uint32_t g1 = min(a.conn_g1, (a.total_meshlets + 31u) / 32u);
+    const uint32_t g0 = min(a.conn_g0, g1);
     const uint32_t f = blockIdx.x * G + pair;
-    if (f >= n_groups) return;  // both warps of the pair
-    conn_group<G>(a, group_at(f, n_groups), pair, parser, lane, smem + pair * conn_pair_bytes(), mtf_masks,
+    if (f >= g1 - g0) return;  // both warps of the pair
+    conn_group<G>(a, g0 + group_at(f, g1 - g0), pair, parser, lane, smem + pair * conn_pair_bytes(), mtf_masks,
                   s_redo + pair);
 }
 
@@ -1094,7 +1096,8 @@ cudaError_t launch_conn(const DecodeArgs& a, const LaunchCfg& cfg, cudaStream_t 
     const size_t smem = static_cast<size_t>(G) * conn_pair_bytes();
     cudaError_t e = opt_in_smem(conn_kernel<G>, smem, configured);
     if (e != cudaSuccess) return e;
-    const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
+    const uint32_t g1 = std::min(a.conn_g1, (a.total_meshlets + 31u) / 32u);
+    const uint32_t n_groups = g1 - std::min(a.conn_g0, g1);
     const uint32_t grid = (n_groups + G - 1) / G;
     if (grid == 0) return cudaSuccess;
     conn_kernel<G><<<grid, G * 64, smem, s>>>(a);
@@ -1258,21 +1261,28 @@ LaunchCfg default_config(uint32_t total_meshlets) {
     return cfg;
 }
 
+namespace {
+// The scan kernel, with the blocks that fill the dequantisation tables.
+int launch_scan(const DecodeArgs& a, cudaStream_t s) {
+    const uint32_t nb = scan_blocks(a.total_meshlets);
+    const uint32_t lut_bx = (a.lut_max + 255u) / 256u;
+    const unsigned long long grid = nb + static_cast<unsigned long long>(a.n_lut_meshes) * lut_bx;
+    if (grid > 0x7FFFFFFFull) return STRIDE_ERR_UNSUPPORTED;
+    if (grid) {
+        scan_kernel<<<static_cast<uint32_t>(grid), kScanThreads, 0, s>>>(a, nb, lut_bx);
+        if (cudaGetLastError() != cudaSuccess) return STRIDE_ERR_CUDA;
+    }
+    return STRIDE_OK;
+}
+}  // namespace
+
 int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void* const* ev) {
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (check_config(cfg, a.wide_codes)) return STRIDE_ERR_ARG;
     if (cudaMemsetAsync(a.status, 0, sizeof(Status), s) != cudaSuccess) return STRIDE_ERR_CUDA;
     record(ev, 0, s);
-    {
-        const uint32_t nb = scan_blocks(a.total_meshlets);
-        const uint32_t lut_bx = (a.lut_max + 255u) / 256u;
-        const unsigned long long grid = nb + static_cast<unsigned long long>(a.n_lut_meshes) * lut_bx;
-        if (grid > 0x7FFFFFFFull) return STRIDE_ERR_UNSUPPORTED;
-        if (grid) {
-            scan_kernel<<<static_cast<uint32_t>(grid), kScanThreads, 0, s>>>(a, nb, lut_bx);
-            if (cudaGetLastError() != cudaSuccess) return STRIDE_ERR_CUDA;
-        }
-    }
+    const int rc = launch_scan(a, s);
+    if (rc) return rc;
     record(ev, 1, s);
     if (a.total_meshlets != 0) {
         cudaError_t e;
@@ -1296,6 +1306,36 @@ int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void
         record(ev, 2, s);
     }
     record(ev, 3, s);
+    return STRIDE_OK;
+}
+
+int enqueue_decode_parts(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, const uint32_t* part_g,
+                         int n_parts, void* scan_done, void* const* conn_done, void* vert_done) {
+    if (cfg.persistent >= 2 || n_parts < 1) return STRIDE_ERR_ARG;
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (check_config(cfg, a.wide_codes)) return STRIDE_ERR_ARG;
+    if (cudaMemsetAsync(a.status, 0, sizeof(Status), s) != cudaSuccess) return STRIDE_ERR_CUDA;
+    const int rc = launch_scan(a, s);
+    if (rc) return rc;
+    if (scan_done) cudaEventRecord(static_cast<cudaEvent_t>(scan_done), s);
+    for (int p = 0; p < n_parts; p++) {
+        DecodeArgs ap = a;
+        ap.conn_g0 = part_g[p];
+        ap.conn_g1 = part_g[p + 1];
+        cudaError_t e;
+        switch (cfg.warps_per_cta) {
+            case 1: e = launch_conn<conn_pairs(1)>(ap, cfg, s); break;
+            case 2: e = launch_conn<conn_pairs(2)>(ap, cfg, s); break;
+            default: e = launch_conn<conn_pairs(4)>(ap, cfg, s); break;
+        }
+        if (e != cudaSuccess) return STRIDE_ERR_CUDA;
+        if (conn_done && conn_done[p]) cudaEventRecord(static_cast<cudaEvent_t>(conn_done[p]), s);
+    }
+    if (a.total_meshlets != 0) {
+        const cudaError_t e = a.wide_codes ? launch_vert<true>(a, cfg, s) : launch_vert<false>(a, cfg, s);
+        if (e != cudaSuccess) return STRIDE_ERR_CUDA;
+    }
+    if (vert_done) cudaEventRecord(static_cast<cudaEvent_t>(vert_done), s);
     return STRIDE_OK;
 }
 

@@ -76,12 +76,15 @@ def test_decode_to_host_and_device_agree(torch_cuda):
         assert np.array_equal(p2.view(np.uint32), pos.view(np.uint32)) and np.array_equal(i2, idx)
 
 
-def test_decode_to_host_pinned_overlap(torch_cuda):
+@pytest.mark.parametrize("grid", [513, 1449])
+def test_decode_to_host_pinned_overlap(torch_cuda, grid):
     """Pinned host outputs: the index copy runs beside the vertex kernel on
-    the handle's copy streams; results equal the device decode bit for bit."""
+    the handle's copy streams (from about 3 M triangles, 1449^2 here, part by
+    part of the connectivity kernel); results equal the device decode bit
+    for bit."""
     torch = torch_cuda
     from meshpress_gb300 import ParaDeltaV5GpuDecoder
-    V, T = synth.noise_heightfield(513, seed=4)
+    V, T = synth.noise_heightfield(grid, seed=4)
     data = encoder.encode(V, T, precision_error=B12, precision_mode="bbox_frac").data
     dec = ParaDeltaV5GpuDecoder(data)
     tris, verts = dec.decode_to_device()
