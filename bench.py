@@ -220,6 +220,33 @@ def measured_peak():
     return 6800.0, "fallback 6.8 TB/s"
 
 
+def link_floor(h_in, h_idx, h_pos, d_idx, d_pos, stream, reps: int = 5) -> dict:
+    """The host link alone: the step's upload (the stream, pinned) and its
+    download (indices and positions into pinned memory) as plain copies,
+    timed with CUDA events; their sum is the floor of an end-to-end step
+    that waits for its inputs before decoding."""
+    import torch
+    d_in = torch.empty(h_in.numel(), dtype=torch.uint8, device=d_idx.device)
+
+    def best(fn):
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return min(ts)
+
+    up = best(lambda: d_in.copy_(h_in, non_blocking=True))
+    down = best(lambda: (h_idx.copy_(d_idx, non_blocking=True), h_pos.copy_(d_pos, non_blocking=True)))
+    nb_up, nb_down = h_in.numel(), 4 * (h_idx.numel() + h_pos.numel())
+    return {"h2d_ms": round(up, 4), "d2h_ms": round(down, 4), "h2d_gbs": round(nb_up / up / 1e6, 1),
+            "d2h_gbs": round(nb_down / down / 1e6, 1), "floor_ms": round(up + down, 4),
+            "what": "plain pinned copies of the step's bytes, CUDA events, best of %d" % reps}
+
+
 def kernel_split(kern, fused: bool, stream_bytes: int, n_v: int, n_t: int, persistent: int = 2):
     """Names of the decode's kernels, the dominant one and its algorithmic
     bytes, from the per-kernel times (scan, connectivity, vertex; a one-kernel
@@ -521,7 +548,8 @@ def run_single(args):
         e2e = {"value": round(replica_value(n_t, world, e2e_s) / 1e6, 3), "unit": "M tris/s",
                "h2d_bytes_per_step": len(data), "d2h_bytes_per_step": 12 * (n_v + n_t),
                "ms_per_step": round(e2e_s * 1e3, 4), "path": "ParaDeltaV5GpuDecoder C ABI: stride_reload + "
-                                                              "stride_decode_host, pinned host buffers"}
+                                                              "stride_decode_host, pinned host buffers",
+               "link": link_floor(h_blob, h_idx, h_pos, idx, pos, stream)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

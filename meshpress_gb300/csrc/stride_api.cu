@@ -198,6 +198,7 @@ struct stride_handle {
     cudaEvent_t scan_done = nullptr, prefix_in = nullptr, part_done[kHostParts] = {};
     BlockPrefix* h_prefix = nullptr;  // pinned: the scan's block prefixes
     uint32_t prefix_cap = 0;
+    Status* h_status = nullptr;       // pinned: the status, copied out with the outputs
 };
 
 static void for_copy_events(stride_handle* h, void (*f)(cudaEvent_t*, cudaError_t*), cudaError_t* e) {
@@ -213,6 +214,8 @@ static void free_copy_streams(stride_handle* h) {
     cudaFreeHost(h->h_prefix);
     h->h_prefix = nullptr;
     h->prefix_cap = 0;
+    cudaFreeHost(h->h_status);
+    h->h_status = nullptr;
 }
 
 static cudaError_t make_copy_streams(stride_handle* h) {
@@ -223,6 +226,7 @@ static cudaError_t make_copy_streams(stride_handle* h) {
     for_copy_events(h, [](cudaEvent_t* ev, cudaError_t* err) {
         if (*err == cudaSuccess) *err = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     }, &e);
+    if (e == cudaSuccess) e = cudaHostAlloc(&h->h_status, sizeof(Status), cudaHostAllocDefault);
     if (e != cudaSuccess) free_copy_streams(h);
     return e;
 }
@@ -653,12 +657,19 @@ int stride_decode_host(stride_handle* h, void* stream, uint32_t* h_idx, float* h
         if (e == cudaSuccess && plen[k])
             e = cudaMemcpyAsync(reinterpret_cast<uint8_t*>(h_pos) + poff[k],
                                 reinterpret_cast<const uint8_t*>(h->d_pos) + poff[k], plen[k], cudaMemcpyDeviceToHost, c);
+        // the status is final with the vertex kernel: it comes back with the
+        // positions, and no synchronous read follows the decode
+        if (e == cudaSuccess && k == 1)
+            e = cudaMemcpyAsync(h->h_status, h->d_status, sizeof(Status), cudaMemcpyDeviceToHost, c);
         if (e == cudaSuccess) e = cudaEventRecord(h->copied[k], c);
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s, h->copied[k], 0);
     }
     if (e == cudaSuccess) e = cudaEventRecord(h->done, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(h->done);
     if (e != cudaSuccess) return cuda_fail(e, "stride_decode_host copy");
-    return stride_status(h, 1, nullptr);
+    uint32_t bad = 0;
+    const int rc = status_to_code(*h->h_status, &bad);
+    return rc ? fail(rc, "%s (meshlet %u)", status_message(rc), bad) : STRIDE_OK;
 }
 
 int stride_set_wait_limit(stride_handle* h, uint64_t clocks) {

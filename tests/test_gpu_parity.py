@@ -247,6 +247,35 @@ def test_truncated_and_offset_corruption(torch_cuda):
     assert r is None and e.code == _lib.STRIDE_ERR_OFFSET
 
 
+@pytest.mark.parametrize("grid", [129, 1449])
+def test_decode_to_host_reports_corruption(torch_cuda, grid):
+    """A shifted offset-table entry in the last quarter of the meshlets (the
+    last connectivity part of a large host decode): decode_to_host fails
+    with the code the device decode reports, and the handle decodes the
+    good stream afterwards."""
+    from meshpress_gb300 import ParaDeltaV5GpuDecoder
+    V, T = synth.noise_heightfield(grid, seed=4)
+    data = encoder.encode(V, T, precision_error=B12, precision_mode="bbox_frac").data
+    dec = ParaDeltaV5GpuDecoder(data)
+    m = (3 * dec.n_meshlets) // 4 + 1
+    bad = bytearray(data)
+    off = 86 + 4 * m
+    bad[off:off + 4] = (int.from_bytes(bad[off:off + 4], "big") + 3).to_bytes(4, "big")
+    dec.reload(bytes(bad))
+    with pytest.raises(_lib.StrideFormatError) as on_host:
+        dec.decode_to_host()
+    with pytest.raises(_lib.StrideFormatError) as on_device:
+        dec.decode_to_device()
+    assert on_host.value.code == on_device.value.code
+    assert on_host.value.code in (_lib.STRIDE_ERR_OFFSET, _lib.STRIDE_ERR_CORRUPT, _lib.STRIDE_ERR_UNSUPPORTED)
+    dec.reload(data)
+    pos, idx = dec.decode_to_host()
+    opos, oidx = oracle.decode_mt(data, 0)
+    assert np.array_equal(pos.view(np.uint32), opos.view(np.uint32))
+    assert np.array_equal(idx.astype(np.int64), oidx)
+    dec.close()
+
+
 def test_bit_flip_fuzz(torch_cuda):
     """Random single-bit corruptions: the GPU either rejects the stream or
     returns exactly what the reference semantics (oracle) return; whenever
