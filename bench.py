@@ -232,9 +232,10 @@ def link_floor(h_in, h_idx, h_pos, d_idx, d_pos, stream, reps: int = 5) -> dict:
         ts = []
         for _ in range(reps):
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            fn()
-            e1.record(stream)
+            with torch.cuda.stream(stream):  # the copies go to the timed stream
+                e0.record(stream)
+                fn()
+                e1.record(stream)
             e1.synchronize()
             ts.append(e0.elapsed_time(e1))
         return min(ts)
@@ -678,7 +679,7 @@ def run_batch(args):
         d.close()
     del outs, decs
 
-    # end to end: pinned host image -> device, graph, outputs -> pinned host
+    # end to end: pinned host image -> device, decode with the outputs copied to pinned host memory
     e2e = None
     if not args.no_e2e:
         img = b.make_image()
@@ -686,15 +687,13 @@ def run_batch(args):
         h_img.numpy()[:] = img
         h_t = torch.empty(b.d_tris.shape, dtype=torch.int32, pin_memory=True)
         h_v = torch.empty(b.d_verts.shape, dtype=torch.float32, pin_memory=True)
+        out = (h_v.numpy(), h_t.numpy().view(np.uint32))
         ts = []
         with torch.cuda.stream(stream):
             for k in range(args.steps + 2):
                 t0 = time.perf_counter()
                 b.upload(h_img.data_ptr(), img.size, stream=stream)
-                b.launch_graph(stream)
-                h_t.copy_(b.d_tris.view(torch.int32), non_blocking=True)
-                h_v.copy_(b.d_verts, non_blocking=True)
-                stream.synchronize()
+                b.decode_to_host(out=out, stream=stream)
                 if k >= 2:
                     ts.append(time.perf_counter() - t0)
         b.check()
@@ -702,7 +701,9 @@ def run_batch(args):
         e2e = {"value": round(sharded_value(n_t_all, e2e_s) / 1e6, 3), "unit": "M tris/s",
                "h2d_bytes_per_step": int(img.size), "d2h_bytes_per_step": 12 * (b.n_t_total + b.n_v_total),
                "ms_per_step": round(e2e_s * 1e3, 4),
-               "path": "BatchDecoder: stride_batch_upload (pinned arena image) + graph launch + pinned copies out"}
+               "path": "BatchDecoder: stride_batch_upload (pinned arena image) + stride_batch_decode_to_host "
+                       "(pinned outputs, copies beside the decode)",
+               "link": link_floor(h_img, h_t, h_v, b.d_tris.view(torch.int32), b.d_verts, stream)}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -147,7 +147,10 @@ int stride_decode(stride_handle* h, void* stream, uint32_t* d_idx, float* d_pos,
  * copy them to h_idx / h_pos (host, n_t*3 uint32 and n_v*3 float32) and
  * synchronise.  Returns the decode status.  The triangle copy starts when
  * the connectivity kernel ends, beside the vertex kernel (a fused launch
- * shape is replaced by the persistent two-kernel one for this call).
+ * shape is replaced by the persistent two-kernel one for this call); from
+ * about 3 million triangles the connectivity runs in four parts and each
+ * part's triangles are copied as soon as it ends.  Pinned host buffers
+ * make the copies asynchronous to the host.
  * Replaces decode_to_host (utils/paradelta_v5_cuda.py:714-718). */
 int stride_decode_host(stride_handle* h, void* stream, uint32_t* h_idx, float* h_pos);
 
@@ -259,6 +262,12 @@ int stride_batch_decode(stride_batch* b, void* stream, uint32_t* d_idx, float* d
  * and vertex kernels (CUDA events) in kernel_ms[0..2] (fused kernel: in
  * kernel_ms[1], kernel_ms[2] = 0, as for stride_decode_timed). */
 int stride_batch_decode_timed(stride_batch* b, void* stream, uint32_t* d_idx, float* d_pos, float* kernel_ms);
+/* Decode into d_idx / d_pos and copy both to h_idx / h_pos (host, the same
+ * sizes; pinned for asynchronous copies), synchronously, overlapping the
+ * copies with the decode as stride_decode_host does.  Returns the decode
+ * status. */
+int stride_batch_decode_to_host(stride_batch* b, void* stream, uint32_t* d_idx, float* d_pos, uint32_t* h_idx,
+                                float* h_pos);
 /* The arena image: stream i sits at blob_offsets[i] of an image_bytes-long
  * buffer (zero bytes elsewhere).  A caller that keeps such an image in
  * (pinned) host memory replaces every stream of the batch with one

@@ -119,6 +119,7 @@ SIGNATURES = [
     ("stride_batch_decode_timed", _I, [_P, _P, _P, _P, _P]),
     ("stride_batch_image", _I, [_P, _P, ctypes.POINTER(_U64)]),
     ("stride_batch_upload", _I, [_P, _P, _P, _SZ]),
+    ("stride_batch_decode_to_host", _I, [_P, _P, _P, _P, _P, _P]),
     ("stride_batch_capture_graph", _I, [_P, _P, _P, _P]),
     ("stride_batch_launch_graph", _I, [_P, _P]),
     ("stride_batch_autotune", _I, [_P, _P, _P, _P, _I, ctypes.POINTER(LaunchCfg),

@@ -81,6 +81,27 @@ class BatchDecoder:
         self.check()
         return tuple(float(x) for x in ms)
 
+    def decode_to_host(self, out=None, *, stream=None):
+        """Decode and copy the outputs to host memory, the copies overlapping
+        the decode; -> (positions float32 (n_v, 3), triangles uint32 (n_t,
+        3)), numpy.  ``out`` = (positions, triangles) host arrays of those
+        shapes (pinned memory makes the copies asynchronous); by default
+        new arrays."""
+        if out is None:
+            pos = np.empty((self.n_v_total, 3), np.float32)
+            idx = np.empty((self.n_t_total, 3), np.uint32)
+        else:
+            pos, idx = out
+            if pos.shape != (self.n_v_total, 3) or pos.dtype != np.float32 or not pos.flags.c_contiguous:
+                raise ValueError("positions: a C-contiguous float32 array of shape (n_v, 3)")
+            if idx.shape != (self.n_t_total, 3) or idx.dtype != np.uint32 or not idx.flags.c_contiguous:
+                raise ValueError("triangles: a C-contiguous uint32 array of shape (n_t, 3)")
+        i, p = self._ptrs()
+        _lib.check(self._lib.stride_batch_decode_to_host(self._h, self._stream(stream), i, p,
+                                                         ctypes.c_void_p(idx.ctypes.data),
+                                                         ctypes.c_void_p(pos.ctypes.data)), "batch decode to host")
+        return pos, idx
+
     def image(self):
         """-> (blob offsets (n_meshes,), image bytes): layout of the arena
         image that ``upload`` takes."""

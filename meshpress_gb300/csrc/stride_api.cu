@@ -158,13 +158,6 @@ unsigned long long plan_luts(MeshParams* p, uint32_t n, uint32_t* meshes, uint32
 
 }  // namespace stride
 
-// stride_decode_host: the connectivity of a mesh of at least kHostPartTris
-// triangles runs as kHostParts launches, and each part's triangles go to
-// the host when it ends (the host link, about 190 GB/s each way, is the
-// bound; a part's connectivity takes less time than its triangles' copy)
-constexpr int kHostParts = 4;
-constexpr uint64_t kHostPartTris = 3ull << 20;
-
 struct stride_handle {
     int device = 0;
     size_t len = 0, cap_bytes = 0;
@@ -191,45 +184,132 @@ struct stride_handle {
     bool cfg_set = false;               // stride_set_config called: keep cfg across reloads
     long long wait_clocks = 1ll << 31;  // DecodeArgs::wait_clocks of this handle's decodes
     uint32_t launch_smem = 0, launch_grid = 0;  // the last decode's main kernel
-    // stride_decode_host: copy streams and the events they wait on
-    cudaStream_t copy[2] = {nullptr, nullptr};
-    cudaEvent_t conn_done = nullptr, vert_done = nullptr, copied[2] = {nullptr, nullptr};
-    // ... and for a decode whose connectivity runs in parts
-    cudaEvent_t scan_done = nullptr, prefix_in = nullptr, part_done[kHostParts] = {};
-    BlockPrefix* h_prefix = nullptr;  // pinned: the scan's block prefixes
-    uint32_t prefix_cap = 0;
-    Status* h_status = nullptr;       // pinned: the status, copied out with the outputs
+    HostLink link;  // stride_decode_host
 };
 
-static void for_copy_events(stride_handle* h, void (*f)(cudaEvent_t*, cudaError_t*), cudaError_t* e) {
-    for (cudaEvent_t* ev : {&h->conn_done, &h->vert_done, &h->copied[0], &h->copied[1], &h->scan_done, &h->prefix_in})
+namespace stride {
+
+static void for_link_events(HostLink& L, void (*f)(cudaEvent_t*, cudaError_t*), cudaError_t* e) {
+    for (cudaEvent_t* ev : {&L.conn_done, &L.vert_done, &L.scan_done, &L.prefix_in, &L.done, &L.copied[0], &L.copied[1]})
         f(ev, e);
-    for (cudaEvent_t& ev : h->part_done) f(&ev, e);
+    for (cudaEvent_t& ev : L.part_done) f(&ev, e);
 }
 
-static void free_copy_streams(stride_handle* h) {
-    for (auto& c : h->copy)
+void host_link_free(HostLink& L) {
+    for (auto& c : L.copy)
         if (c) cudaStreamDestroy(c), c = nullptr;
-    for_copy_events(h, [](cudaEvent_t* ev, cudaError_t*) { if (*ev) cudaEventDestroy(*ev), *ev = nullptr; }, nullptr);
-    cudaFreeHost(h->h_prefix);
-    h->h_prefix = nullptr;
-    h->prefix_cap = 0;
-    cudaFreeHost(h->h_status);
-    h->h_status = nullptr;
+    for_link_events(L, [](cudaEvent_t* ev, cudaError_t*) { if (*ev) cudaEventDestroy(*ev), *ev = nullptr; }, nullptr);
+    cudaFreeHost(L.h_prefix);
+    L.h_prefix = nullptr;
+    L.prefix_cap = 0;
+    cudaFreeHost(L.h_status);
+    L.h_status = nullptr;
 }
 
-static cudaError_t make_copy_streams(stride_handle* h) {
-    if (h->copy[0]) return cudaSuccess;
+static cudaError_t host_link_init(HostLink& L) {
+    if (L.copy[0]) return cudaSuccess;
     cudaError_t e = cudaSuccess;
-    for (auto& c : h->copy)
+    for (auto& c : L.copy)
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking);
-    for_copy_events(h, [](cudaEvent_t* ev, cudaError_t* err) {
+    for_link_events(L, [](cudaEvent_t* ev, cudaError_t* err) {
         if (*err == cudaSuccess) *err = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     }, &e);
-    if (e == cudaSuccess) e = cudaHostAlloc(&h->h_status, sizeof(Status), cudaHostAllocDefault);
-    if (e != cudaSuccess) free_copy_streams(h);
+    if (e == cudaSuccess) e = cudaHostAlloc(&L.h_status, sizeof(Status), cudaHostAllocDefault);
+    if (e != cudaSuccess) host_link_free(L);
     return e;
 }
+
+int decode_to_host(HostLink& L, const DecodeArgs& a, LaunchCfg cfg, void* stream, uint64_t n_t, uint64_t n_v,
+                   uint32_t* h_idx, float* h_pos, uint32_t* bad, bool* ran) {
+    *ran = false;
+    cudaError_t e = host_link_init(L);
+    if (e != cudaSuccess) return cuda_fail(e, "copy streams");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    // a failure once work is queued: nothing may still run on the buffers
+    // or write the host outputs when this returns
+    auto bail = [&](cudaError_t err, const char* what) {
+        cudaStreamSynchronize(s);
+        cudaStreamSynchronize(L.copy[0]);
+        cudaStreamSynchronize(L.copy[1]);
+        return cuda_fail(err, what);
+    };
+    if (cfg.persistent == 2) cfg.persistent = 1;
+    const size_t ib = 12 * n_t, pb = 12 * n_v;
+    const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
+    const uint32_t n_win = (n_groups + 7u) / 8u;
+    const bool parts = cfg.persistent < 2 && n_t >= kHostPartTris && n_win >= kHostParts;
+    size_t tri_at[kHostParts + 1] = {0};  // byte offsets of the parts' triangles
+    if (parts) {
+        uint32_t part_g[kHostParts + 1];
+        void* cd[kHostParts];
+        for (int p = 0; p < kHostParts; p++) {
+            part_g[p] = 8u * static_cast<uint32_t>(static_cast<uint64_t>(n_win) * p / kHostParts);
+            cd[p] = L.part_done[p];
+        }
+        part_g[kHostParts] = n_groups;
+        if (L.prefix_cap < n_win) {
+            cudaFreeHost(L.h_prefix);
+            L.h_prefix = nullptr;
+            L.prefix_cap = 0;
+            if ((e = cudaHostAlloc(&L.h_prefix, n_win * sizeof(BlockPrefix), cudaHostAllocDefault)) != cudaSuccess)
+                return cuda_fail(e, "cudaHostAlloc(prefix)");
+            L.prefix_cap = n_win;
+        }
+        const int rc = enqueue_decode_parts(a, cfg, stream, part_g, kHostParts, L.scan_done, cd, L.vert_done);
+        if (rc) return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+        // the parts' first triangle rows: the scan's block prefixes, read
+        // back while the first part runs
+        if ((e = cudaStreamWaitEvent(L.copy[1], L.scan_done, 0)) != cudaSuccess ||
+            (e = cudaMemcpyAsync(L.h_prefix, a.blk_prefix, n_win * sizeof(BlockPrefix), cudaMemcpyDeviceToHost,
+                                 L.copy[1])) != cudaSuccess ||
+            (e = cudaEventRecord(L.prefix_in, L.copy[1])) != cudaSuccess ||
+            (e = cudaEventSynchronize(L.prefix_in)) != cudaSuccess)
+            return bail(e, "decode to host: block prefixes");
+        // a corrupt stream's prefixes are clamped (its status reports it)
+        for (int p = 1; p < kHostParts; p++)
+            tri_at[p] = std::max(tri_at[p - 1], 12 * std::min<size_t>(L.h_prefix[part_g[p] / 8u].t, n_t));
+        tri_at[kHostParts] = ib;
+        // every part's triangles in order on the first copy stream
+        for (int p = 0; p < kHostParts && e == cudaSuccess; p++) {
+            if ((e = cudaStreamWaitEvent(L.copy[0], L.part_done[p], 0)) == cudaSuccess && tri_at[p + 1] > tri_at[p])
+                e = cudaMemcpyAsync(reinterpret_cast<uint8_t*>(h_idx) + tri_at[p],
+                                    reinterpret_cast<const uint8_t*>(a.idx) + tri_at[p], tri_at[p + 1] - tri_at[p],
+                                    cudaMemcpyDeviceToHost, L.copy[0]);
+        }
+    } else {
+        void* ev[4] = {nullptr, nullptr, L.conn_done, L.vert_done};
+        const int rc = enqueue_decode(a, cfg, stream, ev);
+        if (rc) return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
+    }
+    // each output (the triangles unless they went by parts) in two halves,
+    // one per copy stream
+    const size_t ih = (ib / 2) & ~size_t(15), ph = (pb / 2) & ~size_t(15);
+    const size_t ioff[2] = {0, ih}, ilen[2] = {ih, ib - ih};
+    const size_t poff[2] = {0, ph}, plen[2] = {ph, pb - ph};
+    for (int k = 0; k < 2 && e == cudaSuccess; k++) {
+        cudaStream_t c = L.copy[k];
+        if (!parts && (e = cudaStreamWaitEvent(c, L.conn_done, 0)) == cudaSuccess && ilen[k])
+            e = cudaMemcpyAsync(reinterpret_cast<uint8_t*>(h_idx) + ioff[k],
+                                reinterpret_cast<const uint8_t*>(a.idx) + ioff[k], ilen[k], cudaMemcpyDeviceToHost, c);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(c, L.vert_done, 0);
+        if (e == cudaSuccess && plen[k])
+            e = cudaMemcpyAsync(reinterpret_cast<uint8_t*>(h_pos) + poff[k],
+                                reinterpret_cast<const uint8_t*>(a.pos) + poff[k], plen[k], cudaMemcpyDeviceToHost, c);
+        // the status is final with the vertex kernel: it comes back with the
+        // positions, and no synchronous read follows the decode
+        if (e == cudaSuccess && k == 1)
+            e = cudaMemcpyAsync(L.h_status, a.status, sizeof(Status), cudaMemcpyDeviceToHost, c);
+        if (e == cudaSuccess) e = cudaEventRecord(L.copied[k], c);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, L.copied[k], 0);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(L.done, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(L.done);
+    if (e != cudaSuccess) return bail(e, "decode to host: copies");
+    *ran = true;
+    return status_to_code(*L.h_status, bad);
+}
+
+}  // namespace stride
 
 static void free_buffers(stride_handle* h) {
     cudaFree(h->d_blob);
@@ -581,94 +661,13 @@ int stride_decode_host(stride_handle* h, void* stream, uint32_t* h_idx, float* h
         if ((e = cudaMalloc(&h->d_idx, 12 * h->params.n_t)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(idx)");
         h->cap_t = h->params.n_t;
     }
-    if ((e = make_copy_streams(h)) != cudaSuccess) return cuda_fail(e, "copy streams");
-    // The triangle indices are final when the connectivity kernel ends, so
-    // their copy to the host runs beside the vertex kernel; each output goes
-    // out in two halves on the handle's two copy streams (two copy engines).
-    // The link is the bound here, so the decode takes the two-kernel shape,
-    // whose connectivity ends first (the fused kernel's ends with it).
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
-    LaunchCfg cfg = h->cfg;
-    if (cfg.persistent == 2) cfg.persistent = 1;
-    const size_t ib = 12 * h->params.n_t, pb = 12 * h->params.n_v;
-    // Large meshes: the connectivity kernel runs in parts of whole windows
-    // and each part's triangles go to the host as soon as it ends, so the
-    // link starts after a quarter of the connectivity instead of all of it.
-    // The parts' first triangle rows come from the scan's block prefixes,
-    // read back while the first part runs.
-    const uint32_t n_groups = (h->params.n_meshlets + 31u) / 32u;
-    const uint32_t n_win = (n_groups + 7u) / 8u;
-    const bool parts = cfg.persistent < 2 && h->params.n_t >= kHostPartTris && n_win >= kHostParts;
-    size_t tri_at[kHostParts + 1] = {0};  // byte offsets of the parts' triangles
-    int n_parts = 1;
-    if (parts) {
-        uint32_t part_g[kHostParts + 1];
-        void* cd[kHostParts];
-        for (int p = 0; p < kHostParts; p++) {
-            part_g[p] = 8u * static_cast<uint32_t>(static_cast<uint64_t>(n_win) * p / kHostParts);
-            cd[p] = h->part_done[p];
-        }
-        part_g[kHostParts] = n_groups;
-        if (h->prefix_cap < n_win) {
-            cudaFreeHost(h->h_prefix);
-            h->h_prefix = nullptr;
-            h->prefix_cap = 0;
-            if ((e = cudaHostAlloc(&h->h_prefix, n_win * sizeof(BlockPrefix), cudaHostAllocDefault)) != cudaSuccess)
-                return cuda_fail(e, "cudaHostAlloc(prefix)");
-            h->prefix_cap = n_win;
-        }
-        int rc = enqueue_decode_parts(handle_args(h, h->d_idx, h->d_pos, nullptr), cfg, stream, part_g, kHostParts,
-                                      h->scan_done, cd, h->vert_done);
-        if (rc) return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
-        h->launched = true;
-        if ((e = cudaStreamWaitEvent(h->copy[1], h->scan_done, 0)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(h->h_prefix, h->d_blk_prefix, n_win * sizeof(BlockPrefix), cudaMemcpyDeviceToHost,
-                                 h->copy[1])) != cudaSuccess ||
-            (e = cudaEventRecord(h->prefix_in, h->copy[1])) != cudaSuccess ||
-            (e = cudaEventSynchronize(h->prefix_in)) != cudaSuccess)
-            return cuda_fail(e, "stride_decode_host prefix");
-        // a corrupt stream's prefixes are clamped (its status reports it)
-        for (int p = 1; p < kHostParts; p++)
-            tri_at[p] = std::max(tri_at[p - 1], 12 * std::min<size_t>(h->h_prefix[part_g[p] / 8u].t, h->params.n_t));
-        tri_at[kHostParts] = ib;
-        n_parts = kHostParts;
-    } else {
-        void* ev[4] = {nullptr, nullptr, h->conn_done, h->vert_done};
-        int rc = enqueue_decode(handle_args(h, h->d_idx, h->d_pos, nullptr), cfg, stream, ev);
-        if (rc) return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
-        h->launched = true;
-    }
-    const size_t ih = (ib / 2) & ~size_t(15), ph = (pb / 2) & ~size_t(15);
-    const size_t ioff[2] = {0, ih}, ilen[2] = {ih, ib - ih};
-    const size_t poff[2] = {0, ph}, plen[2] = {ph, pb - ph};
-    // parts: every part's triangles in order on the first copy stream
-    for (int p = 0; parts && p < n_parts && e == cudaSuccess; p++) {
-        if ((e = cudaStreamWaitEvent(h->copy[0], h->part_done[p], 0)) == cudaSuccess && tri_at[p + 1] > tri_at[p])
-            e = cudaMemcpyAsync(reinterpret_cast<uint8_t*>(h_idx) + tri_at[p],
-                                reinterpret_cast<const uint8_t*>(h->d_idx) + tri_at[p], tri_at[p + 1] - tri_at[p],
-                                cudaMemcpyDeviceToHost, h->copy[0]);
-    }
-    for (int k = 0; k < 2 && e == cudaSuccess; k++) {
-        cudaStream_t c = h->copy[k];
-        if (!parts && (e = cudaStreamWaitEvent(c, h->conn_done, 0)) == cudaSuccess && ilen[k])
-            e = cudaMemcpyAsync(reinterpret_cast<uint8_t*>(h_idx) + ioff[k],
-                                reinterpret_cast<const uint8_t*>(h->d_idx) + ioff[k], ilen[k], cudaMemcpyDeviceToHost, c);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(c, h->vert_done, 0);
-        if (e == cudaSuccess && plen[k])
-            e = cudaMemcpyAsync(reinterpret_cast<uint8_t*>(h_pos) + poff[k],
-                                reinterpret_cast<const uint8_t*>(h->d_pos) + poff[k], plen[k], cudaMemcpyDeviceToHost, c);
-        // the status is final with the vertex kernel: it comes back with the
-        // positions, and no synchronous read follows the decode
-        if (e == cudaSuccess && k == 1)
-            e = cudaMemcpyAsync(h->h_status, h->d_status, sizeof(Status), cudaMemcpyDeviceToHost, c);
-        if (e == cudaSuccess) e = cudaEventRecord(h->copied[k], c);
-        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, h->copied[k], 0);
-    }
-    if (e == cudaSuccess) e = cudaEventRecord(h->done, s);
-    if (e == cudaSuccess) e = cudaEventSynchronize(h->done);
-    if (e != cudaSuccess) return cuda_fail(e, "stride_decode_host copy");
     uint32_t bad = 0;
-    const int rc = status_to_code(*h->h_status, &bad);
+    bool ran = false;
+    const int rc = decode_to_host(h->link, handle_args(h, h->d_idx, h->d_pos, nullptr), h->cfg, stream,
+                                  h->params.n_t, h->params.n_v, h_idx, h_pos, &bad, &ran);
+    if (!ran) return rc;
+    h->launched = true;  // later status queries see this decode
+    cudaEventRecord(h->done, static_cast<cudaStream_t>(stream));
     return rc ? fail(rc, "%s (meshlet %u)", status_message(rc), bad) : STRIDE_OK;
 }
 
@@ -697,7 +696,7 @@ void stride_close(stride_handle* h) {
     if (!h) return;
     if (h->launched) cudaEventSynchronize(h->done);
     if (h->done) cudaEventDestroy(h->done);
-    free_copy_streams(h);
+    host_link_free(h->link);
     free_buffers(h);
     delete h;
 }

@@ -39,6 +39,7 @@ struct stride_batch {
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t done = nullptr;
     bool launched = false;
+    HostLink link;  // stride_batch_decode_to_host
 };
 
 namespace stride {
@@ -78,6 +79,7 @@ int build_mesh_table(const uint8_t* const* blobs, const size_t* lens, uint32_t n
 }  // namespace stride
 
 static void batch_free(stride_batch* b) {
+    host_link_free(b->link);
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
     if (b->done) cudaEventDestroy(b->done);
@@ -236,6 +238,34 @@ int stride_batch_decode(stride_batch* b, void* stream, uint32_t* d_idx, float* d
     if (e != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
     b->launched = true;
     return STRIDE_OK;
+}
+
+// A decode error's message, with the batch meshlet turned into mesh and
+// meshlet.
+static int batch_error(const stride_batch* b, int rc, uint32_t bad, uint32_t* bad_mesh, uint32_t* bad_meshlet) {
+    uint32_t mesh = 0;
+    for (uint32_t i = 0; i < b->n_meshes; i++)
+        if (b->params[i].meshlet_begin <= bad) mesh = i;
+    if (bad_mesh) *bad_mesh = mesh;
+    if (bad_meshlet) *bad_meshlet = bad - b->params[mesh].meshlet_begin;
+    return fail(rc, "%s (mesh %u, meshlet %u)", status_message(rc), mesh, bad - b->params[mesh].meshlet_begin);
+}
+
+int stride_batch_decode_to_host(stride_batch* b, void* stream, uint32_t* d_idx, float* d_pos, uint32_t* h_idx,
+                                float* h_pos) {
+    if (!b) return fail(STRIDE_ERR_ARG, "null batch");
+    if ((!d_idx || !h_idx) && b->total_t) return fail(STRIDE_ERR_ARG, "null index output");
+    if ((!d_pos || !h_pos) && b->total_v) return fail(STRIDE_ERR_ARG, "null position output");
+    if ((reinterpret_cast<uintptr_t>(d_idx) & 15u) || (reinterpret_cast<uintptr_t>(d_pos) & 3u))
+        return fail(STRIDE_ERR_ARG, "index output must be 16-byte aligned, positions 4-byte aligned");
+    uint32_t bad = 0;
+    bool ran = false;
+    const int rc = decode_to_host(b->link, batch_args(b, d_idx, d_pos), b->cfg, stream, b->total_t, b->total_v,
+                                  h_idx, h_pos, &bad, &ran);
+    if (!ran) return rc;
+    b->launched = true;  // later status queries see this decode
+    cudaEventRecord(b->done, static_cast<cudaStream_t>(stream));
+    return rc ? batch_error(b, rc, bad, nullptr, nullptr) : STRIDE_OK;
 }
 
 int stride_batch_image(const stride_batch* b, uint64_t* blob_offsets, uint64_t* image_bytes) {
@@ -405,15 +435,7 @@ int stride_batch_status(stride_batch* b, int wait, uint32_t* bad_mesh, uint32_t*
         return cuda_fail(e, "cudaMemcpy(status)");
     uint32_t bad = 0;
     const int rc = status_to_code(st, &bad);
-    if (rc) {
-        uint32_t mesh = 0;
-        for (uint32_t i = 0; i < b->n_meshes; i++)
-            if (b->params[i].meshlet_begin <= bad) mesh = i;
-        if (bad_mesh) *bad_mesh = mesh;
-        if (bad_meshlet) *bad_meshlet = bad - b->params[mesh].meshlet_begin;
-        return fail(rc, "%s (mesh %u, meshlet %u)", status_message(rc), mesh, bad - b->params[mesh].meshlet_begin);
-    }
-    return STRIDE_OK;
+    return rc ? batch_error(b, rc, bad, bad_mesh, bad_meshlet) : STRIDE_OK;
 }
 
 void stride_batch_destroy(stride_batch* b) {

@@ -121,3 +121,56 @@ def test_batch_of_one_equals_single_decoder(torch_cuda):
     assert torch_cuda.equal(bt.view(torch_cuda.int32), dt.view(torch_cuda.int32))
     assert torch_cuda.equal(bv.view(torch_cuda.int32), dv.view(torch_cuda.int32))
     b.close()
+
+
+@pytest.fixture(scope="module")
+def large_streams(mixed_streams):
+    """Two 1025^2 heightfields around the mixed meshes: about 4.6 M
+    triangles, so a host decode runs its connectivity in parts whose
+    boundaries fall inside meshes."""
+    out = []
+    for seed in (1, 2):
+        V, T = synth.noise_heightfield(1025, seed=seed)
+        out.append(encoder.encode(V, T, precision_error=B12, precision_mode="bbox_frac").data)
+    return [out[0]] + list(mixed_streams) + [out[1]]
+
+
+@pytest.mark.parametrize("which", ["mixed", "large"])
+def test_batch_decode_to_host(torch_cuda, mixed_streams, large_streams, which):
+    """Host outputs (pinned, copied while the decode runs) equal the device
+    decode bit for bit, for the mixed batch and for one large enough for the
+    connectivity to run in parts."""
+    torch = torch_cuda
+    from meshpress_gb300.batch import BatchDecoder
+    streams = mixed_streams if which == "mixed" else large_streams
+    b = BatchDecoder(streams)
+    ref_t, ref_v = (x.cpu().numpy() for x in b.decode())
+    h_pos = torch.empty((b.n_v_total, 3), dtype=torch.float32, pin_memory=True)
+    h_idx = torch.empty((b.n_t_total, 3), dtype=torch.int32, pin_memory=True)
+    for _ in range(2):
+        h_pos.fill_(float("nan"))
+        h_idx.fill_(-1)
+        pos, idx = b.decode_to_host(out=(h_pos.numpy(), h_idx.numpy().view(np.uint32)))
+        assert np.array_equal(idx, ref_t.view(np.uint32))
+        assert np.array_equal(pos.view(np.uint32), ref_v.view(np.uint32))
+    # pageable outputs: the same bytes
+    pos, idx = b.decode_to_host()
+    assert np.array_equal(idx, ref_t.view(np.uint32)) and np.array_equal(pos.view(np.uint32), ref_v.view(np.uint32))
+    if which == "large":
+        _check_meshes(b, streams, torch.from_numpy(idx.view(np.int32)), torch.from_numpy(pos))
+    b.close()
+
+
+def test_batch_decode_to_host_reports_the_corrupt_mesh(torch_cuda, large_streams):
+    from meshpress_gb300.batch import BatchDecoder
+    streams = list(large_streams)
+    streams[-2] = streams[-2][: len(streams[-2]) - 64]
+    b = BatchDecoder(streams)
+    with pytest.raises(_lib.StrideFormatError) as e:
+        b.decode_to_host()
+    assert e.value.code in (_lib.STRIDE_ERR_OFFSET, _lib.STRIDE_ERR_CORRUPT, _lib.STRIDE_ERR_UNSUPPORTED)
+    assert f"mesh {len(streams) - 2}," in str(e.value)
+    bm, bl = ctypes.c_uint32(), ctypes.c_uint32()
+    assert b._lib.stride_batch_status(b._h, 1, ctypes.byref(bm), ctypes.byref(bl)) == e.value.code
+    assert bm.value == len(streams) - 2
+    b.close()
