@@ -302,8 +302,9 @@ typedef struct {
     uint32_t max_queue;          /* queued requests before submit is refused  */
     uint32_t copy_to_host;       /* 1 = also copy results to host buffers     */
     uint32_t pad0;
-    uint64_t pinned_budget_bytes; /* pinned host bytes for payloads copied at submit
-                                   * (0 = 4 GiB); past it payloads are staged per launch */
+    uint64_t pinned_budget_bytes; /* pinned slab for payloads copied at submit, pinned
+                                   * once at create (0 = 1 GiB); a payload that finds
+                                   * no room in it is staged per launch             */
 } stride_server_opts;
 
 typedef struct {

@@ -49,11 +49,12 @@ using namespace stride;
 namespace {
 
 constexpr uint64_t kAlign = 256;
-// Pinned host bytes the engine keeps for payloads of queued and running
-// requests (stride_server_opts::pinned_budget_bytes, 0: this); past it a
-// payload waits in pageable memory and goes through a launch's staging
-// buffer.
-constexpr uint64_t kPinnedPayloadBudget = uint64_t(4) << 30;
+// Pinned host slab for the payloads of queued and running requests
+// (stride_server_opts::pinned_budget_bytes, 0: this), pinned once when the
+// server is created: pinning on the submit path took milliseconds per new
+// buffer and held the engine lock meanwhile.  A payload that finds no room
+// waits in pageable memory and goes through a launch's staging buffer.
+constexpr uint64_t kPayloadSlab = uint64_t(1) << 30;
 
 uint64_t up(uint64_t x) { return (x + kAlign - 1) & ~(kAlign - 1); }
 
@@ -162,7 +163,8 @@ struct Request {
     uint64_t blob_off = 0;  // arena, while running
     bool has_blob = false;
     std::shared_ptr<Launch> launch;  // owner of the result buffers once done
-    Pinned pay;                      // the payload and kBlobPad zero bytes, pinned (when ptr is set)
+    uint8_t* pay = nullptr;          // the payload and kBlobPad zero bytes in the pinned slab (when set)
+    uint64_t pay_off = 0;            // its offset in the slab
     uint64_t t_rel = 0, v_rel = 0;   // offsets inside the launch's outputs
     double t_submit = 0, t_admit = 0, t_done = 0;
 };
@@ -204,8 +206,9 @@ struct stride_server {
     std::deque<Request*> queue;
     std::unordered_map<uint64_t, std::unique_ptr<Request>> reqs;
     std::vector<Slot> slots;
-    std::vector<Pinned> pinned_pool;
-    size_t pinned_payload = 0;            // pinned bytes held by queued and running payloads
+    std::vector<Pinned> pinned_pool;      // staging and host-output buffers
+    uint8_t* h_pay = nullptr;             // pinned payload slab
+    Arena pay_arena;                      // its free space
     uint64_t next_id = 1, launches = 0, completed = 0, seq = 0;
     std::atomic<bool> stop{false};
     bool hold = false;                    // queue without dispatching (stride_server_hold)
@@ -284,9 +287,9 @@ void finish_request(stride_server* s, Request* r, int status) {
         s->arena.release(r->blob_off, blob_alloc_bytes(r->len));
         r->has_blob = false;
     }
-    if (r->pay.ptr) {  // its upload, if any, has completed: the launch retired
-        s->pinned_payload -= r->pay.bytes;
-        pinned_put(s, r->pay);
+    if (r->pay) {  // its upload, if any, has completed: the launch retired
+        s->pay_arena.release(r->pay_off, r->len + kBlobPad);
+        r->pay = nullptr;
     }
     s->completed++;
 }
@@ -436,7 +439,7 @@ bool dispatch(stride_server* s, int slot_i) {
     // stage: mesh table | meshlet->mesh map | table mesh list | payloads
     const size_t list_off = up(sizeof(MeshParams) * take.size()) + up(4ull * std::max<uint32_t>(1u, tm));
     size_t stage_bytes = list_off + up(4ull * take.size());
-    for (Request* r : take) stage_bytes += r->pay.ptr ? 0u : up(r->len);
+    for (Request* r : take) stage_bytes += r->pay ? 0u : up(r->len);
     if (slot.stage.bytes < stage_bytes) {
         pinned_put(s, slot.stage);  // idle: the slot's previous launch has retired
         if (!pinned_get(s, stage_bytes, &slot.stage)) {
@@ -466,8 +469,8 @@ bool dispatch(stride_server* s, int slot_i) {
         e = cudaMemcpyAsync(sc + sp.lut_list, hs + list_off, 4ull * n_lut, cudaMemcpyHostToDevice, st);
     for (Request* r : take) {
         if (e != cudaSuccess) break;
-        if (r->pay.ptr) {  // payload and padding already pinned: one copy
-            e = cudaMemcpyAsync(base + r->blob_off, r->pay.ptr, r->len + kBlobPad, cudaMemcpyHostToDevice, st);
+        if (r->pay) {  // payload and padding already pinned: one copy
+            e = cudaMemcpyAsync(base + r->blob_off, r->pay, r->len + kBlobPad, cudaMemcpyHostToDevice, st);
             continue;
         }
         std::memcpy(hp, r->data.data(), r->len);
@@ -592,6 +595,12 @@ int stride_server_create(const stride_server_opts* opts, stride_server** out) {
     const uint64_t budget = s->opts.hbm_budget_bytes & ~(kAlign - 1);
     if ((e = cudaMalloc(&s->d_arena, budget)) != cudaSuccess) return cuda_fail(e, "cudaMalloc(arena)");
     s->arena.reset(budget);
+    const uint64_t slab = up(s->opts.pinned_budget_bytes ? s->opts.pinned_budget_bytes : kPayloadSlab);
+    if ((e = cudaHostAlloc(reinterpret_cast<void**>(&s->h_pay), slab, cudaHostAllocDefault)) != cudaSuccess) {
+        cudaFree(s->d_arena);
+        return cuda_fail(e, "cudaHostAlloc(payload slab)");
+    }
+    s->pay_arena.reset(slab);
     s->slots.resize(s->opts.n_streams);
     for (Slot& sl : s->slots) {
         if ((e = cudaStreamCreateWithFlags(&sl.stream, cudaStreamNonBlocking)) != cudaSuccess ||
@@ -601,6 +610,7 @@ int stride_server_create(const stride_server_opts* opts, stride_server** out) {
                 if (x.stream) cudaStreamDestroy(x.stream);
                 if (x.h_status) cudaFreeHost(x.h_status);
             }
+            cudaFreeHost(s->h_pay);
             cudaFree(s->d_arena);
             return cuda_fail(e, "stride_server_create");
         }
@@ -622,25 +632,24 @@ int stride_server_submit(stride_server* s, const uint8_t* data, size_t len, uint
                     static_cast<unsigned long long>(footprint(r->p, len)),
                     static_cast<unsigned long long>(s->arena.size()));
     r->len = len;
-    {  // the payload into pinned memory, copied on this thread, within the pinned budget
+    {  // room in the pinned slab, if any; the copy runs on this thread, unlocked
         std::lock_guard<std::mutex> g(s->mu);
-        const uint64_t budget = s->opts.pinned_budget_bytes ? s->opts.pinned_budget_bytes : kPinnedPayloadBudget;
-        if (s->pinned_payload + len + kBlobPad <= budget && pinned_get(s, len + kBlobPad, &r->pay))
-            s->pinned_payload += r->pay.bytes;
+        uint64_t off = 0;
+        if (s->h_pay && s->pay_arena.alloc(len + kBlobPad, &off)) {
+            r->pay = s->h_pay + off;
+            r->pay_off = off;
+        }
     }
-    if (r->pay.ptr) {
-        std::memcpy(r->pay.ptr, data, len);
-        std::memset(r->pay.ptr + len, 0, kBlobPad);
+    if (r->pay) {
+        std::memcpy(r->pay, data, len);
+        std::memset(r->pay + len, 0, kBlobPad);
     } else {
         r->data.assign(data, data + len);
     }
     {
         std::lock_guard<std::mutex> g(s->mu);
         if (s->stop.load() || s->queue.size() >= s->opts.max_queue) {
-            if (r->pay.ptr) {
-                s->pinned_payload -= r->pay.bytes;
-                pinned_put(s, r->pay);
-            }
+            if (r->pay) s->pay_arena.release(r->pay_off, len + kBlobPad);
             if (s->stop.load()) return fail(STRIDE_ERR_ARG, "server is shutting down");
             return fail(STRIDE_ERR_BUSY, "request queue full");
         }
@@ -741,12 +750,9 @@ void stride_server_destroy(stride_server* s) {
             cudaFreeHost(kv.second->launch->host.ptr);
             kv.second->launch->host = Pinned{};
         }
-        if (kv.second->pay.ptr) {
-            cudaFreeHost(kv.second->pay.ptr);
-            kv.second->pay = Pinned{};
-        }
     }
     for (Pinned& p : s->pinned_pool) cudaFreeHost(p.ptr);
+    cudaFreeHost(s->h_pay);
     cudaFree(s->d_arena);
     delete s;
 }
