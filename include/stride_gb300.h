@@ -125,9 +125,13 @@ int stride_inspect(const uint8_t* data, size_t len, stride_info_t* info);
 int stride_open(const uint8_t* data, size_t len, stride_handle** out);
 
 /* Replace the handle's stream with new bytes (re-validates the header,
- * grows device buffers if needed, uploads asynchronously on `stream`).
- * `data` must stay valid until the upload completes; pinned host memory makes
- * the upload asynchronous. */
+ * grows device buffers if needed, uploads asynchronously after the work
+ * queued on `stream`; every later decode of the handle waits for it).
+ * `data` must stay valid until the upload completes (the next decode or a
+ * synchronisation); pinned host memory makes the upload asynchronous.  A
+ * stream of about 3 million triangles or more goes up in four parts on a
+ * copy stream of the handle's, so that stride_decode_host can start each
+ * part of its decode as that part arrives. */
 int stride_reload(stride_handle* h, const uint8_t* data, size_t len, void* stream);
 
 int stride_info(const stride_handle* h, stride_info_t* info);
@@ -149,8 +153,10 @@ int stride_decode(stride_handle* h, void* stream, uint32_t* d_idx, float* d_pos,
  * the connectivity kernel ends, beside the vertex kernel (a fused launch
  * shape is replaced by the persistent two-kernel one for this call); from
  * about 3 million triangles the connectivity runs in four parts and each
- * part's triangles are copied as soon as it ends.  Pinned host buffers
- * make the copies asynchronous to the host.
+ * part's triangles are copied as soon as it ends, and after a
+ * stride_reload of such a stream (uploaded in the same parts) each part
+ * starts when its bytes are in.  Pinned host buffers make the copies
+ * asynchronous to the host.
  * Replaces decode_to_host (utils/paradelta_v5_cuda.py:714-718). */
 int stride_decode_host(stride_handle* h, void* stream, uint32_t* h_idx, float* h_pos);
 

@@ -184,43 +184,59 @@ struct stride_handle {
     bool cfg_set = false;               // stride_set_config called: keep cfg across reloads
     long long wait_clocks = 1ll << 31;  // DecodeArgs::wait_clocks of this handle's decodes
     uint32_t launch_smem = 0, launch_grid = 0;  // the last decode's main kernel
-    HostLink link;  // stride_decode_host
+    HostLink link;          // stride_decode_host, and a reload that uploads by parts
+    bool up_parts = false;  // the last reload uploaded by parts (link.bytes_in)
 };
+
+// A reload that uploaded by parts: the decode stream waits for all of it
+// (decodes that do not go by parts).
+static cudaError_t wait_upload(stride_handle* h, cudaStream_t s) {
+    return h->up_parts ? cudaStreamWaitEvent(s, h->link.bytes_in[kHostParts - 1], 0) : cudaSuccess;
+}
 
 namespace stride {
 
 static void for_link_events(HostLink& L, void (*f)(cudaEvent_t*, cudaError_t*), cudaError_t* e) {
-    for (cudaEvent_t* ev : {&L.conn_done, &L.vert_done, &L.scan_done, &L.prefix_in, &L.done, &L.copied[0], &L.copied[1]})
+    for (cudaEvent_t* ev : {&L.conn_done, &L.vert_done, &L.done, &L.copied[0], &L.copied[1], &L.before_up})
         f(ev, e);
-    for (cudaEvent_t& ev : L.part_done) f(&ev, e);
+    for (int p = 0; p < kHostParts; p++)
+        for (cudaEvent_t* ev : {&L.part_done[p], &L.scan_done[p], &L.end_in[p], &L.bytes_in[p]}) f(ev, e);
 }
 
 void host_link_free(HostLink& L) {
-    for (auto& c : L.copy)
-        if (c) cudaStreamDestroy(c), c = nullptr;
+    for (cudaStream_t* c : {&L.copy[0], &L.copy[1], &L.up})
+        if (*c) cudaStreamDestroy(*c), *c = nullptr;
     for_link_events(L, [](cudaEvent_t* ev, cudaError_t*) { if (*ev) cudaEventDestroy(*ev), *ev = nullptr; }, nullptr);
-    cudaFreeHost(L.h_prefix);
-    L.h_prefix = nullptr;
-    L.prefix_cap = 0;
+    cudaFreeHost(L.h_end);
+    L.h_end = nullptr;
     cudaFreeHost(L.h_status);
     L.h_status = nullptr;
 }
 
-static cudaError_t host_link_init(HostLink& L) {
+cudaError_t host_link_init(HostLink& L) {
     if (L.copy[0]) return cudaSuccess;
     cudaError_t e = cudaSuccess;
-    for (auto& c : L.copy)
-        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c, cudaStreamNonBlocking);
+    for (cudaStream_t* c : {&L.copy[0], &L.copy[1], &L.up})
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(c, cudaStreamNonBlocking);
     for_link_events(L, [](cudaEvent_t* ev, cudaError_t* err) {
         if (*err == cudaSuccess) *err = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
     }, &e);
     if (e == cudaSuccess) e = cudaHostAlloc(&L.h_status, sizeof(Status), cudaHostAllocDefault);
+    if (e == cudaSuccess) e = cudaHostAlloc(&L.h_end, kHostParts * sizeof(PartEnd), cudaHostAllocDefault);
     if (e != cudaSuccess) host_link_free(L);
     return e;
 }
 
+void host_part_groups(uint32_t total_meshlets, uint32_t* part_g) {
+    const uint32_t n_groups = (total_meshlets + 31u) / 32u;
+    const uint32_t n_win = (n_groups + 7u) / 8u;
+    for (int p = 0; p < kHostParts; p++)
+        part_g[p] = 8u * static_cast<uint32_t>(static_cast<uint64_t>(n_win) * p / kHostParts);
+    part_g[kHostParts] = n_groups;
+}
+
 int decode_to_host(HostLink& L, const DecodeArgs& a, LaunchCfg cfg, void* stream, uint64_t n_t, uint64_t n_v,
-                   uint32_t* h_idx, float* h_pos, uint32_t* bad, bool* ran) {
+                   uint32_t* h_idx, float* h_pos, const cudaEvent_t* bytes_in, uint32_t* bad, bool* ran) {
     *ran = false;
     cudaError_t e = host_link_init(L);
     if (e != cudaSuccess) return cuda_fail(e, "copy streams");
@@ -235,48 +251,52 @@ int decode_to_host(HostLink& L, const DecodeArgs& a, LaunchCfg cfg, void* stream
     };
     if (cfg.persistent == 2) cfg.persistent = 1;
     const size_t ib = 12 * n_t, pb = 12 * n_v;
-    const uint32_t n_groups = (a.total_meshlets + 31u) / 32u;
-    const uint32_t n_win = (n_groups + 7u) / 8u;
-    const bool parts = cfg.persistent < 2 && n_t >= kHostPartTris && n_win >= kHostParts;
-    size_t tri_at[kHostParts + 1] = {0};  // byte offsets of the parts' triangles
+    const bool parts = cfg.persistent < 2 && host_parts(n_t, a.total_meshlets);
     if (parts) {
+        // Part by part: its scan, the read-back of its end (the next part's
+        // first triangle row), its connectivity; then, once its end is
+        // known, the copy of its triangles, queued before the next part's
+        // kernels so that it starts as soon as the part's connectivity ends.
+        // A corrupt stream's ends are clamped (its status reports it).
         uint32_t part_g[kHostParts + 1];
-        void* cd[kHostParts];
-        for (int p = 0; p < kHostParts; p++) {
-            part_g[p] = 8u * static_cast<uint32_t>(static_cast<uint64_t>(n_win) * p / kHostParts);
-            cd[p] = L.part_done[p];
-        }
-        part_g[kHostParts] = n_groups;
-        if (L.prefix_cap < n_win) {
-            cudaFreeHost(L.h_prefix);
-            L.h_prefix = nullptr;
-            L.prefix_cap = 0;
-            if ((e = cudaHostAlloc(&L.h_prefix, n_win * sizeof(BlockPrefix), cudaHostAllocDefault)) != cudaSuccess)
-                return cuda_fail(e, "cudaHostAlloc(prefix)");
-            L.prefix_cap = n_win;
-        }
-        const int rc = enqueue_decode_parts(a, cfg, stream, part_g, kHostParts, L.scan_done, cd, L.vert_done);
-        if (rc) return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
-        // the parts' first triangle rows: the scan's block prefixes, read
-        // back while the first part runs
-        if ((e = cudaStreamWaitEvent(L.copy[1], L.scan_done, 0)) != cudaSuccess ||
-            (e = cudaMemcpyAsync(L.h_prefix, a.blk_prefix, n_win * sizeof(BlockPrefix), cudaMemcpyDeviceToHost,
-                                 L.copy[1])) != cudaSuccess ||
-            (e = cudaEventRecord(L.prefix_in, L.copy[1])) != cudaSuccess ||
-            (e = cudaEventSynchronize(L.prefix_in)) != cudaSuccess)
-            return bail(e, "decode to host: block prefixes");
-        // a corrupt stream's prefixes are clamped (its status reports it)
-        for (int p = 1; p < kHostParts; p++)
-            tri_at[p] = std::max(tri_at[p - 1], 12 * std::min<size_t>(L.h_prefix[part_g[p] / 8u].t, n_t));
-        tri_at[kHostParts] = ib;
-        // every part's triangles in order on the first copy stream
-        for (int p = 0; p < kHostParts && e == cudaSuccess; p++) {
-            if ((e = cudaStreamWaitEvent(L.copy[0], L.part_done[p], 0)) == cudaSuccess && tri_at[p + 1] > tri_at[p])
-                e = cudaMemcpyAsync(reinterpret_cast<uint8_t*>(h_idx) + tri_at[p],
-                                    reinterpret_cast<const uint8_t*>(a.idx) + tri_at[p], tri_at[p + 1] - tri_at[p],
+        host_part_groups(a.total_meshlets, part_g);
+        int rc = enqueue_parts_begin(a, cfg, stream);
+        size_t from = 0;
+        for (int p = 0; p < kHostParts && rc == STRIDE_OK && e == cudaSuccess; p++) {
+            rc = enqueue_part(a, cfg, stream, part_g[p], part_g[p + 1], p == 0, bytes_in ? bytes_in[p] : nullptr,
+                              L.scan_done[p], L.part_done[p]);
+            if (rc) break;
+            size_t to = ib;
+            if (p + 1 < kHostParts) {
+                const uint32_t last = part_g[p + 1] / 8u - 1u;  // the part's last window
+                if ((e = cudaStreamWaitEvent(L.copy[1], L.scan_done[p], 0)) != cudaSuccess ||
+                    (e = cudaMemcpyAsync(&L.h_end[p].prefix, a.blk_prefix + last, sizeof(BlockPrefix),
+                                         cudaMemcpyDeviceToHost, L.copy[1])) != cudaSuccess ||
+                    (e = cudaMemcpyAsync(&L.h_end[p].sums, a.blk_sums + last, sizeof(uint4), cudaMemcpyDeviceToHost,
+                                         L.copy[1])) != cudaSuccess ||
+                    (e = cudaEventRecord(L.end_in[p], L.copy[1])) != cudaSuccess ||
+                    (e = cudaEventSynchronize(L.end_in[p])) != cudaSuccess)
+                    break;
+                const PartEnd& pe = L.h_end[p];
+                to = std::max(from, 12 * std::min<size_t>(pe.prefix.t + pe.sums.y, n_t));
+            }
+            if ((e = cudaStreamWaitEvent(L.copy[0], L.part_done[p], 0)) == cudaSuccess && to > from)
+                e = cudaMemcpyAsync(reinterpret_cast<uint8_t*>(h_idx) + from,
+                                    reinterpret_cast<const uint8_t*>(a.idx) + from, to - from,
                                     cudaMemcpyDeviceToHost, L.copy[0]);
+            from = to;
+        }
+        if (rc == STRIDE_OK && e == cudaSuccess) rc = enqueue_parts_end(a, cfg, stream, L.vert_done);
+        if (e != cudaSuccess) return bail(e, "decode to host: parts");
+        if (rc) {
+            cudaStreamSynchronize(s);
+            cudaStreamSynchronize(L.copy[0]);
+            cudaStreamSynchronize(L.copy[1]);
+            return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
         }
     } else {
+        if (bytes_in && (e = cudaStreamWaitEvent(s, bytes_in[kHostParts - 1], 0)) != cudaSuccess)
+            return cuda_fail(e, "decode to host: upload");
         void* ev[4] = {nullptr, nullptr, L.conn_done, L.vert_done};
         const int rc = enqueue_decode(a, cfg, stream, ev);
         if (rc) return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
@@ -493,11 +513,50 @@ int stride_reload(stride_handle* h, const uint8_t* data, size_t len, void* strea
     if (!h->cfg_set) h->cfg = default_config(p.n_meshlets);
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaError_t e;
-    if ((e = cudaMemcpyAsync(h->d_blob, data, len, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
-        (e = cudaMemsetAsync(h->d_blob + len, 0, std::min<size_t>(h->cap_bytes - len, kBlobPad), s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(h->d_params, &h->params, sizeof(MeshParams), cudaMemcpyHostToDevice, s)) !=
+    const size_t pad = std::min<size_t>(h->cap_bytes - len, kBlobPad);
+    // an earlier upload by parts may still be writing the arena
+    if ((e = wait_upload(h, s)) != cudaSuccess) return cuda_fail(e, "stride_reload");
+    h->up_parts = false;
+    if (host_parts(p.n_t, p.n_meshlets) && host_link_init(h->link) == cudaSuccess) {
+        // A stream large enough for a host decode by parts goes up in the
+        // same parts (whole windows of meshlets, cut where the offset table
+        // says the part's first meshlet starts), one event per part, on
+        // the handle's upload stream after the work already queued on
+        // `stream` (a decode there may still read the arena).
+        uint32_t part_g[kHostParts + 1];
+        host_part_groups(p.n_meshlets, part_g);
+        size_t cut[kHostParts + 1];
+        cut[0] = 0;
+        cut[kHostParts] = len;
+        for (int q = 1; q < kHostParts; q++) {
+            const uint8_t* t = data + kHeaderBytes + 4ull * (32ull * part_g[q]);  // inside the table
+            const uint64_t bit = (uint64_t(t[0]) << 24) | (uint64_t(t[1]) << 16) | (uint64_t(t[2]) << 8) | t[3];
+            cut[q] = std::min(len, std::max(cut[q - 1], static_cast<size_t>((bit + 7) / 8)));
+        }
+        HostLink& L = h->link;
+        if ((e = cudaEventRecord(L.before_up, s)) != cudaSuccess || (e = cudaStreamWaitEvent(L.up, L.before_up, 0)))
+            return cuda_fail(e, "stride_reload");
+        // the mesh record first: a copy queued on `stream` would go after
+        // every part on the copy engine, and the first part's scan needs it
+        if ((e = cudaMemcpyAsync(h->d_params, &h->params, sizeof(MeshParams), cudaMemcpyHostToDevice, L.up)) !=
             cudaSuccess)
+            return cuda_fail(e, "stride_reload");
+        for (int q = 0; q < kHostParts; q++) {
+            if (cut[q + 1] > cut[q] &&
+                (e = cudaMemcpyAsync(h->d_blob + cut[q], data + cut[q], cut[q + 1] - cut[q], cudaMemcpyHostToDevice,
+                                     L.up)) != cudaSuccess)
+                return cuda_fail(e, "stride_reload");
+            if (q + 1 == kHostParts && (e = cudaMemsetAsync(h->d_blob + len, 0, pad, L.up)) != cudaSuccess)
+                return cuda_fail(e, "stride_reload");
+            if ((e = cudaEventRecord(L.bytes_in[q], L.up)) != cudaSuccess) return cuda_fail(e, "stride_reload");
+        }
+        h->up_parts = true;
+    } else if ((e = cudaMemcpyAsync(h->d_blob, data, len, cudaMemcpyHostToDevice, s)) != cudaSuccess ||
+               (e = cudaMemsetAsync(h->d_blob + len, 0, pad, s)) != cudaSuccess ||
+               (e = cudaMemcpyAsync(h->d_params, &h->params, sizeof(MeshParams), cudaMemcpyHostToDevice, s)) !=
+                   cudaSuccess) {
         return cuda_fail(e, "stride_reload");
+    }
     return STRIDE_OK;
 }
 
@@ -541,7 +600,9 @@ int stride_decode_timed(stride_handle* h, void* stream, uint32_t* d_idx, float* 
     cudaEvent_t ev[4];
     for (auto& e : ev) cudaEventCreate(&e);
     void* evp[4] = {ev[0], ev[1], ev[2], ev[3]};
-    int rc = enqueue_decode(handle_args(h, d_idx, d_pos, nullptr), h->cfg, stream, evp);
+    int rc = wait_upload(h, static_cast<cudaStream_t>(stream)) == cudaSuccess
+                 ? enqueue_decode(handle_args(h, d_idx, d_pos, nullptr), h->cfg, stream, evp)
+                 : STRIDE_ERR_CUDA;
     if (rc == STRIDE_OK) {
         last_launch(&h->launch_smem, &h->launch_grid);
         cudaEventRecord(h->done, static_cast<cudaStream_t>(stream));
@@ -565,6 +626,8 @@ int stride_decode(stride_handle* h, void* stream, uint32_t* d_idx, float* d_pos,
     if ((reinterpret_cast<uintptr_t>(d_idx) & 15u) || (reinterpret_cast<uintptr_t>(d_pos) & 3u) ||
         (reinterpret_cast<uintptr_t>(d_codes) & 3u))
         return fail(STRIDE_ERR_ARG, "index output must be 16-byte aligned, positions and codes 4-byte aligned");
+    if (wait_upload(h, static_cast<cudaStream_t>(stream)) != cudaSuccess)
+        return fail(STRIDE_ERR_CUDA, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     const int rc = enqueue_decode(handle_args(h, d_idx, d_pos, d_codes), h->cfg, stream);
     if (rc) return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     last_launch(&h->launch_smem, &h->launch_grid);
@@ -663,8 +726,14 @@ int stride_decode_host(stride_handle* h, void* stream, uint32_t* h_idx, float* h
     }
     uint32_t bad = 0;
     bool ran = false;
+    // after a reload by parts, each part of the decode starts when its
+    // bytes are in.  With a valid offset table a part's meshlets lie inside
+    // the bytes up to its cut; a table that decreases is rejected by the
+    // scan, whatever the bytes not yet in hold (which of its faults the
+    // error names can then differ from a decode after the whole upload)
+    const cudaEvent_t* bytes_in = h->up_parts ? h->link.bytes_in : nullptr;
     const int rc = decode_to_host(h->link, handle_args(h, h->d_idx, h->d_pos, nullptr), h->cfg, stream,
-                                  h->params.n_t, h->params.n_v, h_idx, h_pos, &bad, &ran);
+                                  h->params.n_t, h->params.n_v, h_idx, h_pos, bytes_in, &bad, &ran);
     if (!ran) return rc;
     h->launched = true;  // later status queries see this decode
     cudaEventRecord(h->done, static_cast<cudaStream_t>(stream));

@@ -261,7 +261,7 @@ int stride_batch_decode_to_host(stride_batch* b, void* stream, uint32_t* d_idx, 
     uint32_t bad = 0;
     bool ran = false;
     const int rc = decode_to_host(b->link, batch_args(b, d_idx, d_pos), b->cfg, stream, b->total_t, b->total_v,
-                                  h_idx, h_pos, &bad, &ran);
+                                  h_idx, h_pos, nullptr, &bad, &ran);
     if (!ran) return rc;
     b->launched = true;  // later status queries see this decode
     cudaEventRecord(b->done, static_cast<cudaStream_t>(stream));

@@ -167,12 +167,17 @@ int parse_header(const uint8_t* data, size_t len, MeshParams* p, char* why, size
 // kernel, after it, after the connectivity (or fused) kernel and after the
 // vertex kernel (right after the fused one).
 int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void* const* ev = nullptr);
-// The two-kernel decode with its connectivity in parts: the scan (then
-// `scan_done`), one connectivity launch per part of whole windows, part p
-// over groups [part_g[p], part_g[p + 1]) and followed by `conn_done[p]`,
-// then the vertex kernel over every group (then `vert_done`).
-int enqueue_decode_parts(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, const uint32_t* part_g,
-                         int n_parts, void* scan_done, void* const* conn_done, void* vert_done);
+// The two-kernel decode in parts of whole windows, enqueued on `stream`
+// as: enqueue_parts_begin; per part (groups [g0, g1), `first` for the
+// first), enqueue_part -- after `bytes_in` (when given: the part's bytes
+// are in the arena), the scan of its windows (then `scan_done`: their
+// block prefixes are final) and its connectivity (then `conn_done`);
+// enqueue_parts_end -- the vertex kernel over every group (then
+// `vert_done`).  Null events are skipped.
+int enqueue_parts_begin(const DecodeArgs& a, const LaunchCfg& cfg, void* stream);
+int enqueue_part(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, uint32_t g0, uint32_t g1, bool first,
+                 void* bytes_in, void* scan_done, void* conn_done);
+int enqueue_parts_end(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void* vert_done);
 // The launch shape a decode of this many meshlets takes unless one is set.
 LaunchCfg default_config(uint32_t total_meshlets);
 

@@ -34,24 +34,44 @@ const char* status_message(int code);
 constexpr int kHostParts = 4;
 constexpr uint64_t kHostPartTris = 3ull << 20;
 
+// The end of a part's windows: the last window's block prefix and sums
+// (their sum is the next part's first rows).
+struct PartEnd {
+    BlockPrefix prefix;
+    uint4 sums;
+};
+
 // Copy streams, events and pinned scratch of such decodes (one per handle
 // or batch; created on first use).
 struct HostLink {
     cudaStream_t copy[2] = {nullptr, nullptr};
-    cudaEvent_t conn_done = nullptr, vert_done = nullptr, scan_done = nullptr, prefix_in = nullptr, done = nullptr;
-    cudaEvent_t copied[2] = {nullptr, nullptr}, part_done[kHostParts] = {};
-    BlockPrefix* h_prefix = nullptr;  // the scan's block prefixes
-    uint32_t prefix_cap = 0;
-    Status* h_status = nullptr;       // the decode's status, copied out with the outputs
+    cudaStream_t up = nullptr;  // a handle's stream upload by parts
+    cudaEvent_t conn_done = nullptr, vert_done = nullptr, done = nullptr, copied[2] = {nullptr, nullptr};
+    cudaEvent_t part_done[kHostParts] = {}, scan_done[kHostParts] = {}, end_in[kHostParts] = {};
+    cudaEvent_t bytes_in[kHostParts] = {}, before_up = nullptr;
+    PartEnd* h_end = nullptr;   // pinned, kHostParts entries
+    Status* h_status = nullptr; // pinned: the decode's status, copied out with the outputs
 };
+cudaError_t host_link_init(HostLink& L);
 void host_link_free(HostLink& L);
 
+// Whether a decode of this many triangles and groups goes by parts.
+inline bool host_parts(uint64_t n_t, uint32_t total_meshlets) {
+    const uint32_t n_win = ((total_meshlets + 31u) / 32u + 7u) / 8u;
+    return n_t >= kHostPartTris && n_win >= static_cast<uint32_t>(kHostParts);
+}
+// Group bounds of the parts (kHostParts + 1 entries): whole windows.
+void host_part_groups(uint32_t total_meshlets, uint32_t* part_g);
+
 // Decode `a` (outputs at a.idx / a.pos, n_t and n_v rows) on `stream` and
-// copy both to h_idx / h_pos; returns when they are there.  *ran says
-// whether the decode ran to its end: then the result is its status code
-// (STRIDE_OK or the error, the failing meshlet in *bad, the message left
-// to the caller); otherwise a launch or copy failure, message recorded.
+// copy both to h_idx / h_pos; returns when they are there.  `bytes_in`,
+// when given (kHostParts events), says when each part's bytes are in the
+// arena (a decode by parts then starts each part when its bytes are).
+// *ran says whether the decode ran to its end: then the result is its
+// status code (STRIDE_OK or the error, the failing meshlet in *bad, the
+// message left to the caller); otherwise a launch or copy failure, message
+// recorded.
 int decode_to_host(HostLink& L, const DecodeArgs& a, LaunchCfg cfg, void* stream, uint64_t n_t, uint64_t n_v,
-                   uint32_t* h_idx, float* h_pos, uint32_t* bad, bool* ran);
+                   uint32_t* h_idx, float* h_pos, const cudaEvent_t* bytes_in, uint32_t* bad, bool* ran);
 
 }  // namespace stride

@@ -161,8 +161,11 @@ __device__ __forceinline__ void lut_block(const DecodeArgs& a, uint32_t b, uint3
     a.lut[P.lut_off + i] = stride_dequant(&P.dq[d], q);
 }
 
-// Blocks [0, nb) scan the meshlets; the blocks after them (lut_bx per mesh
-// with tables) fill the dequantisation tables in the same launch.
+// Blocks [0, nb) scan the meshlets of scan blocks b0 .. b0 + nb - 1; the
+// blocks after them (lut_bx per mesh with tables) fill the dequantisation
+// tables in the same launch.  A decode scans in one launch (b0 = 0, every
+// block) or in launches over consecutive block ranges, each continuing the
+// block prefixes of the ones before it.
 //
 // Slots: the decode kernels take meshlets in groups of 32 slots, one lane
 // each, and a warp runs as many token iterations as its longest meshlet.
@@ -170,7 +173,8 @@ __device__ __forceinline__ void lut_block(const DecodeArgs& a, uint32_t b, uint3
 // plus two per strip; ties by index) and slot i of the block holds the
 // meshlet of rank i, so a group's lanes have about the same work.  Outputs
 // are placed per meshlet, so the order changes no result.
-__global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a, uint32_t nb, uint32_t lut_bx) {
+__global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a, uint32_t b0, uint32_t nb,
+                                                             uint32_t lut_bx) {
     // The fused kernel may be scheduled once every block of this launch has
     // started (it waits for this grid's completion before it reads
     // anything): its launch latency then overlaps this kernel, and it never
@@ -185,7 +189,8 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a, uint32
     __shared__ uint32_t sslot[kScanThreads];
     __shared__ int is_last;
     const uint32_t tid = threadIdx.x;
-    const uint32_t m = blockIdx.x * kScanThreads + tid;
+    const uint32_t blk = b0 + blockIdx.x;
+    const uint32_t m = blk * kScanThreads + tid;
     uint32_t nl = 0u, nt = 0u;
     MeshletDesc d;
     memset(&d, 0, sizeof(d));
@@ -219,7 +224,7 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a, uint32
         }
         sslot[rank] = tid;
         __syncthreads();
-        d.slot_meshlet = blockIdx.x * kScanThreads + sslot[tid];
+        d.slot_meshlet = blk * kScanThreads + sslot[tid];
     }
     if (m < a.total_meshlets) {
         d.v_pref = static_cast<uint32_t>(e1);
@@ -233,19 +238,27 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a, uint32
         dst[3] = src[3];
     }
     if (tid == 0)
-        a.blk_sums[blockIdx.x] = make_uint4(static_cast<uint32_t>(t1), static_cast<uint32_t>(t1 >> 32),
-                                            static_cast<uint32_t>(t2), 0u);
-    // The last block to finish turns the block sums into block prefixes.
+        a.blk_sums[blk] = make_uint4(static_cast<uint32_t>(t1), static_cast<uint32_t>(t1 >> 32),
+                                     static_cast<uint32_t>(t2), 0u);
+    // The last block to finish turns the block sums into block prefixes
+    // (the ticket counts the blocks of this decode's scan launches so far).
     __threadfence();
     __syncthreads();
-    if (tid == 0) is_last = atomicAdd(&a.status->ticket, 1u) == nb - 1u;
+    if (tid == 0) is_last = atomicAdd(&a.status->ticket, 1u) == b0 + nb - 1u;
     __syncthreads();
     if (!is_last) return;
     __threadfence();
     unsigned long long cv = 0ull, ct = 0ull, cw = 0ull;
+    if (b0) {  // the totals of the blocks before this launch's
+        const BlockPrefix* pp = a.blk_prefix + b0 - 1u;
+        const uint4 q = __ldcg(a.blk_sums + b0 - 1u);
+        cv = __ldcg(&pp->v) + q.x;
+        ct = __ldcg(&pp->t) + q.y;
+        cw = __ldcg(&pp->wp) + q.z;
+    }
     for (uint32_t base = 0; base < nb; base += kScanThreads) {
         const uint32_t i = base + tid;
-        const uint4 s = i < nb ? __ldcg(a.blk_sums + i) : make_uint4(0u, 0u, 0u, 0u);
+        const uint4 s = i < nb ? __ldcg(a.blk_sums + b0 + i) : make_uint4(0u, 0u, 0u, 0u);
         // per-chunk sums stay below 2^32 (256 blocks x 65536), so pack pairs
         unsigned long long ta, tb;
         const unsigned long long ea = block_scan((static_cast<unsigned long long>(s.y) << 32) | s.x, wsum, ta);
@@ -256,7 +269,7 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a, uint32
             p.t = ct + (ea >> 32);
             p.wp = cw + eb;
             p.pad = 0ull;
-            a.blk_prefix[i] = p;
+            a.blk_prefix[b0 + i] = p;
         }
         cv += ta & 0xFFFFFFFFull;
         ct += ta >> 32;
@@ -1262,14 +1275,15 @@ LaunchCfg default_config(uint32_t total_meshlets) {
 }
 
 namespace {
-// The scan kernel, with the blocks that fill the dequantisation tables.
-int launch_scan(const DecodeArgs& a, cudaStream_t s) {
-    const uint32_t nb = scan_blocks(a.total_meshlets);
+// The scan kernel over scan blocks [b0, b1), with the blocks that fill the
+// dequantisation tables when `tables`.
+int launch_scan(const DecodeArgs& a, cudaStream_t s, uint32_t b0, uint32_t b1, bool tables) {
+    const uint32_t nb = b1 - b0;
     const uint32_t lut_bx = (a.lut_max + 255u) / 256u;
-    const unsigned long long grid = nb + static_cast<unsigned long long>(a.n_lut_meshes) * lut_bx;
+    const unsigned long long grid = nb + (tables ? static_cast<unsigned long long>(a.n_lut_meshes) * lut_bx : 0ull);
     if (grid > 0x7FFFFFFFull) return STRIDE_ERR_UNSUPPORTED;
     if (grid) {
-        scan_kernel<<<static_cast<uint32_t>(grid), kScanThreads, 0, s>>>(a, nb, lut_bx);
+        scan_kernel<<<static_cast<uint32_t>(grid), kScanThreads, 0, s>>>(a, b0, nb, lut_bx);
         if (cudaGetLastError() != cudaSuccess) return STRIDE_ERR_CUDA;
     }
     return STRIDE_OK;
@@ -1281,7 +1295,7 @@ int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void
     if (check_config(cfg, a.wide_codes)) return STRIDE_ERR_ARG;
     if (cudaMemsetAsync(a.status, 0, sizeof(Status), s) != cudaSuccess) return STRIDE_ERR_CUDA;
     record(ev, 0, s);
-    const int rc = launch_scan(a, s);
+    const int rc = launch_scan(a, s, 0u, scan_blocks(a.total_meshlets), true);
     if (rc) return rc;
     record(ev, 1, s);
     if (a.total_meshlets != 0) {
@@ -1309,33 +1323,46 @@ int enqueue_decode(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void
     return STRIDE_OK;
 }
 
-int enqueue_decode_parts(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, const uint32_t* part_g,
-                         int n_parts, void* scan_done, void* const* conn_done, void* vert_done) {
-    if (cfg.persistent >= 2 || n_parts < 1) return STRIDE_ERR_ARG;
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
+int enqueue_parts_begin(const DecodeArgs& a, const LaunchCfg& cfg, void* stream) {
+    if (cfg.persistent >= 2) return STRIDE_ERR_ARG;
     if (check_config(cfg, a.wide_codes)) return STRIDE_ERR_ARG;
-    if (cudaMemsetAsync(a.status, 0, sizeof(Status), s) != cudaSuccess) return STRIDE_ERR_CUDA;
-    const int rc = launch_scan(a, s);
+    return cudaMemsetAsync(a.status, 0, sizeof(Status), static_cast<cudaStream_t>(stream)) == cudaSuccess
+               ? STRIDE_OK
+               : STRIDE_ERR_CUDA;
+}
+
+int enqueue_part(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, uint32_t g0, uint32_t g1, bool first,
+                 void* bytes_in, void* scan_done, void* conn_done) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (bytes_in && cudaStreamWaitEvent(s, static_cast<cudaEvent_t>(bytes_in), 0) != cudaSuccess)
+        return STRIDE_ERR_CUDA;
+    // the part's windows are its scan blocks
+    const uint32_t nb = scan_blocks(a.total_meshlets);
+    const uint32_t b0 = std::min(g0 / 8u, nb), b1 = std::max(b0, std::min((g1 + 7u) / 8u, nb));
+    const int rc = launch_scan(a, s, b0, b1, first);
     if (rc) return rc;
-    if (scan_done) cudaEventRecord(static_cast<cudaEvent_t>(scan_done), s);
-    for (int p = 0; p < n_parts; p++) {
-        DecodeArgs ap = a;
-        ap.conn_g0 = part_g[p];
-        ap.conn_g1 = part_g[p + 1];
-        cudaError_t e;
-        switch (cfg.warps_per_cta) {
-            case 1: e = launch_conn<conn_pairs(1)>(ap, cfg, s); break;
-            case 2: e = launch_conn<conn_pairs(2)>(ap, cfg, s); break;
-            default: e = launch_conn<conn_pairs(4)>(ap, cfg, s); break;
-        }
-        if (e != cudaSuccess) return STRIDE_ERR_CUDA;
-        if (conn_done && conn_done[p]) cudaEventRecord(static_cast<cudaEvent_t>(conn_done[p]), s);
+    if (scan_done && cudaEventRecord(static_cast<cudaEvent_t>(scan_done), s) != cudaSuccess) return STRIDE_ERR_CUDA;
+    DecodeArgs ap = a;
+    ap.conn_g0 = g0;
+    ap.conn_g1 = g1;
+    cudaError_t e;
+    switch (cfg.warps_per_cta) {
+        case 1: e = launch_conn<conn_pairs(1)>(ap, cfg, s); break;
+        case 2: e = launch_conn<conn_pairs(2)>(ap, cfg, s); break;
+        default: e = launch_conn<conn_pairs(4)>(ap, cfg, s); break;
     }
+    if (e != cudaSuccess) return STRIDE_ERR_CUDA;
+    if (conn_done && cudaEventRecord(static_cast<cudaEvent_t>(conn_done), s) != cudaSuccess) return STRIDE_ERR_CUDA;
+    return STRIDE_OK;
+}
+
+int enqueue_parts_end(const DecodeArgs& a, const LaunchCfg& cfg, void* stream, void* vert_done) {
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (a.total_meshlets != 0) {
         const cudaError_t e = a.wide_codes ? launch_vert<true>(a, cfg, s) : launch_vert<false>(a, cfg, s);
         if (e != cudaSuccess) return STRIDE_ERR_CUDA;
     }
-    if (vert_done) cudaEventRecord(static_cast<cudaEvent_t>(vert_done), s);
+    if (vert_done && cudaEventRecord(static_cast<cudaEvent_t>(vert_done), s) != cudaSuccess) return STRIDE_ERR_CUDA;
     return STRIDE_OK;
 }
 

@@ -80,22 +80,29 @@ def test_decode_to_host_and_device_agree(torch_cuda):
 def test_decode_to_host_pinned_overlap(torch_cuda, grid):
     """Pinned host outputs: the index copy runs beside the vertex kernel on
     the handle's copy streams (from about 3 M triangles, 1449^2 here, part by
-    part of the connectivity kernel); results equal the device decode bit
-    for bit."""
+    part of the connectivity kernel, and after a reload part by part of the
+    upload); results equal the device decode bit for bit."""
     torch = torch_cuda
     from meshpress_gb300 import ParaDeltaV5GpuDecoder
     V, T = synth.noise_heightfield(grid, seed=4)
     data = encoder.encode(V, T, precision_error=B12, precision_mode="bbox_frac").data
     dec = ParaDeltaV5GpuDecoder(data)
-    tris, verts = dec.decode_to_device()
+    tris, verts = (x.clone() for x in dec.decode_to_device())
     h_pos = torch.empty((dec.n_v_total, 3), dtype=torch.float32, pin_memory=True)
     h_idx = torch.empty((dec.n_t_total, 3), dtype=torch.int32, pin_memory=True)
-    for _ in range(3):
+    for reload in (False, False, True, True):
+        if reload:  # a large stream then goes up by parts, each decoded when its bytes are in
+            dec.reload(data)
         h_pos.fill_(float("nan"))
         h_idx.fill_(-1)
         pos, idx = dec.decode_to_host(out=(h_pos.numpy(), h_idx.numpy().view(np.uint32)))
         assert np.array_equal(pos.view(np.uint32), verts.cpu().numpy().view(np.uint32))
         assert np.array_equal(idx, tris.view(torch.int32).cpu().numpy().view(np.uint32))
+    # a device decode after such a reload waits for the whole upload
+    dec.reload(data)
+    t2, v2 = dec.decode_to_device()
+    assert torch.equal(t2.view(torch.int32), tris.view(torch.int32))
+    assert torch.equal(v2.view(torch.int32), verts.view(torch.int32))
     dec.close()
 
 
