@@ -254,6 +254,31 @@ def test_truncated_and_offset_corruption(torch_cuda):
     assert r is None and e.code == _lib.STRIDE_ERR_OFFSET
 
 
+def test_reloads_in_a_row(torch_cuda):
+    """Reloads without a decode between them: a large stream (uploaded by
+    parts on the handle's copy stream), then a small one (uploaded on the
+    decode stream, after the large one's parts), then the large one again;
+    each decode, to host or device, equals the oracle."""
+    from meshpress_gb300 import ParaDeltaV5GpuDecoder
+    V, T = synth.noise_heightfield(1449, seed=8)
+    big = encoder.encode(V, T, precision_error=B12, precision_mode="bbox_frac").data
+    small = _golden.load("grid129_b12")["data"]
+    dec = ParaDeltaV5GpuDecoder(small)
+    for seq in ([big, small], [small, big], [big, big]):
+        for data in seq:
+            dec.reload(data)
+        last = seq[-1]
+        opos, oidx = oracle.decode_mt(last, 0)
+        pos, idx = dec.decode_to_host()
+        assert np.array_equal(pos.view(np.uint32), opos.view(np.uint32))
+        assert np.array_equal(idx.astype(np.int64), oidx)
+        dec.reload(last)
+        tris, verts = dec.decode_to_device()
+        assert np.array_equal(verts.cpu().numpy().view(np.uint32), opos.view(np.uint32))
+        assert np.array_equal(tris.view(torch_cuda.int32).cpu().numpy().astype(np.int64), oidx)
+    dec.close()
+
+
 @pytest.mark.parametrize("grid", [129, 1449])
 def test_decode_to_host_reports_corruption(torch_cuda, grid):
     """A shifted offset-table entry in the last quarter of the meshlets (the
