@@ -242,9 +242,15 @@ __global__ void __launch_bounds__(kScanThreads) scan_kernel(DecodeArgs a, uint32
                                      static_cast<uint32_t>(t2), 0u);
     // The last block to finish turns the block sums into block prefixes
     // (the ticket counts the blocks of this decode's scan launches so far).
-    __threadfence();
+    // Only the block sum, thread 0's own write, is read inside this grid,
+    // so only thread 0 fences before taking its ticket (the descriptors are
+    // read by the next kernels); a fence on every thread made every block
+    // wait for its 16 KB of descriptors to reach L2.
     __syncthreads();
-    if (tid == 0) is_last = atomicAdd(&a.status->ticket, 1u) == b0 + nb - 1u;
+    if (tid == 0) {
+        __threadfence();
+        is_last = atomicAdd(&a.status->ticket, 1u) == b0 + nb - 1u;
+    }
     __syncthreads();
     if (!is_last) return;
     __threadfence();
