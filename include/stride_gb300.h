@@ -279,6 +279,11 @@ int stride_batch_decode_to_host(stride_batch* b, void* stream, uint32_t* d_idx, 
  * (pinned) host memory replaces every stream of the batch with one
  * asynchronous copy on `stream` through stride_batch_upload. */
 int stride_batch_image(const stride_batch* b, uint64_t* blob_offsets, uint64_t* image_bytes);
+/* The upload runs after the work queued on `stream`, and every later decode
+ * of the batch waits for it; `image` must stay valid until then.  A batch
+ * of about 3 million triangles or more goes up in four parts on a copy
+ * stream of the batch's, so that stride_batch_decode_to_host can start each
+ * part of its decode as that part arrives. */
 int stride_batch_upload(stride_batch* b, void* stream, const void* image, size_t bytes);
 /* Capture the decode sequence for these output pointers into a CUDA graph
  * (replaces any earlier graph) and replay it with stride_batch_launch_graph. */

@@ -39,8 +39,15 @@ struct stride_batch {
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t done = nullptr;
     bool launched = false;
-    HostLink link;  // stride_batch_decode_to_host
+    HostLink link;          // stride_batch_decode_to_host, and an upload by parts
+    bool up_parts = false;  // the last stride_batch_upload went by parts (link.bytes_in)
 };
+
+// After an upload by parts, a decode that does not go by parts waits for
+// all of it.
+static cudaError_t batch_wait_upload(stride_batch* b, cudaStream_t s) {
+    return b->up_parts ? cudaStreamWaitEvent(s, b->link.bytes_in[kHostParts - 1], 0) : cudaSuccess;
+}
 
 namespace stride {
 
@@ -232,6 +239,8 @@ int stride_batch_decode(stride_batch* b, void* stream, uint32_t* d_idx, float* d
     if ((!d_idx && b->total_t) || (!d_pos && b->total_v)) return fail(STRIDE_ERR_ARG, "null output pointer");
     if ((reinterpret_cast<uintptr_t>(d_idx) & 15u) || (reinterpret_cast<uintptr_t>(d_pos) & 3u))
         return fail(STRIDE_ERR_ARG, "index output must be 16-byte aligned, positions 4-byte aligned");
+    if (batch_wait_upload(b, static_cast<cudaStream_t>(stream)) != cudaSuccess)
+        return fail(STRIDE_ERR_CUDA, "batch decode: %s", cudaGetErrorString(cudaGetLastError()));
     const int rc = enqueue_decode(batch_args(b, d_idx, d_pos), b->cfg, stream);
     if (rc) return fail(rc, "batch decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
     cudaError_t e = cudaEventRecord(b->done, static_cast<cudaStream_t>(stream));
@@ -260,8 +269,9 @@ int stride_batch_decode_to_host(stride_batch* b, void* stream, uint32_t* d_idx, 
         return fail(STRIDE_ERR_ARG, "index output must be 16-byte aligned, positions 4-byte aligned");
     uint32_t bad = 0;
     bool ran = false;
+    // after an upload by parts each part of the decode starts when its bytes are in
     const int rc = decode_to_host(b->link, batch_args(b, d_idx, d_pos), b->cfg, stream, b->total_t, b->total_v,
-                                  h_idx, h_pos, nullptr, &bad, &ran);
+                                  h_idx, h_pos, b->up_parts ? b->link.bytes_in : nullptr, &bad, &ran);
     if (!ran) return rc;
     b->launched = true;  // later status queries see this decode
     cudaEventRecord(b->done, static_cast<cudaStream_t>(stream));
@@ -281,8 +291,43 @@ int stride_batch_upload(stride_batch* b, void* stream, const void* image, size_t
     if (bytes != b->arena_bytes)
         return fail(STRIDE_ERR_ARG, "image is %zu bytes, the batch's arena %llu", bytes,
                     static_cast<unsigned long long>(b->arena_bytes));
-    const cudaError_t e =
-        cudaMemcpyAsync(b->d_arena, image, bytes, cudaMemcpyHostToDevice, static_cast<cudaStream_t>(stream));
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    cudaError_t e = batch_wait_upload(b, s);  // an earlier upload by parts may still be writing
+    if (e != cudaSuccess) return cuda_fail(e, "stride_batch_upload");
+    b->up_parts = false;
+    if (host_parts(b->total_t, b->total_meshlets) && host_link_init(b->link) == cudaSuccess) {
+        // As a handle's reload: the image goes up in the parts of a host
+        // decode, cut where the offset table of the mesh holding a part's
+        // first meshlet puts that meshlet, one event per part, on the
+        // batch's upload stream after the work already queued on `stream`.
+        const uint8_t* img = static_cast<const uint8_t*>(image);
+        uint32_t part_g[kHostParts + 1];
+        host_part_groups(b->total_meshlets, part_g);
+        size_t cut[kHostParts + 1];
+        cut[0] = 0;
+        cut[kHostParts] = bytes;
+        for (int q = 1; q < kHostParts; q++) {
+            const uint32_t m = 32u * part_g[q];
+            uint32_t i = 0;  // the mesh holding meshlet m
+            while (i + 1 < b->n_meshes && b->params[i + 1].meshlet_begin <= m) i++;
+            const MeshParams& P = b->params[i];
+            const uint8_t* t = img + P.blob_off + kHeaderBytes + 4ull * (m - P.meshlet_begin);  // its table
+            const uint64_t bit = (uint64_t(t[0]) << 24) | (uint64_t(t[1]) << 16) | (uint64_t(t[2]) << 8) | t[3];
+            cut[q] = std::min<size_t>(bytes, std::max<size_t>(cut[q - 1], P.blob_off + (bit + 7) / 8));
+        }
+        HostLink& L = b->link;
+        if ((e = cudaEventRecord(L.before_up, s)) != cudaSuccess || (e = cudaStreamWaitEvent(L.up, L.before_up, 0)))
+            return cuda_fail(e, "stride_batch_upload");
+        for (int q = 0; q < kHostParts; q++) {
+            if (cut[q + 1] > cut[q] && (e = cudaMemcpyAsync(b->d_arena + cut[q], img + cut[q], cut[q + 1] - cut[q],
+                                                            cudaMemcpyHostToDevice, L.up)) != cudaSuccess)
+                return cuda_fail(e, "stride_batch_upload");
+            if ((e = cudaEventRecord(L.bytes_in[q], L.up)) != cudaSuccess) return cuda_fail(e, "stride_batch_upload");
+        }
+        b->up_parts = true;
+        return STRIDE_OK;
+    }
+    e = cudaMemcpyAsync(b->d_arena, image, bytes, cudaMemcpyHostToDevice, s);
     return e == cudaSuccess ? STRIDE_OK : cuda_fail(e, "stride_batch_upload");
 }
 
@@ -293,7 +338,9 @@ int stride_batch_decode_timed(stride_batch* b, void* stream, uint32_t* d_idx, fl
     cudaEvent_t ev[4];
     for (auto& e : ev) cudaEventCreate(&e);
     void* evp[4] = {ev[0], ev[1], ev[2], ev[3]};
-    int rc = enqueue_decode(batch_args(b, d_idx, d_pos), b->cfg, stream, evp);
+    int rc = batch_wait_upload(b, static_cast<cudaStream_t>(stream)) == cudaSuccess
+                 ? enqueue_decode(batch_args(b, d_idx, d_pos), b->cfg, stream, evp)
+                 : STRIDE_ERR_CUDA;
     if (rc == STRIDE_OK) {
         cudaEventRecord(b->done, static_cast<cudaStream_t>(stream));
         b->launched = true;
@@ -346,7 +393,8 @@ int stride_batch_launch_graph(stride_batch* b, void* stream) {
     if (!b || !b->exec) return fail(STRIDE_ERR_ARG, "no captured graph");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     cudaError_t e;
-    if ((e = cudaGraphLaunch(b->exec, s)) != cudaSuccess) return cuda_fail(e, "cudaGraphLaunch");
+    if ((e = batch_wait_upload(b, s)) != cudaSuccess || (e = cudaGraphLaunch(b->exec, s)) != cudaSuccess)
+        return cuda_fail(e, "cudaGraphLaunch");
     if ((e = cudaEventRecord(b->done, s)) != cudaSuccess) return cuda_fail(e, "cudaEventRecord");
     b->launched = true;
     return STRIDE_OK;
@@ -357,6 +405,7 @@ int stride_batch_autotune(stride_batch* b, void* stream, uint32_t* d_idx, float*
     if (!b) return fail(STRIDE_ERR_ARG, "null batch");
     if (iters < 1) iters = 3;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (batch_wait_upload(b, s) != cudaSuccess) return fail(STRIDE_ERR_CUDA, "autotune: upload");
     std::vector<LaunchCfg> cands;
     // the vertex kernel stages half of stage_bytes
     const uint32_t stage_opts[] = {8u * 1024u, 10u * 1024u, 12u * 1024u, 16u * 1024u, 24u * 1024u};

@@ -158,6 +158,22 @@ def test_batch_decode_to_host(torch_cuda, mixed_streams, large_streams, which):
     assert np.array_equal(idx, ref_t.view(np.uint32)) and np.array_equal(pos.view(np.uint32), ref_v.view(np.uint32))
     if which == "large":
         _check_meshes(b, streams, torch.from_numpy(idx.view(np.int32)), torch.from_numpy(pos))
+        # an arena image then goes up by parts, each part decoded when its bytes are in
+        img = b.make_image()
+        h_img = torch.empty(img.size, dtype=torch.uint8, pin_memory=True)
+        h_img.numpy()[:] = img
+        for _ in range(2):
+            b.upload(h_img.data_ptr(), img.size)
+            h_pos.fill_(float("nan"))
+            h_idx.fill_(-1)
+            pos, idx = b.decode_to_host(out=(h_pos.numpy(), h_idx.numpy().view(np.uint32)))
+            assert np.array_equal(idx, ref_t.view(np.uint32))
+            assert np.array_equal(pos.view(np.uint32), ref_v.view(np.uint32))
+        # a device decode after such an upload waits for all of it
+        b.upload(h_img.data_ptr(), img.size)
+        tris, verts = b.decode()
+        assert np.array_equal(tris.cpu().numpy().view(np.uint32), ref_t.view(np.uint32))
+        assert np.array_equal(verts.cpu().numpy().view(np.uint32), ref_v.view(np.uint32))
     b.close()
 
 
