@@ -243,10 +243,13 @@ int decode_to_host(HostLink& L, const DecodeArgs& a, LaunchCfg cfg, void* stream
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     // a failure once work is queued: nothing may still run on the buffers
     // or write the host outputs when this returns
-    auto bail = [&](cudaError_t err, const char* what) {
+    auto drain = [&]() {
         cudaStreamSynchronize(s);
         cudaStreamSynchronize(L.copy[0]);
         cudaStreamSynchronize(L.copy[1]);
+    };
+    auto bail = [&](cudaError_t err, const char* what) {
+        drain();
         return cuda_fail(err, what);
     };
     if (cfg.persistent == 2) cfg.persistent = 1;
@@ -289,9 +292,7 @@ int decode_to_host(HostLink& L, const DecodeArgs& a, LaunchCfg cfg, void* stream
         if (rc == STRIDE_OK && e == cudaSuccess) rc = enqueue_parts_end(a, cfg, stream, L.vert_done);
         if (e != cudaSuccess) return bail(e, "decode to host: parts");
         if (rc) {
-            cudaStreamSynchronize(s);
-            cudaStreamSynchronize(L.copy[0]);
-            cudaStreamSynchronize(L.copy[1]);
+            drain();
             return fail(rc, "decode launch failed: %s", cudaGetErrorString(cudaGetLastError()));
         }
     } else {
